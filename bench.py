@@ -1,0 +1,344 @@
+"""Benchmark: multi-source BFS GTEPS on one GB300 (R-MAT scale 20, 512 sources).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Workload (the headline multi-source BFS configuration): undirected R-MAT,
+scale 20 (2^20 vertices), edge factor 16, (a,b,c,d) = (0.57,0.19,0.19,0.05),
+symmetrised, duplicates and self-loops removed, vertex labels permuted, seed 1;
+512 distinct sources drawn uniformly with seed 2; int32 distance rows.
+
+One step = one multi-source BFS over the 512 sources (one persistent kernel
+launch).  GTEPS counts, per source, the undirected edges of the component it
+reaches (Graph500 convention: sum over sources of scanned CSR entries / 2).
+
+ours:      `value`  -- device-resident inputs, CUDA events around K steps.
+           `e2e`    -- the C-ABI host-buffer call (gu_bfs_host): pinned host
+                       sources in, pinned host distance rows out, copies inside.
+reference: the oracle port of the reference CPU path
+           (examples/multi_search/multi_search_test.cu:17-38) on all host
+           threads, each step a bounded sample of the sources.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "graph-utils_gb300"))
+
+import numpy as np  # noqa: E402
+
+SCALE, EDGE_FACTOR, GRAPH_SEED, K_SOURCES, SOURCE_SEED = 20, 16, 1, 512, 2
+WORKLOAD = "rmat20_ef16_512src_bfs"
+FALLBACK_HBM_GBS = 6800.0
+
+
+def parse_args():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--variant", default="auto")
+    p.add_argument("--scale", type=int, default=SCALE)
+    p.add_argument("--sources", type=int, default=K_SOURCES)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--cpu-seconds", type=float, default=15.0, help="budget of the cpu_baseline sample")
+    p.add_argument("--kernel-only", action="store_true", help="skip e2e (for profiling runs)")
+    return p.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return FALLBACK_HBM_GBS, "fallback"
+
+
+def ncu_traffic_per_launch():
+    """dram bytes per launch of the dominant kernel, from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "ms_grid_kernel_auto_rmat20.md")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        if line.startswith("traffic_bytes_per_launch:"):
+            try:
+                return int(line.split(":", 1)[1].strip())
+            except ValueError:
+                return None
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        rows = []
+        try:
+            for line in open(self.path):
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        except OSError:
+            pass
+        finally:
+            try:
+                os.unlink(self.path)
+            except OSError:
+                pass
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+        sm = [num(r[1]) for r in rows if num(r[1]) is not None]
+        smax = [num(r[2]) for r in rows if num(r[2]) is not None]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def build_workload(scale, k):
+    import gu
+    hg = gu.HostGraph.rmat(scale, EDGE_FACTOR, 0.57, 0.19, 0.19, seed=GRAPH_SEED, permute=True)
+    srcs = gu.sources(hg.n, k, seed=SOURCE_SEED)
+    return hg, srcs
+
+
+def edges_and_bytes(torch, dist, deg, n):
+    """Per-source scanned CSR entries E_s and reached vertices V_s, on the GPU."""
+    INF = 2147483647
+    E = torch.zeros(dist.shape[0], dtype=torch.float64, device=dist.device)
+    V = torch.zeros(dist.shape[0], dtype=torch.float64, device=dist.device)
+    for b in range(0, dist.shape[0], 64):
+        reached = dist[b:b + 64] != INF
+        E[b:b + 64] = (reached.to(torch.float64) @ deg)
+        V[b:b + 64] = reached.sum(1).to(torch.float64)
+    E_tot = float(E.sum())
+    V_tot = float(V.sum())
+    # algorithmic bytes per source: 4n (distance row) + 8 V_s (R pairs) + 8 E_s (C + dist check)
+    alg_bytes = dist.shape[0] * 4.0 * n + 8.0 * V_tot + 8.0 * E_tot
+    return E_tot, V_tot, alg_bytes
+
+
+def cpu_sample(hg, srcs, seconds):
+    """Oracle port on all host threads over growing source samples until `seconds`."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    cores = os.cpu_count() or 1
+    done, edges, t_total = 0, 0, 0.0
+    chunk = cores
+    while done < len(srcs) and t_total < seconds:
+        part = srcs[done:done + chunk]
+        t0 = time.perf_counter()
+        _, scanned = oracle.bfs_multi(hg.R, hg.C, hg.n, part, nthreads=cores)
+        t_total += time.perf_counter() - t0
+        edges += scanned
+        done += len(part)
+    return edges / 2.0, t_total, done, cores
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    hg, srcs = build_workload(args.scale, args.sources)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    cores = os.cpu_count() or 1
+    per_step = cores  # one source per host thread per step
+    times, edges = [], []
+    off = 0
+    for i in range(args.warmup + args.steps):
+        part = np.take(srcs, np.arange(off, off + per_step) % len(srcs))
+        off += per_step
+        t0 = time.perf_counter()
+        _, scanned = oracle.bfs_multi(hg.R, hg.C, hg.n, part, nthreads=cores)
+        dt = time.perf_counter() - t0
+        if i >= args.warmup:
+            times.append(dt)
+            edges.append(scanned / 2.0)
+    T = sum(times)
+    value = sum(edges) / T / 1e9
+    sample = f"{per_step} sources per step ({cores} host threads), of the {args.sources} workload sources"
+    line = {"impl": "reference", "metric": "multi-source BFS GTEPS", "value": value, "unit": "GTEPS",
+            "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * T / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+            "data": "synthetic", "config": {"workload": WORKLOAD, "scale": args.scale, "edge_factor": EDGE_FACTOR,
+                                            "sources": args.sources, "graph_seed": GRAPH_SEED,
+                                            "source_seed": SOURCE_SEED},
+            "cpu_baseline": {"value": value, "unit": "GTEPS", "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": "GTEPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+    import gu
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+    hg, srcs = build_workload(args.scale, args.sources)
+    g = gu.Graph(hg)
+    stream = torch.cuda.Stream(device=dev)
+    s_dev = torch.as_tensor(srcs, device=dev)
+    dist_buf = torch.empty((len(srcs), hg.n), dtype=torch.int32, device=dev)
+    deg = torch.as_tensor(np.diff(hg.R).astype(np.float64), device=dev)
+
+    def step():
+        g.bfs(s_dev, dist_buf, variant=args.variant, stream=stream)
+
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            step()
+    torch.cuda.synchronize()
+    E_tot, V_tot, alg_bytes = edges_and_bytes(torch, dist_buf, deg, hg.n)
+    gteps_edges = E_tot / 2.0  # undirected graph: each edge once per reaching source
+
+    def barrier():
+        if ws > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    kernel_times = []
+    levels = None
+    with ClockSampler(local) as clk:
+        barrier()
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        for _ in range(args.steps):
+            step()
+            kt, td, bu, ml = g.last_launch()
+            kernel_times.append(kt)
+            levels = (td, bu, ml)
+        ev1.record(stream)
+        barrier()
+    clocks = clk.summary()
+    t_total = ev0.elapsed_time(ev1) / 1e3
+    if ws > 1:
+        t = torch.tensor([t_total], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        t_total = float(t.item())
+    value = ws * gteps_edges * args.steps / t_total / 1e9
+
+    e2e = None
+    if not args.kernel_only:
+        pin_src = torch.as_tensor(srcs).pin_memory()
+        pin_out = torch.empty((len(srcs), hg.n), dtype=torch.int32).pin_memory()
+        src_np, out_np = pin_src.numpy(), pin_out.numpy()
+        for _ in range(max(1, args.warmup // 2)):
+            g.bfs_host(src_np, args.variant, out=out_np, stream=stream)
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            g.bfs_host(src_np, args.variant, out=out_np, stream=stream)
+        barrier()
+        t_e2e = time.perf_counter() - t0
+        if ws > 1:
+            t = torch.tensor([t_e2e], device=dev)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            t_e2e = float(t.item())
+        ok = np.array_equal(out_np[:4], dist_buf[:4].cpu().numpy())
+        e2e = {"value": ws * gteps_edges * args.steps / t_e2e / 1e9, "unit": "GTEPS",
+               "h2d_bytes_per_step": int(srcs.nbytes), "d2h_bytes_per_step": int(len(srcs) * hg.n * 4),
+               "ms_per_step": 1e3 * t_e2e / args.steps, "host_rows_match_device": bool(ok)}
+
+    peak, peak_kind = peaks()
+    kt_avg = statistics.mean(kernel_times)
+    achieved = alg_bytes / kt_avg / 1e9
+    traffic = ncu_traffic_per_launch()
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": traffic, "peak_source": f"{peak_kind} hbm_gbs (MEASURED_PEAKS.json)" if
+                peak_kind == "measured" else "fallback 6800 GB/s",
+                "kernel": "gu::ms_grid_kernel<AUTO>", "kernel_ms": 1e3 * kt_avg,
+                "model": "per-source algorithmic bytes 4n + 8*V_s + 8*E_s summed over the 512 sources of the "
+                         "launch; the batched kernel shares CSR reads across 64 sources, so this effective "
+                         "fraction can exceed 1",
+                "physical_frac": (traffic / kt_avg / 1e9 / peak) if traffic else None}
+
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        e_cpu, t_cpu, nsrc, cores = cpu_sample(hg, srcs, args.cpu_seconds)
+        cpu = {"value": e_cpu / t_cpu / 1e9, "unit": "GTEPS", "cores": cores, "kind": "port",
+               "sample": f"first {nsrc} of the {len(srcs)} workload sources, oracle port of "
+                         f"multi_search_test.cu:17-38 on {cores} host threads, {t_cpu:.1f} s"}
+
+    if rank == 0:
+        line = {"metric": "multi-source BFS GTEPS", "value": value, "unit": "GTEPS", "n_gpus": ws,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_total / args.steps,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+                "data": "synthetic",
+                "config": {"workload": WORKLOAD, "scale": args.scale, "edge_factor": EDGE_FACTOR,
+                           "n": hg.n, "m_csr": hg.m, "sources": len(srcs), "graph_seed": GRAPH_SEED,
+                           "source_seed": SOURCE_SEED, "variant": args.variant,
+                           "l2": "inputs larger than L2 (CSR 134 MB + 2 GiB distance rows per step)",
+                           "edges_per_step": gteps_edges, "levels_td_bu_max": levels},
+                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
+                "gpu_launches": args.steps}
+        print(json.dumps(line), flush=True)
+    g.close()
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,372 @@
+// capi.cpp -- the extern "C" boundary declared in include/gu.h.
+//
+// Every entry point converts exceptions into a gu_status and a thread-local
+// message (the reference exits the process instead, util_device.cuh:10-22).
+#include "gu_internal.h"
+
+#include <climits>
+#include <cstring>
+#include <functional>
+#include <memory>
+
+namespace gu {
+DeviceGraph *create_device_graph(const int32_t *R, const int32_t *C, int32_t n, int64_t m, bool directed,
+                                 cudaStream_t stream);
+void msbfs_read_status(DeviceGraph &g, int *dev_err, int *td_levels, int *bu_levels, int *max_level);
+
+static thread_local std::string t_last_error;
+void set_last_error(const std::string &msg) { t_last_error = msg; }
+
+template <class F>
+static gu_status guarded(F &&fn)
+{
+    try {
+        fn();
+        return GU_OK;
+    } catch (const gu_error &e) {
+        set_last_error(e.what());
+        return e.code;
+    } catch (const std::bad_alloc &) {
+        set_last_error("host allocation failed");
+        return GU_ERR_OUT_OF_MEMORY;
+    } catch (const std::exception &e) {
+        set_last_error(e.what());
+        return GU_ERR_INTERNAL;
+    }
+}
+
+// Makes the graph's device current for the scope of a call.
+struct DeviceScope {
+    int prev = -1;
+    explicit DeviceScope(int dev)
+    {
+        GU_CUDA_CHECK(cudaGetDevice(&prev));
+        if (prev != dev) GU_CUDA_CHECK(cudaSetDevice(dev));
+    }
+    ~DeviceScope()
+    {
+        int cur = -1;
+        cudaGetDevice(&cur);
+        if (prev >= 0 && cur != prev) cudaSetDevice(prev);
+    }
+};
+
+static void check_dev_status(DeviceGraph &g, cudaStream_t stream)
+{
+    GU_CUDA_CHECK(cudaStreamSynchronize(stream));
+    GU_CUDA_CHECK(cudaGetLastError());
+    int err = 0;
+    msbfs_read_status(g, &err, nullptr, nullptr, nullptr);
+    if (err == DEV_ERR_BARRIER_TIMEOUT) throw gu_error(GU_ERR_TIMEOUT, "a device-side wait exceeded its limit");
+    if (err != 0) throw gu_error(GU_ERR_INTERNAL, "device reported error code " + std::to_string(err));
+}
+
+}  // namespace gu
+
+using namespace gu;
+
+struct gu_graph_s {
+    std::unique_ptr<DeviceGraph> g;
+};
+struct gu_hgraph_s {
+    HostGraph h;
+};
+struct gu_timer_s {
+    cudaEvent_t a = nullptr, b = nullptr;
+};
+
+extern "C" {
+
+int gu_version(void) { return 10000; }
+
+const char *gu_last_error(void) { return t_last_error.c_str(); }
+
+const char *gu_status_string(gu_status s)
+{
+    switch (s) {
+    case GU_OK: return "ok";
+    case GU_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case GU_ERR_CUDA: return "CUDA error";
+    case GU_ERR_OUT_OF_MEMORY: return "out of memory";
+    case GU_ERR_CAPACITY: return "capacity exceeded";
+    case GU_ERR_OVERFLOW: return "overflow";
+    case GU_ERR_TIMEOUT: return "device wait timed out";
+    case GU_ERR_UNSUPPORTED: return "unsupported";
+    case GU_ERR_INTERNAL: return "internal error";
+    }
+    return "unknown status";
+}
+
+gu_status gu_choose_device(int requested, int *chosen)
+{
+    return guarded([&] {
+        int count = 0;
+        GU_CUDA_CHECK(cudaGetDeviceCount(&count));
+        if (count < 1) throw gu_error(GU_ERR_CUDA, "no CUDA device");
+        int best = requested;
+        if (requested == -1) {
+            double best_bw = -1;
+            for (int d = 0; d < count; ++d) {
+                int clk = 0, bus = 0;
+                GU_CUDA_CHECK(cudaDeviceGetAttribute(&clk, cudaDevAttrMemoryClockRate, d));
+                GU_CUDA_CHECK(cudaDeviceGetAttribute(&bus, cudaDevAttrGlobalMemoryBusWidth, d));
+                const double bw = (double)clk * 1000.0 * (bus / 8) * 2 / 1e9;
+                if (bw > best_bw) {
+                    best_bw = bw;
+                    best = d;
+                }
+            }
+        } else if (requested < -1 || requested >= count) {
+            throw gu_error(GU_ERR_INVALID_ARGUMENT, "device index out of range 0.." + std::to_string(count - 1));
+        }
+        GU_CUDA_CHECK(cudaSetDevice(best));
+        if (chosen) *chosen = best;
+    });
+}
+
+gu_status gu_timer_start(void *stream, gu_timer *out)
+{
+    return guarded([&] {
+        if (!out) throw gu_error(GU_ERR_INVALID_ARGUMENT, "null timer");
+        std::unique_ptr<gu_timer_s> t(new gu_timer_s());
+        GU_CUDA_CHECK(cudaEventCreate(&t->a));
+        GU_CUDA_CHECK(cudaEventCreate(&t->b));
+        GU_CUDA_CHECK(cudaEventRecord(t->a, (cudaStream_t)stream));
+        *out = t.release();
+    });
+}
+
+gu_status gu_timer_stop(gu_timer t, void *stream, double *seconds)
+{
+    return guarded([&] {
+        if (!t) throw gu_error(GU_ERR_INVALID_ARGUMENT, "null timer");
+        std::unique_ptr<gu_timer_s> own(t);
+        GU_CUDA_CHECK(cudaEventRecord(t->b, (cudaStream_t)stream));
+        GU_CUDA_CHECK(cudaEventSynchronize(t->b));
+        float ms = 0;
+        GU_CUDA_CHECK(cudaEventElapsedTime(&ms, t->a, t->b));
+        cudaEventDestroy(t->a);
+        cudaEventDestroy(t->b);
+        if (seconds) *seconds = ms / 1000.0;
+    });
+}
+
+// ---- host graphs -----------------------------------------------------------------
+static gu_status make_hgraph(gu_hgraph *out, const std::function<HostGraph()> &fn)
+{
+    return guarded([&] {
+        if (!out) throw gu_error(GU_ERR_INVALID_ARGUMENT, "null output handle");
+        std::unique_ptr<gu_hgraph_s> h(new gu_hgraph_s());
+        h->h = fn();
+        *out = h.release();
+    });
+}
+
+gu_status gu_hgraph_rmat(int scale, int edge_factor, double a, double b, double c, uint64_t seed, int permute,
+                         gu_hgraph *out)
+{
+    return make_hgraph(out, [&] { return gen_rmat(scale, edge_factor, a, b, c, seed, permute != 0); });
+}
+
+gu_status gu_hgraph_er(int32_t n, int64_t m, uint64_t seed, gu_hgraph *out)
+{
+    return make_hgraph(out, [&] { return gen_er(n, m, seed); });
+}
+
+gu_status gu_hgraph_grid(int32_t rows, int32_t cols, double p_delete, uint64_t seed, gu_hgraph *out)
+{
+    return make_hgraph(out, [&] { return gen_grid(rows, cols, p_delete, seed); });
+}
+
+gu_status gu_hgraph_dag(int32_t n, int64_t m, uint64_t seed, gu_hgraph *out)
+{
+    return make_hgraph(out, [&] { return gen_dag(n, m, seed); });
+}
+
+gu_status gu_hgraph_from_edges(int32_t n, const int32_t *u, const int32_t *v, int64_t count, int symmetric,
+                               gu_hgraph *out)
+{
+    return make_hgraph(out, [&] {
+        if (n < 0 || count < 0 || (count > 0 && (!u || !v))) throw gu_error(GU_ERR_INVALID_ARGUMENT, "bad edge list");
+        std::vector<int32_t> eu(u, u + count), ev(v, v + count);
+        for (int64_t i = 0; i < count; ++i)
+            if (eu[i] < 0 || eu[i] >= n || ev[i] < 0 || ev[i] >= n)
+                throw gu_error(GU_ERR_INVALID_ARGUMENT, "edge endpoint out of range");
+        HostGraph g;
+        g.n = n;
+        g.directed = symmetric == 0;
+        build_csr(n, eu, ev, symmetric != 0, g.R, g.C);
+        return g;
+    });
+}
+
+gu_status gu_hgraph_arrays(gu_hgraph h, const int32_t **R, const int32_t **C, int32_t *n, int64_t *m, int *directed)
+{
+    return guarded([&] {
+        if (!h) throw gu_error(GU_ERR_INVALID_ARGUMENT, "null graph");
+        if (R) *R = h->h.R.data();
+        if (C) *C = h->h.C.data();
+        if (n) *n = h->h.n;
+        if (m) *m = h->h.m();
+        if (directed) *directed = h->h.directed ? 1 : 0;
+    });
+}
+
+gu_status gu_hgraph_destroy(gu_hgraph h)
+{
+    delete h;
+    return GU_OK;
+}
+
+gu_status gu_sources(int32_t n, int32_t k, uint64_t seed, int32_t *out_host)
+{
+    return guarded([&] {
+        if (!out_host && k > 0) throw gu_error(GU_ERR_INVALID_ARGUMENT, "null output");
+        std::vector<int32_t> s = gen_sources(n, k, seed);
+        std::memcpy(out_host, s.data(), sizeof(int32_t) * (size_t)k);
+    });
+}
+
+// ---- device graphs -------------------------------------------------------------
+gu_status gu_graph_create(const int32_t *R_host, const int32_t *C_host, int32_t n, int64_t m, int directed,
+                          void *stream, gu_graph *out)
+{
+    return guarded([&] {
+        if (!out) throw gu_error(GU_ERR_INVALID_ARGUMENT, "null output handle");
+        std::unique_ptr<gu_graph_s> h(new gu_graph_s());
+        h->g.reset(create_device_graph(R_host, C_host, n, m, directed != 0, (cudaStream_t)stream));
+        *out = h.release();
+    });
+}
+
+gu_status gu_graph_destroy(gu_graph g)
+{
+    return guarded([&] {
+        if (!g) return;
+        {
+            std::lock_guard<std::mutex> lk(g->g->mu);
+        }
+        delete g;
+    });
+}
+
+gu_status gu_graph_info(gu_graph g, int32_t *n, int64_t *m, int *directed, size_t *device_bytes)
+{
+    return guarded([&] {
+        if (!g) throw gu_error(GU_ERR_INVALID_ARGUMENT, "null graph");
+        if (n) *n = g->g->n;
+        if (m) *m = g->g->m;
+        if (directed) *directed = g->g->directed ? 1 : 0;
+        if (device_bytes) *device_bytes = g->g->bytes + g->g->ws.bytes;
+    });
+}
+
+gu_status gu_graph_last_launch(gu_graph g, double *kernel_seconds, int *td_levels, int *bu_levels, int *max_level)
+{
+    return guarded([&] {
+        if (!g) throw gu_error(GU_ERR_INVALID_ARGUMENT, "null graph");
+        DeviceGraph &dg = *g->g;
+        std::lock_guard<std::mutex> lk(dg.mu);
+        DeviceScope ds(dg.device);
+        if (!dg.timed) throw gu_error(GU_ERR_INVALID_ARGUMENT, "no launch recorded on this graph yet");
+        GU_CUDA_CHECK(cudaEventSynchronize(dg.ev_stop));
+        float ms = 0;
+        GU_CUDA_CHECK(cudaEventElapsedTime(&ms, dg.ev_start, dg.ev_stop));
+        if (kernel_seconds) *kernel_seconds = ms / 1000.0;
+        int err = 0, td = 0, bu = 0, ml = 0;
+        if (dg.ws.ptr) msbfs_read_status(dg, &err, &td, &bu, &ml);
+        if (td_levels) *td_levels = td;
+        if (bu_levels) *bu_levels = bu;
+        if (max_level) *max_level = ml;
+    });
+}
+
+gu_status gu_graph_arrays(gu_graph g, const int32_t **R_dev, const int32_t **C_dev, const int32_t **RT_dev,
+                          const int32_t **CT_dev)
+{
+    return guarded([&] {
+        if (!g) throw gu_error(GU_ERR_INVALID_ARGUMENT, "null graph");
+        if (R_dev) *R_dev = g->g->R;
+        if (C_dev) *C_dev = g->g->C;
+        if (RT_dev) *RT_dev = g->g->RT;
+        if (CT_dev) *CT_dev = g->g->CT;
+    });
+}
+
+// ---- BFS ---------------------------------------------------------------------------
+static void validate_sources_host(const int32_t *s, int32_t k, int32_t n)
+{
+    for (int32_t i = 0; i < k; ++i)
+        if (s[i] < 0 || s[i] >= n) throw gu_error(GU_ERR_INVALID_ARGUMENT, "source vertex out of range");
+}
+
+static void bfs_device(DeviceGraph &g, int variant, const int32_t *sources_dev, int32_t k, int32_t *dist_dev,
+                       int64_t ld, cudaStream_t stream)
+{
+    if (k == 0) return;
+    if (variant == GU_BFS_PLAIN) {
+        launch_plain_bfs(g, sources_dev, k, dist_dev, ld, stream);
+        GU_CUDA_CHECK(cudaStreamSynchronize(stream));
+        GU_CUDA_CHECK(cudaGetLastError());
+        return;
+    }
+    MsOptions opt;
+    opt.variant = variant;
+    launch_msbfs(g, sources_dev, k, dist_dev, ld, opt, stream, nullptr);
+    check_dev_status(g, stream);
+}
+
+static void check_bfs_args(gu_graph g, int variant, int32_t k, int64_t ld)
+{
+    if (!g) throw gu_error(GU_ERR_INVALID_ARGUMENT, "null graph");
+    if (variant < GU_BFS_AUTO || variant > GU_BFS_PLAIN) throw gu_error(GU_ERR_INVALID_ARGUMENT, "unknown BFS variant");
+    if (k < 0) throw gu_error(GU_ERR_INVALID_ARGUMENT, "k must be >= 0");
+    if (ld < g->g->n) throw gu_error(GU_ERR_INVALID_ARGUMENT, "ld must be >= n");
+}
+
+gu_status gu_bfs(gu_graph g, int variant, const int32_t *sources_dev, int32_t k, int32_t *dist_dev, int64_t ld,
+                 void *stream)
+{
+    return guarded([&] {
+        check_bfs_args(g, variant, k, ld);
+        if (k > 0 && (!sources_dev || !dist_dev)) throw gu_error(GU_ERR_INVALID_ARGUMENT, "null device buffer");
+        DeviceGraph &dg = *g->g;
+        std::lock_guard<std::mutex> lk(dg.mu);
+        DeviceScope ds(dg.device);
+        // validate sources on the host side of the boundary (a bad id would index out of bounds)
+        std::vector<int32_t> hs((size_t)k);
+        if (k > 0) {
+            GU_CUDA_CHECK(cudaMemcpyAsync(hs.data(), sources_dev, sizeof(int32_t) * (size_t)k, cudaMemcpyDeviceToHost,
+                                          (cudaStream_t)stream));
+            GU_CUDA_CHECK(cudaStreamSynchronize((cudaStream_t)stream));
+        }
+        validate_sources_host(hs.data(), k, dg.n);
+        bfs_device(dg, variant, sources_dev, k, dist_dev, ld, (cudaStream_t)stream);
+    });
+}
+
+gu_status gu_bfs_host(gu_graph g, int variant, const int32_t *sources_host, int32_t k, int32_t *dist_host, int64_t ld,
+                      void *stream)
+{
+    return guarded([&] {
+        check_bfs_args(g, variant, k, ld);
+        if (k > 0 && (!sources_host || !dist_host)) throw gu_error(GU_ERR_INVALID_ARGUMENT, "null host buffer");
+        DeviceGraph &dg = *g->g;
+        validate_sources_host(sources_host, k, dg.n);
+        std::lock_guard<std::mutex> lk(dg.mu);
+        DeviceScope ds(dg.device);
+        cudaStream_t st = (cudaStream_t)stream;
+        if (k == 0) return;
+        const size_t src_bytes = ((sizeof(int32_t) * (size_t)k + 255) / 256) * 256;
+        char *io = (char *)dg.io.get(src_bytes + sizeof(int32_t) * (size_t)k * (size_t)dg.n);
+        int32_t *d_src = reinterpret_cast<int32_t *>(io);
+        int32_t *d_dist = reinterpret_cast<int32_t *>(io + src_bytes);
+        GU_CUDA_CHECK(cudaMemcpyAsync(d_src, sources_host, sizeof(int32_t) * (size_t)k, cudaMemcpyHostToDevice, st));
+        bfs_device(dg, variant, d_src, k, d_dist, dg.n, st);
+        GU_CUDA_CHECK(cudaMemcpy2DAsync(dist_host, sizeof(int32_t) * (size_t)ld, d_dist, sizeof(int32_t) * (size_t)dg.n,
+                                        sizeof(int32_t) * (size_t)dg.n, (size_t)k, cudaMemcpyDeviceToHost, st));
+        GU_CUDA_CHECK(cudaStreamSynchronize(st));
+    });
+}
+
+}  // extern "C"

@@ -1,0 +1,157 @@
+// graph.cu -- the device-resident graph (replaces device_graph, device_graph.h:7-22
+// and device_graph.cpp:3-14) and its workspace.
+//
+// Layout in HBM: R (n+1 int32), C (m int32), both from cudaMalloc (256-byte
+// aligned); for directed graphs the in-edge CSR RT/CT (bottom-up levels pull
+// over in-edges), for undirected graphs RT/CT alias R/C.  The COO source array F
+// (device_graph's F) is built on the device on first use by the edge-parallel
+// variant instead of being copied with every graph.
+#include "device_utils.cuh"
+#include "gu_internal.h"
+
+#include <memory>
+
+namespace gu {
+
+int device_sm_count(int device)
+{
+    int sms = 0;
+    GU_CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+    return sms;
+}
+
+void *Workspace::get(size_t need)
+{
+    if (need <= bytes && ptr) return ptr;
+    if (ptr) {
+        GU_CUDA_CHECK(cudaDeviceSynchronize());
+        GU_CUDA_CHECK(cudaFree(ptr));
+        ptr = nullptr;
+        bytes = 0;
+    }
+    size_t want = need + need / 8;
+    cudaError_t e = cudaMalloc(&ptr, want);
+    if (e != cudaSuccess) {
+        (void)cudaGetLastError();
+        ptr = nullptr;
+        e = cudaMalloc(&ptr, need);
+        if (e != cudaSuccess) {
+            (void)cudaGetLastError();
+            ptr = nullptr;
+            throw gu_error(GU_ERR_OUT_OF_MEMORY, "workspace allocation of " + std::to_string(need) + " bytes failed");
+        }
+        want = need;
+    }
+    bytes = want;
+    return ptr;
+}
+
+void Workspace::release()
+{
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    bytes = 0;
+}
+
+void DeviceGraph::mark_start(cudaStream_t s)
+{
+    if (!ev_start) {
+        GU_CUDA_CHECK(cudaEventCreate(&ev_start));
+        GU_CUDA_CHECK(cudaEventCreate(&ev_stop));
+    }
+    GU_CUDA_CHECK(cudaEventRecord(ev_start, s));
+}
+
+void DeviceGraph::mark_stop(cudaStream_t s)
+{
+    GU_CUDA_CHECK(cudaEventRecord(ev_stop, s));
+    timed = true;
+}
+
+DeviceGraph::~DeviceGraph()
+{
+    int prev = -1;
+    cudaGetDevice(&prev);
+    cudaSetDevice(device);
+    if (ev_start) cudaEventDestroy(ev_start);
+    if (ev_stop) cudaEventDestroy(ev_stop);
+    ws.release();
+    io.release();
+    if (F) cudaFree(F);
+    if (RT && RT != R) cudaFree(RT);
+    if (CT && CT != C) cudaFree(CT);
+    if (R) cudaFree(R);
+    if (C) cudaFree(C);
+    if (prev >= 0) cudaSetDevice(prev);
+}
+
+__global__ void coo_from_csr_kernel(const int32_t *__restrict__ R, int32_t n, int32_t *__restrict__ F)
+{
+    // one warp per vertex, lanes fill its CSR range
+    const long long gw = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    for (long long v = gw; v < n; v += nw) {
+        const int32_t e1 = R[v + 1];
+        for (int32_t e = R[v] + lane; e < e1; e += 32) F[e] = (int32_t)v;
+    }
+}
+
+void ensure_coo(DeviceGraph &g, cudaStream_t stream)
+{
+    if (g.F || g.m == 0) return;
+    GU_CUDA_CHECK(cudaMalloc(&g.F, sizeof(int32_t) * (size_t)g.m));
+    g.bytes += sizeof(int32_t) * (size_t)g.m;
+    coo_from_csr_kernel<<<g.sm_count * 4, 256, 0, stream>>>(g.R, g.n, g.F);
+    GU_CUDA_CHECK(cudaGetLastError());
+}
+
+DeviceGraph *create_device_graph(const int32_t *R, const int32_t *C, int32_t n, int64_t m, bool directed,
+                                 cudaStream_t stream)
+{
+    if (n < 0) throw gu_error(GU_ERR_INVALID_ARGUMENT, "n must be >= 0");
+    if (m < 0 || m > INT32_MAX) throw gu_error(GU_ERR_INVALID_ARGUMENT, "m must be in [0, INT32_MAX]");
+    if (!R || (m > 0 && !C)) throw gu_error(GU_ERR_INVALID_ARGUMENT, "null CSR array");
+    if (R[0] != 0 || (int64_t)R[n] != m) throw gu_error(GU_ERR_INVALID_ARGUMENT, "R[0] must be 0 and R[n] must equal m");
+    int32_t maxdeg = 0;
+    for (int32_t v = 0; v < n; ++v) {
+        const int32_t d = R[v + 1] - R[v];
+        if (d < 0) throw gu_error(GU_ERR_INVALID_ARGUMENT, "R must be non-decreasing");
+        if (d > maxdeg) maxdeg = d;
+    }
+    for (int64_t e = 0; e < m; ++e)
+        if (C[e] < 0 || C[e] >= n) throw gu_error(GU_ERR_INVALID_ARGUMENT, "column index out of range");
+
+    std::unique_ptr<DeviceGraph> g(new DeviceGraph());
+    GU_CUDA_CHECK(cudaGetDevice(&g->device));
+    g->sm_count = device_sm_count(g->device);
+    g->n = n;
+    g->m = m;
+    g->directed = directed;
+    g->max_degree = maxdeg;
+    GU_CUDA_CHECK(cudaMalloc(&g->R, sizeof(int32_t) * ((size_t)n + 1)));
+    GU_CUDA_CHECK(cudaMalloc(&g->C, sizeof(int32_t) * (size_t)(m > 0 ? m : 1)));
+    GU_CUDA_CHECK(cudaMemcpyAsync(g->R, R, sizeof(int32_t) * ((size_t)n + 1), cudaMemcpyHostToDevice, stream));
+    if (m > 0) GU_CUDA_CHECK(cudaMemcpyAsync(g->C, C, sizeof(int32_t) * (size_t)m, cudaMemcpyHostToDevice, stream));
+    g->bytes = sizeof(int32_t) * ((size_t)n + 1 + (size_t)m);
+    if (directed) {
+        HostGraph h;
+        h.n = n;
+        h.R.assign(R, R + n + 1);
+        h.C.assign(C, C + m);
+        HostGraph t = transpose(h);
+        GU_CUDA_CHECK(cudaMalloc(&g->RT, sizeof(int32_t) * ((size_t)n + 1)));
+        GU_CUDA_CHECK(cudaMalloc(&g->CT, sizeof(int32_t) * (size_t)(m > 0 ? m : 1)));
+        GU_CUDA_CHECK(cudaMemcpyAsync(g->RT, t.R.data(), sizeof(int32_t) * ((size_t)n + 1), cudaMemcpyHostToDevice, stream));
+        if (m > 0) GU_CUDA_CHECK(cudaMemcpyAsync(g->CT, t.C.data(), sizeof(int32_t) * (size_t)m, cudaMemcpyHostToDevice, stream));
+        GU_CUDA_CHECK(cudaStreamSynchronize(stream));  // t goes out of scope
+        g->bytes *= 2;
+    } else {
+        g->RT = g->R;
+        g->CT = g->C;
+    }
+    GU_CUDA_CHECK(cudaStreamSynchronize(stream));
+    return g.release();
+}
+
+}  // namespace gu

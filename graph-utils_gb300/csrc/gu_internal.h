@@ -1,0 +1,114 @@
+// gu_internal.h -- internal host-side declarations shared by the library's
+// translation units (never installed; the public boundary is include/gu.h).
+#pragma once
+
+#include <cstdint>
+#include <cstddef>
+#include <mutex>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/gu.h"
+
+#ifdef __CUDACC__
+#include <cuda_runtime.h>
+#else
+#include <cuda_runtime_api.h>
+#endif
+
+namespace gu {
+
+// Device-side error codes written to a launch's control block.
+enum DevErr : int {
+    DEV_OK = 0,
+    DEV_ERR_BARRIER_TIMEOUT = 1,
+    DEV_ERR_QUEUE_OVERFLOW = 2,
+};
+
+struct gu_error : std::runtime_error {
+    gu_status code;
+    gu_error(gu_status c, const std::string &msg) : std::runtime_error(msg), code(c) {}
+};
+
+void set_last_error(const std::string &msg);
+
+#define GU_CUDA_CHECK(expr)                                                                          \
+    do {                                                                                             \
+        cudaError_t e__ = (expr);                                                                    \
+        if (e__ != cudaSuccess) {                                                                    \
+            throw ::gu::gu_error(e__ == cudaErrorMemoryAllocation ? GU_ERR_OUT_OF_MEMORY : GU_ERR_CUDA, \
+                                 std::string(#expr) + ": " + cudaGetErrorString(e__));               \
+        }                                                                                            \
+    } while (0)
+
+// Host CSR graph (the reference's host_graph, parse.h:15-35, without F; F is
+// derived on the device when a variant needs it).
+struct HostGraph {
+    int32_t n = 0;
+    bool directed = false;
+    std::vector<int32_t> R, C;
+    int64_t m() const { return (int64_t)C.size(); }
+};
+
+HostGraph gen_rmat(int scale, int edge_factor, double a, double b, double c, uint64_t seed, bool permute);
+HostGraph gen_er(int32_t n, int64_t m, uint64_t seed);
+HostGraph gen_grid(int32_t rows, int32_t cols, double p_delete, uint64_t seed);
+HostGraph gen_dag(int32_t n, int64_t m, uint64_t seed);
+std::vector<int32_t> gen_sources(int32_t n, int32_t k, uint64_t seed);
+HostGraph transpose(const HostGraph &g);
+void build_csr(int32_t n, const std::vector<int32_t> &eu, const std::vector<int32_t> &ev, bool symmetric,
+               std::vector<int32_t> &R, std::vector<int32_t> &C);
+
+// Device workspace: one allocation grown on demand, owned by a graph handle.
+struct Workspace {
+    void *ptr = nullptr;
+    size_t bytes = 0;
+    int device = -1;
+    void *get(size_t need);  // grows (synchronously) when needed
+    void release();
+};
+
+// Device-resident graph (the reference's device_graph, device_graph.h:7-22):
+// 256-byte-aligned int32 arrays in HBM.  RT/CT is the transposed (in-edge)
+// CSR, identical to R/C for undirected graphs.  F (COO source of every CSR
+// entry) is built on first use by the edge-parallel variant.
+struct DeviceGraph {
+    int device = 0;
+    int32_t n = 0;
+    int64_t m = 0;
+    bool directed = false;
+    int32_t *R = nullptr, *C = nullptr;
+    int32_t *RT = nullptr, *CT = nullptr;
+    int32_t *F = nullptr;
+    int32_t max_degree = 0;
+    size_t bytes = 0;
+    std::mutex mu;  // serialises calls on one handle (workspace reuse)
+    Workspace ws;  // kernel scratch
+    Workspace io;  // device staging for calls that take host buffers
+    int sm_count = 0;
+    // events bracketing the last main kernel launch (kernel-only timing)
+    cudaEvent_t ev_start = nullptr, ev_stop = nullptr;
+    bool timed = false;
+    void mark_start(cudaStream_t s);
+    void mark_stop(cudaStream_t s);
+    ~DeviceGraph();
+};
+
+// Per-call options of the batched multi-source engine.
+struct MsOptions {
+    int variant = GU_BFS_AUTO;
+    int batch_words = 1;  // 64-source words per batch
+    float alpha = 14.f;   // top-down -> bottom-up when frontier edges > unexplored / alpha
+    float beta = 24.f;    // bottom-up -> top-down when frontier vertices < n / beta
+};
+
+// Kernel launchers (device pointers, stream ordered; return after enqueue).
+void launch_msbfs(DeviceGraph &g, const int32_t *sources, int32_t k, int32_t *dist, int64_t ld,
+                  const MsOptions &opt, cudaStream_t stream, int *dev_err_out);
+void launch_plain_bfs(DeviceGraph &g, const int32_t *sources, int32_t k, int32_t *dist, int64_t ld,
+                      cudaStream_t stream);
+void ensure_coo(DeviceGraph &g, cudaStream_t stream);
+int device_sm_count(int device);
+
+}  // namespace gu

@@ -1,0 +1,220 @@
+"""ctypes binding of the graph-utils GB300 C ABI (include/gu.h).
+
+Host-side mirror of the reference's entry points for Python callers (tests,
+bench).  Device buffers are torch CUDA tensors (PyTorch is used for device
+memory and streams only); host buffers are numpy arrays.  The compute path is
+libgu_gb300.so; there is no fallback: loading fails loudly when the library is
+missing.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "lib", "libgu_gb300.so")
+
+OK = 0
+STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "out of memory", 4: "capacity exceeded",
+          5: "overflow", 6: "device wait timed out", 7: "unsupported", 8: "internal error"}
+
+BFS_AUTO, BFS_LINEAR, BFS_EDGE, BFS_WARP, BFS_CTA_WARP, BFS_SCAN, BFS_SHUFFLE, BFS_BOTTOM_UP, BFS_PLAIN = range(9)
+VARIANTS = {"auto": BFS_AUTO, "linear": BFS_LINEAR, "edge": BFS_EDGE, "warp": BFS_WARP,
+            "cta_warp": BFS_CTA_WARP, "scan": BFS_SCAN, "shuffle": BFS_SHUFFLE, "bottom_up": BFS_BOTTOM_UP,
+            "plain": BFS_PLAIN}
+UNREACHABLE = 2147483647
+
+_i32p = ctypes.POINTER(ctypes.c_int32)
+_i64p = ctypes.POINTER(ctypes.c_int64)
+_vp = ctypes.c_void_p
+
+
+class GuError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"{STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+_lib = None
+
+
+def lib():
+    """Load libgu_gb300.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise FileNotFoundError(f"{LIB_PATH} is missing: run __graft_entry__.build() first")
+    L = ctypes.CDLL(LIB_PATH)
+    sig = {
+        "gu_version": ([], ctypes.c_int),
+        "gu_last_error": ([], ctypes.c_char_p),
+        "gu_status_string": ([ctypes.c_int], ctypes.c_char_p),
+        "gu_choose_device": ([ctypes.c_int, ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
+        "gu_timer_start": ([_vp, ctypes.POINTER(_vp)], ctypes.c_int),
+        "gu_timer_stop": ([_vp, _vp, ctypes.POINTER(ctypes.c_double)], ctypes.c_int),
+        "gu_hgraph_rmat": ([ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                            ctypes.c_uint64, ctypes.c_int, ctypes.POINTER(_vp)], ctypes.c_int),
+        "gu_hgraph_er": ([ctypes.c_int32, ctypes.c_int64, ctypes.c_uint64, ctypes.POINTER(_vp)], ctypes.c_int),
+        "gu_hgraph_grid": ([ctypes.c_int32, ctypes.c_int32, ctypes.c_double, ctypes.c_uint64, ctypes.POINTER(_vp)],
+                           ctypes.c_int),
+        "gu_hgraph_dag": ([ctypes.c_int32, ctypes.c_int64, ctypes.c_uint64, ctypes.POINTER(_vp)], ctypes.c_int),
+        "gu_hgraph_from_edges": ([ctypes.c_int32, _i32p, _i32p, ctypes.c_int64, ctypes.c_int, ctypes.POINTER(_vp)],
+                                 ctypes.c_int),
+        "gu_hgraph_arrays": ([_vp, ctypes.POINTER(_i32p), ctypes.POINTER(_i32p), _i32p, _i64p,
+                              ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
+        "gu_hgraph_destroy": ([_vp], ctypes.c_int),
+        "gu_sources": ([ctypes.c_int32, ctypes.c_int32, ctypes.c_uint64, _i32p], ctypes.c_int),
+        "gu_graph_create": ([_i32p, _i32p, ctypes.c_int32, ctypes.c_int64, ctypes.c_int, _vp, ctypes.POINTER(_vp)],
+                            ctypes.c_int),
+        "gu_graph_destroy": ([_vp], ctypes.c_int),
+        "gu_graph_info": ([_vp, _i32p, _i64p, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_size_t)],
+                          ctypes.c_int),
+        "gu_graph_arrays": ([_vp, ctypes.POINTER(_vp), ctypes.POINTER(_vp), ctypes.POINTER(_vp),
+                             ctypes.POINTER(_vp)], ctypes.c_int),
+        "gu_graph_last_launch": ([_vp, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int),
+                                  ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
+        "gu_bfs": ([_vp, ctypes.c_int, _vp, ctypes.c_int32, _vp, ctypes.c_int64, _vp], ctypes.c_int),
+        "gu_bfs_host": ([_vp, ctypes.c_int, _i32p, ctypes.c_int32, _i32p, ctypes.c_int64, _vp], ctypes.c_int),
+    }
+    for name, (args, res) in sig.items():
+        fn = getattr(L, name)
+        fn.argtypes = args
+        fn.restype = res
+    _lib = L
+    return L
+
+
+def check(status):
+    if status != OK:
+        raise GuError(status, lib().gu_last_error().decode())
+
+
+def _ptr(a):
+    return a.ctypes.data_as(_i32p)
+
+
+class HostGraph:
+    """Host CSR (R, C as int32 numpy arrays), from a generator or arrays."""
+
+    def __init__(self, R, C, n, directed=False):
+        self.R = np.ascontiguousarray(R, dtype=np.int32)
+        self.C = np.ascontiguousarray(C, dtype=np.int32)
+        self.n = int(n)
+        self.m = int(self.C.shape[0])
+        self.directed = bool(directed)
+
+    @staticmethod
+    def _from_handle(h):
+        L = lib()
+        R, C = _i32p(), _i32p()
+        n, m, d = ctypes.c_int32(), ctypes.c_int64(), ctypes.c_int()
+        check(L.gu_hgraph_arrays(h, ctypes.byref(R), ctypes.byref(C), ctypes.byref(n), ctypes.byref(m),
+                                 ctypes.byref(d)))
+        Rn = np.ctypeslib.as_array(R, shape=(n.value + 1,)).copy()
+        Cn = np.ctypeslib.as_array(C, shape=(max(m.value, 1),))[: m.value].copy() if m.value else \
+            np.zeros(0, np.int32)
+        L.gu_hgraph_destroy(h)
+        return HostGraph(Rn, Cn, n.value, bool(d.value))
+
+    @staticmethod
+    def rmat(scale, edge_factor=16, a=0.57, b=0.19, c=0.19, seed=1, permute=True):
+        h = _vp()
+        check(lib().gu_hgraph_rmat(scale, edge_factor, a, b, c, seed, int(permute), ctypes.byref(h)))
+        return HostGraph._from_handle(h)
+
+    @staticmethod
+    def er(n, m, seed=1):
+        h = _vp()
+        check(lib().gu_hgraph_er(n, m, seed, ctypes.byref(h)))
+        return HostGraph._from_handle(h)
+
+    @staticmethod
+    def grid(rows, cols, p_delete=0.05, seed=7):
+        h = _vp()
+        check(lib().gu_hgraph_grid(rows, cols, p_delete, seed, ctypes.byref(h)))
+        return HostGraph._from_handle(h)
+
+    @staticmethod
+    def dag(n, m, seed=1):
+        h = _vp()
+        check(lib().gu_hgraph_dag(n, m, seed, ctypes.byref(h)))
+        return HostGraph._from_handle(h)
+
+    @staticmethod
+    def from_edges(n, u, v, symmetric=True):
+        u = np.ascontiguousarray(u, dtype=np.int32)
+        v = np.ascontiguousarray(v, dtype=np.int32)
+        h = _vp()
+        check(lib().gu_hgraph_from_edges(n, _ptr(u), _ptr(v), len(u), int(symmetric), ctypes.byref(h)))
+        return HostGraph._from_handle(h)
+
+    def degrees(self):
+        return np.diff(self.R)
+
+
+def sources(n, k, seed=2):
+    out = np.zeros(k, dtype=np.int32)
+    check(lib().gu_sources(n, k, seed, _ptr(out)))
+    return out
+
+
+def _stream_handle(stream):
+    if stream is None:
+        return None
+    if isinstance(stream, int):
+        return stream
+    return stream.cuda_stream  # torch.cuda.Stream
+
+
+class Graph:
+    """Device-resident graph (the reference's device_graph)."""
+
+    def __init__(self, hg, stream=None):
+        self.host = hg
+        self.n, self.m, self.directed = hg.n, hg.m, hg.directed
+        self._h = _vp()
+        check(lib().gu_graph_create(_ptr(hg.R), _ptr(hg.C) if hg.m else None, hg.n, hg.m, int(hg.directed),
+                                    _stream_handle(stream), ctypes.byref(self._h)))
+
+    def close(self):
+        if self._h:
+            lib().gu_graph_destroy(self._h)
+            self._h = _vp()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def device_bytes(self):
+        b = ctypes.c_size_t()
+        check(lib().gu_graph_info(self._h, None, None, None, ctypes.byref(b)))
+        return b.value
+
+    def last_launch(self):
+        """(kernel seconds, top-down levels, bottom-up levels, max level) of the last launch."""
+        t = ctypes.c_double()
+        td, bu, ml = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        check(lib().gu_graph_last_launch(self._h, ctypes.byref(t), ctypes.byref(td), ctypes.byref(bu),
+                                         ctypes.byref(ml)))
+        return t.value, td.value, bu.value, ml.value
+
+    def bfs(self, sources_dev, dist_dev, variant="auto", ld=None, stream=None):
+        """Device form: sources_dev (int32 cuda tensor, k), dist_dev (int32 cuda tensor, k x ld)."""
+        k = int(sources_dev.numel())
+        ld = self.n if ld is None else ld
+        check(lib().gu_bfs(self._h, VARIANTS[variant] if isinstance(variant, str) else variant,
+                           sources_dev.data_ptr(), k, dist_dev.data_ptr(), ld, _stream_handle(stream)))
+        return dist_dev
+
+    def bfs_host(self, sources_host, variant="auto", out=None, stream=None):
+        """Host form: numpy sources in, numpy k x n int32 distances out."""
+        s = np.ascontiguousarray(sources_host, dtype=np.int32)
+        k = len(s)
+        if out is None:
+            out = np.empty((k, self.n), dtype=np.int32)
+        check(lib().gu_bfs_host(self._h, VARIANTS[variant] if isinstance(variant, str) else variant, _ptr(s), k,
+                                out.ctypes.data_as(_i32p), out.shape[1], _stream_handle(stream)))
+        return out

@@ -1,0 +1,142 @@
+/*
+ * gu.h -- C ABI of graph-utils for GB300 (sm_103a).
+ *
+ * Drop-in boundary for the multi-source search hot path of graph-utils.  Plain
+ * pointers and sizes only.  Every call returns a gu_status (the reference calls
+ * exit() on any error, util_device.cuh:10-22); gu_last_error() gives the
+ * message of the last failing call on the calling thread.
+ *
+ * Pointer conventions: arguments named *_dev are device pointers on the graph's
+ * device and the call is ordered on `stream` (a cudaStream_t, NULL = legacy
+ * default stream); the call synchronises `stream` before returning so that a
+ * device-side failure is reported as a status.  Arguments named *_host are host
+ * pointers (pinned memory gives full copy bandwidth); the call copies them
+ * through the device inside the call, as the reference's *_setup functions do.
+ *
+ * Graph handles are thread-safe: concurrent calls on one handle are serialised.
+ */
+#ifndef GU_H
+#define GU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum gu_status {
+    GU_OK = 0,
+    GU_ERR_INVALID_ARGUMENT = 1,
+    GU_ERR_CUDA = 2,
+    GU_ERR_OUT_OF_MEMORY = 3,
+    GU_ERR_CAPACITY = 4,
+    GU_ERR_OVERFLOW = 5,
+    GU_ERR_TIMEOUT = 6,
+    GU_ERR_UNSUPPORTED = 7,
+    GU_ERR_INTERNAL = 8
+} gu_status;
+
+/* Breadth-first-search variants.  Each names the neighbour-gathering strategy
+ * of one reference kernel; all variants return identical distances.
+ *   LINEAR    thread per frontier vertex   (multi_search/linear_with_atomics.cu:42-159)
+ *   EDGE      sweep of all CSR entries     (multi_search/edge_parallel.cu:37-92)
+ *   WARP      warp strip-mining with race-and-resolve election
+ *                                          (multi_search/warp_based.cu:47-190)
+ *   CTA_WARP  CTA gathers degree > 2048, warps the rest (multi_search/CTA_warp.cu:42-289)
+ *   SCAN      block-scan ranked gather     (multi_search/scan_based.cu:43-194)
+ *   SHUFFLE   warp per vertex, dynamic queue (multi_search/shuffle_based.cuh:81-286)
+ *   BOTTOM_UP frontier bitmap pull (no reference counterpart)
+ *   AUTO      per-level direction and gather choice (autotuned)
+ *   PLAIN     one CTA per source, int32 distance row as the visited set -- the
+ *             reference's own structure, kept as the one-launch-per-request baseline.
+ * All but PLAIN run 64 sources per bitmap word in one persistent launch. */
+typedef enum gu_bfs_variant {
+    GU_BFS_AUTO = 0,
+    GU_BFS_LINEAR = 1,
+    GU_BFS_EDGE = 2,
+    GU_BFS_WARP = 3,
+    GU_BFS_CTA_WARP = 4,
+    GU_BFS_SCAN = 5,
+    GU_BFS_SHUFFLE = 6,
+    GU_BFS_BOTTOM_UP = 7,
+    GU_BFS_PLAIN = 8
+} gu_bfs_variant;
+
+#define GU_DIST_UNREACHABLE 2147483647 /* INT_MAX, as the reference (warp_based.cu:73) */
+
+typedef struct gu_graph_s *gu_graph;   /* device-resident graph */
+typedef struct gu_hgraph_s *gu_hgraph; /* host CSR graph (generators) */
+
+/* ---- library ------------------------------------------------------------ */
+int gu_version(void);
+const char *gu_last_error(void);
+const char *gu_status_string(gu_status s);
+
+/* Select a device: `requested` >= 0 selects it; -1 picks the device with the
+ * highest memory bandwidth.  Replaces choose_device (util_device.cu:23-76). */
+gu_status gu_choose_device(int requested, int *chosen);
+
+/* Stream-ordered interval timer on `stream`, in seconds; replaces
+ * start_clock/end_clock (util_device.cu:4-21). */
+typedef struct gu_timer_s *gu_timer;
+gu_status gu_timer_start(void *stream, gu_timer *out);
+gu_status gu_timer_stop(gu_timer t, void *stream, double *seconds); /* also frees t */
+
+/* ---- host graphs (generators; no reference counterpart) ------------------ */
+/* R-MAT: 2^scale vertices, edge_factor*2^scale edge draws, quadrant
+ * probabilities a,b,c (d = 1-a-b-c); symmetrised, duplicates and self-loops
+ * removed; permute != 0 relabels vertices by a seeded random permutation. */
+gu_status gu_hgraph_rmat(int scale, int edge_factor, double a, double b, double c, uint64_t seed,
+                         int permute, gu_hgraph *out);
+/* Erdos-Renyi G(n, m): m distinct undirected edges. */
+gu_status gu_hgraph_er(int32_t n, int64_t m, uint64_t seed, gu_hgraph *out);
+/* rows x cols 4-neighbour grid, each edge deleted with probability p_delete. */
+gu_status gu_hgraph_grid(int32_t rows, int32_t cols, double p_delete, uint64_t seed, gu_hgraph *out);
+/* Random DAG: m edge draws u -> v with u before v in a random topological order. */
+gu_status gu_hgraph_dag(int32_t n, int64_t m, uint64_t seed, gu_hgraph *out);
+/* CSR from an edge list (u[i], v[i]); symmetric != 0 adds both directions. */
+gu_status gu_hgraph_from_edges(int32_t n, const int32_t *u, const int32_t *v, int64_t count, int symmetric,
+                               gu_hgraph *out);
+gu_status gu_hgraph_arrays(gu_hgraph h, const int32_t **R, const int32_t **C, int32_t *n, int64_t *m,
+                           int *directed);
+gu_status gu_hgraph_destroy(gu_hgraph h);
+/* k distinct sources drawn uniformly without replacement from [0, n). */
+gu_status gu_sources(int32_t n, int32_t k, uint64_t seed, int32_t *out_host);
+
+/* ---- device graphs ------------------------------------------------------- */
+/* Copies the CSR (R: n+1 offsets, C: m neighbours, host pointers) to the
+ * current device.  Replaces device_graph::device_graph(const host_graph&)
+ * (device_graph.h:11, device_graph.cpp:3-14). */
+gu_status gu_graph_create(const int32_t *R_host, const int32_t *C_host, int32_t n, int64_t m, int directed,
+                          void *stream, gu_graph *out);
+gu_status gu_graph_destroy(gu_graph g);
+gu_status gu_graph_info(gu_graph g, int32_t *n, int64_t *m, int *directed, size_t *device_bytes);
+/* Device pointers of the resident CSR (R, C) and the in-edge CSR (RT, CT). */
+gu_status gu_graph_arrays(gu_graph g, const int32_t **R_dev, const int32_t **C_dev, const int32_t **RT_dev,
+                          const int32_t **CT_dev);
+
+/* Duration of the last search kernel launched on g (CUDA events on the call's
+ * stream, kernel only) and, for the batched engine, the number of top-down and
+ * bottom-up levels it ran and the deepest level reached.  Replaces the
+ * per-call timing prints of the reference's *_setup functions
+ * (e.g. shuffle_based.cu:42-44). */
+gu_status gu_graph_last_launch(gu_graph g, double *kernel_seconds, int *td_levels, int *bu_levels, int *max_level);
+
+/* ---- multi-source BFS ------------------------------------------------------ */
+/* Row i of dist (row stride ld >= n elements) receives the distances from
+ * sources[i]; GU_DIST_UNREACHABLE where unreachable.  Replaces
+ * multi_search_{linear_atomics,edge_parallel,warp_based,CTA_warp_based,
+ * scan_based,shuffle_based}_setup (linear_with_atomics.cuh:14,
+ * edge_parallel.cuh:13, warp_based.cuh:15, CTA_warp.cuh:15, scan_based.cuh:15,
+ * shuffle_based.cuh:16), which return the rows of the last #SM sources only;
+ * this call returns every row. */
+gu_status gu_bfs(gu_graph g, int variant, const int32_t *sources_dev, int32_t k, int32_t *dist_dev, int64_t ld,
+                 void *stream);
+gu_status gu_bfs_host(gu_graph g, int variant, const int32_t *sources_host, int32_t k, int32_t *dist_host,
+                      int64_t ld, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GU_H */

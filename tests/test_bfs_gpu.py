@@ -1,0 +1,144 @@
+"""Parity of the CUDA multi-source BFS (every variant) with the oracle.
+
+Distances must be bit-exact.  Small cases compare against the golden vectors
+of the reference's own checkers and against oracle/gu_oracle.c; the full-size
+R-MAT scale-20 case is checked through BFS certificates that hold at any size.
+"""
+import numpy as np
+import pytest
+
+import gu
+import oracle
+from conftest import golden_names, load_golden
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+VARIANTS = ["auto", "linear", "edge", "warp", "cta_warp", "scan", "shuffle", "bottom_up", "plain"]
+
+
+def run_bfs(g, srcs, variant, ld=None):
+    dev = torch.device("cuda:0")
+    s = torch.as_tensor(np.asarray(srcs, np.int32), device=dev)
+    ld = g.n if ld is None else ld
+    out = torch.full((max(len(srcs), 1), ld), -7, dtype=torch.int32, device=dev)
+    g.bfs(s, out, variant=variant, ld=ld)
+    torch.cuda.synchronize()
+    return out[: len(srcs), : g.n].cpu().numpy(), out.cpu().numpy()
+
+
+@pytest.fixture(scope="module")
+def golden_graphs():
+    out = {}
+    for name in golden_names():
+        d = load_golden(name)
+        hg = gu.HostGraph(d["R"], d["C"], int(d["n"]), bool(d["directed"]))
+        out[name] = (gu.Graph(hg), d)
+    return out
+
+
+@pytest.mark.parametrize("variant", VARIANTS)
+def test_golden_all_variants(golden_graphs, variant):
+    for name, (g, d) in golden_graphs.items():
+        got, _ = run_bfs(g, d["sources"], variant)
+        np.testing.assert_array_equal(got, d["dist"], err_msg=f"{name}/{variant}")
+
+
+@pytest.mark.parametrize("variant", VARIANTS)
+def test_rmat14_vs_oracle(variant):
+    hg = gu.HostGraph.rmat(14, 16, seed=9)
+    g = gu.Graph(hg)
+    srcs = gu.sources(hg.n, 150, seed=2)  # two full batches + a partial one
+    ref, _ = oracle.bfs_multi(hg.R, hg.C, hg.n, srcs, nthreads=8)
+    got, _ = run_bfs(g, srcs, variant)
+    np.testing.assert_array_equal(got, ref)
+
+
+@pytest.mark.parametrize("variant", ["auto", "linear", "scan", "bottom_up", "plain"])
+def test_grid_high_diameter_vs_oracle(variant):
+    hg = gu.HostGraph.grid(96, 80, 0.05, seed=7)
+    g = gu.Graph(hg)
+    srcs = gu.sources(hg.n, 70, seed=2)
+    ref, _ = oracle.bfs_multi(hg.R, hg.C, hg.n, srcs, nthreads=8)
+    got, _ = run_bfs(g, srcs, variant)
+    np.testing.assert_array_equal(got, ref)
+
+
+@pytest.mark.parametrize("variant", ["auto", "shuffle", "bottom_up", "edge"])
+def test_directed_dag_vs_oracle(variant):
+    hg = gu.HostGraph.dag(5000, 40000, seed=4)
+    g = gu.Graph(hg)
+    srcs = gu.sources(hg.n, 100, seed=2)
+    ref, _ = oracle.bfs_multi(hg.R, hg.C, hg.n, srcs, nthreads=8)
+    got, _ = run_bfs(g, srcs, variant)
+    np.testing.assert_array_equal(got, ref)
+
+
+def test_edge_cases():
+    hg = gu.HostGraph.rmat(10, 4, seed=3)  # has degree-0 vertices
+    g = gu.Graph(hg)
+    deg = hg.degrees()
+    zero = np.nonzero(deg == 0)[0]
+    assert len(zero) > 0
+    srcs = np.array([zero[0], 5, 5, zero[0], hg.n - 1, 0], np.int32)  # duplicates + isolated
+    ref, _ = oracle.bfs_multi(hg.R, hg.C, hg.n, srcs)
+    for v in VARIANTS:
+        got, full = run_bfs(g, srcs, v, ld=hg.n + 13)
+        np.testing.assert_array_equal(got, ref, err_msg=v)
+        assert np.all(full[:, hg.n:] == -7), "padding beyond n untouched"
+    # k = 0 is a no-op
+    s = torch.zeros(0, dtype=torch.int32, device="cuda")
+    out = torch.zeros((1, hg.n), dtype=torch.int32, device="cuda")
+    g.bfs(s, out)
+    # out-of-range source is rejected before any launch
+    s = torch.tensor([0, hg.n], dtype=torch.int32, device="cuda")
+    out = torch.zeros((2, hg.n), dtype=torch.int32, device="cuda")
+    with pytest.raises(gu.GuError) as e:
+        g.bfs(s, out)
+    assert e.value.status == 1
+
+
+def test_host_form_matches_device_form():
+    hg = gu.HostGraph.rmat(12, 16, seed=1)
+    g = gu.Graph(hg)
+    srcs = gu.sources(hg.n, 100, seed=5)
+    dev, _ = run_bfs(g, srcs, "auto")
+    host = g.bfs_host(srcs, "auto")
+    np.testing.assert_array_equal(dev, host)
+
+
+def test_rmat20_full_size_certificates():
+    """R-MAT scale 20, 512 sources: per-edge BFS certificates on the GPU plus
+    exact agreement with the oracle on a sample of rows."""
+    hg = gu.HostGraph.rmat(20, 16, seed=1)
+    g = gu.Graph(hg)
+    srcs = gu.sources(hg.n, 512, seed=2)
+    dev = torch.device("cuda:0")
+    s = torch.as_tensor(srcs, device=dev)
+    dist = torch.empty((512, hg.n), dtype=torch.int32, device=dev)
+    g.bfs(s, dist, variant="auto")
+    R = torch.as_tensor(hg.R.astype(np.int64), device=dev)
+    C = torch.as_tensor(hg.C.astype(np.int64), device=dev)
+    src_of = torch.repeat_interleave(torch.arange(hg.n, device=dev), R[1:] - R[:-1])
+    INF = gu.UNREACHABLE
+    B = 8
+    for b in range(0, 512, B):
+        d = dist[b:b + B]
+        du, dv = d[:, src_of], d[:, C]
+        fin_u, fin_v = du != INF, dv != INF
+        # an edge never joins reached and unreached vertices (undirected graph)
+        assert torch.equal(fin_u, fin_v)
+        # adjacent reached vertices differ by at most one level
+        diff = torch.where(fin_u, (du - dv).abs(), torch.zeros_like(du))
+        assert int(diff.max()) <= 1
+        # every reached non-source vertex has a neighbour one level closer
+        has = (fin_u & (du + 1 == dv)).to(torch.int32)
+        parent = torch.zeros_like(d).scatter_reduce_(1, C.unsqueeze(0).expand(B, -1), has, reduce="amax")
+        need = (d != INF) & (d > 0)
+        assert bool(((parent > 0) | ~need).all())
+        rows = torch.arange(b, b + B, device=dev)
+        assert bool((d[torch.arange(B, device=dev), s[rows].long()] == 0).all())
+        del du, dv, fin_u, fin_v, diff, has, parent
+    sample = [0, 1, 63, 64, 200, 511]
+    ref, _ = oracle.bfs_multi(hg.R, hg.C, hg.n, srcs[sample], nthreads=8)
+    np.testing.assert_array_equal(dist[sample].cpu().numpy(), ref)

@@ -1,0 +1,126 @@
+"""Host-side tests of the C ABI: symbols, status handling, generators.  No GPU."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+import gu
+import oracle
+from conftest import ROOT
+
+
+def declared_functions():
+    names = []
+    for h in sorted(os.listdir(os.path.join(ROOT, "include"))):
+        if not h.endswith(".h"):
+            continue
+        text = open(os.path.join(ROOT, "include", h)).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        names += re.findall(r"^\s*(?:[\w\*\s]+?)\b(gu_\w+)\s*\(", text, flags=re.M)
+    return sorted(set(names))
+
+
+def test_library_exports_every_declared_symbol():
+    L = gu.lib()
+    names = declared_functions()
+    assert len(names) >= 15
+    missing = [n for n in names if not hasattr(L, n)]
+    assert not missing, missing
+
+
+def test_version_and_status_strings():
+    L = gu.lib()
+    assert L.gu_version() >= 10000
+    assert L.gu_status_string(0) == b"ok"
+    assert L.gu_status_string(6) == b"device wait timed out"
+
+
+def test_invalid_arguments_report_status():
+    L = gu.lib()
+    h = ctypes.c_void_p()
+    st = L.gu_hgraph_er(1, 5, 1, ctypes.byref(h))
+    assert st == 1
+    assert b"n >= 2" in L.gu_last_error()
+    assert L.gu_hgraph_rmat(0, 16, 0.57, 0.19, 0.19, 1, 1, ctypes.byref(h)) == 1
+    assert L.gu_hgraph_rmat(10, 16, 0.7, 0.2, 0.2, 1, 1, ctypes.byref(h)) == 1
+    out = np.zeros(4, np.int32)
+    assert L.gu_sources(3, 4, 1, out.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))) == 1
+
+
+def _csr_ok(g):
+    assert g.R[0] == 0 and g.R[-1] == g.m
+    assert np.all(np.diff(g.R) >= 0)
+    for v in range(min(g.n, 2000)):
+        adj = g.C[g.R[v]:g.R[v + 1]]
+        assert np.all(np.diff(adj) > 0), "sorted, no duplicates"
+        assert not np.any(adj == v), "no self loops"
+
+
+def test_rmat_deterministic_and_symmetric():
+    a = gu.HostGraph.rmat(12, 16, seed=3)
+    b = gu.HostGraph.rmat(12, 16, seed=3)
+    c = gu.HostGraph.rmat(12, 16, seed=4)
+    np.testing.assert_array_equal(a.R, b.R)
+    np.testing.assert_array_equal(a.C, b.C)
+    assert not np.array_equal(a.C, c.C)
+    assert a.n == 4096 and not a.directed
+    _csr_ok(a)
+    src = np.repeat(np.arange(a.n), np.diff(a.R))
+    fwd = set(zip(src.tolist(), a.C.tolist()))
+    assert all((v, u) in fwd for (u, v) in list(fwd)[:5000])
+    # skewed degrees (R-MAT), 16*4096 draws minus duplicates
+    deg = a.degrees()
+    assert deg.max() > 20 * deg.mean()
+    assert 0.5 * 2 * 16 * 4096 < a.m <= 2 * 16 * 4096
+
+
+def test_er_exact_edge_count():
+    g = gu.HostGraph.er(198, 2742, seed=1)
+    assert g.n == 198 and g.m == 2 * 2742
+    _csr_ok(g)
+
+
+def test_grid_structure():
+    g = gu.HostGraph.grid(40, 30, 0.0, seed=7)
+    assert g.n == 1200 and g.m == 2 * (40 * 29 + 39 * 30)
+    h = gu.HostGraph.grid(40, 30, 0.05, seed=7)
+    removed = (g.m - h.m) // 2
+    assert 0 < removed < 0.12 * g.m / 2
+    assert h.degrees().max() <= 4
+    _csr_ok(h)
+
+
+def test_dag_is_acyclic():
+    g = gu.HostGraph.dag(500, 4000, seed=3)
+    assert g.directed
+    _csr_ok(g)
+    # Kahn's algorithm consumes every vertex
+    indeg = np.bincount(g.C, minlength=g.n)
+    stack = list(np.nonzero(indeg == 0)[0])
+    seen = 0
+    while stack:
+        v = stack.pop()
+        seen += 1
+        for w in g.C[g.R[v]:g.R[v + 1]]:
+            indeg[w] -= 1
+            if indeg[w] == 0:
+                stack.append(w)
+    assert seen == g.n
+
+
+def test_sources_distinct_deterministic():
+    a = gu.sources(1000, 300, seed=2)
+    b = gu.sources(1000, 300, seed=2)
+    np.testing.assert_array_equal(a, b)
+    assert len(set(a.tolist())) == 300 and a.min() >= 0 and a.max() < 1000
+
+
+def test_from_edges_matches_oracle_semantics():
+    u = np.array([0, 1, 2, 2, 3, 3, 0], np.int32)
+    v = np.array([1, 2, 0, 2, 4, 4, 1], np.int32)
+    g = gu.HostGraph.from_edges(6, u, v, symmetric=True)
+    assert g.m == 2 * 4  # (0,1),(1,2),(2,0),(3,4); self loop and duplicates dropped
+    d = oracle.bfs(g.R, g.C, g.n, 0)
+    assert d.tolist() == [0, 1, 1, oracle.INF, oracle.INF, oracle.INF]

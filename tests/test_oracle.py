@@ -1,0 +1,136 @@
+"""The CPU oracle against the golden vectors made by the reference's own code.
+
+Every golden file in tests/golden/ was produced by oracle/_ref/ref_oracle, i.e.
+the reference graph-utils checkers compiled from their sources (see
+tests/golden/make_golden.py).  These tests pin oracle/gu_oracle.c to them
+bit-for-bit before it is trusted as the parity checker of the CUDA path.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from conftest import golden_names, load_golden
+
+GRAPHS = golden_names()
+
+
+@pytest.mark.parametrize("name", GRAPHS)
+def test_bfs_matches_reference(name):
+    g = load_golden(name)
+    d, _ = oracle.bfs_multi(g["R"], g["C"], int(g["n"]), g["sources"])
+    np.testing.assert_array_equal(d, g["dist"])
+
+
+@pytest.mark.parametrize("name", GRAPHS)
+def test_bfs_multithreaded_same(name):
+    g = load_golden(name)
+    d, _ = oracle.bfs_multi(g["R"], g["C"], int(g["n"]), g["sources"], nthreads=4)
+    np.testing.assert_array_equal(d, g["dist"])
+
+
+@pytest.mark.parametrize("name", GRAPHS)
+def test_sigma_matches_reference(name):
+    g = load_golden(name)
+    d, s = oracle.sigma_multi(g["R"], g["C"], int(g["n"]), g["sources"])
+    np.testing.assert_array_equal(d, g["dist"])
+    np.testing.assert_array_equal(s, g["sigma"])
+
+
+@pytest.mark.parametrize("name", GRAPHS)
+def test_brandes_f32_bit_exact(name):
+    g = load_golden(name)
+    n = int(g["n"])
+    for i, s in enumerate(g["sources"]):
+        _, _, de = oracle.brandes(g["R"], g["C"], n, int(s), "f32")
+        np.testing.assert_array_equal(de.view(np.uint32), g["delta_f32"][i].view(np.uint32))
+
+
+@pytest.mark.parametrize("name", GRAPHS)
+def test_brandes_f64_close_to_reference_f32(name):
+    g = load_golden(name)
+    n = int(g["n"])
+    for i, s in enumerate(g["sources"][:40]):
+        _, _, de = oracle.brandes(g["R"], g["C"], n, int(s), "f64")
+        ref = g["delta_f32"][i].astype(np.float64)
+        np.testing.assert_allclose(de, ref, rtol=2e-5, atol=1e-5)
+
+
+@pytest.mark.parametrize("name", [n for n in GRAPHS if n not in ("test7", "dag300")])
+def test_pull_equals_push_on_undirected(name):
+    g = load_golden(name)
+    n = int(g["n"])
+    for s in g["sources"][:40]:
+        _, _, a = oracle.brandes(g["R"], g["C"], n, int(s), "f64")
+        _, _, b = oracle.brandes(g["R"], g["C"], n, int(s), "pull")
+        np.testing.assert_allclose(a, b, rtol=1e-13, atol=1e-13)
+
+
+@pytest.mark.parametrize("name", GRAPHS)
+def test_diameter_matches_reference(name):
+    g = load_golden(name)
+    assert oracle.diameter(g["R"], g["C"], int(g["n"]), g["sources"]) == int(g["diameter"])
+
+
+def test_dag_reachability_matches_reference():
+    for name in ("test7", "dag300"):
+        g = load_golden(name)
+        assert oracle.dag_reach_pairs(g["R"], g["C"], int(g["n"])) == int(g["dag_pairs"])
+
+
+@pytest.mark.parametrize("name", golden_names("lbs_"))
+def test_lbs_matches_reference(name):
+    g = load_golden(name, "lbs_")
+    scanned, result, total = oracle.lbs(g["counts"])
+    assert total == int(g["counts"].sum())
+    np.testing.assert_array_equal(scanned, g["scanned"])
+    np.testing.assert_array_equal(result, g["result"])
+
+
+def test_lbs_overflow_rejected():
+    with pytest.raises(ValueError):
+        oracle.lbs(np.full(4, 2**30, np.int32))
+
+
+def test_race_and_resolve_semantics():
+    assert oracle.race_and_resolve(0, 7) == 7
+    assert oracle.race_and_resolve(1, 5) == 0
+    assert oracle.race_and_resolve(0x80000001, 3) == 31
+    assert oracle.race_and_resolve(0b0110, 0) == 2
+
+
+def test_jazz_known_answers():
+    """Values of the reference checkers on graphs/jazz.graph (n=198)."""
+    g = load_golden("jazz")
+    n = int(g["n"])
+    reach = oracle.reach_count(g["R"], g["C"], n, np.arange(n))
+    assert reach == 39204
+    assert oracle.diameter(g["R"], g["C"], n, np.arange(n)) == 6
+    bc = oracle.bc(g["R"], g["C"], n, np.arange(n))
+    assert int(np.argmax(bc)) == 135
+    # the reference's FP32 deltas (golden) summed in double give exactly this value
+    d32 = g["delta_f32"].astype(np.float64)
+    bc32 = d32.sum(0) - np.diag(d32)
+    assert abs(bc32.max() - 5832.580306529999) < 1e-9
+    # the FP64 oracle differs from it by FP32 rounding only
+    assert abs(bc.max() - 5832.580306529999) / 5832.58 < 1e-7
+    np.testing.assert_allclose(bc, bc32, rtol=1e-5, atol=1e-6)
+
+
+def test_textbook_bc_maxima():
+    """test1..5 maxima of the all-source BC (ordered pairs, source excluded)."""
+    expect = {"test1": 38, "test2": 20, "test3": 7, "test4": 30, "test5": 18}
+    for name, mx in expect.items():
+        g = load_golden(name)
+        n = int(g["n"])
+        bc = oracle.bc(g["R"], g["C"], n, np.arange(n))
+        assert abs(bc.max() - mx) < 1e-9, (name, bc.max())
+
+
+def test_bc_threads_deterministic_and_close():
+    g = load_golden("er198")
+    n = int(g["n"])
+    a = oracle.bc(g["R"], g["C"], n, np.arange(n), nthreads=1)
+    b = oracle.bc(g["R"], g["C"], n, np.arange(n), nthreads=4)
+    c = oracle.bc(g["R"], g["C"], n, np.arange(n), nthreads=4)
+    np.testing.assert_array_equal(b, c)
+    np.testing.assert_allclose(a, b, rtol=1e-14)
