@@ -78,6 +78,7 @@ DeviceGraph::~DeviceGraph()
     ws.release();
     io.release();
     if (F) cudaFree(F);
+    if (heavy) cudaFree(heavy);
     if (RT && RT != R) cudaFree(RT);
     if (CT && CT != C) cudaFree(CT);
     if (R) cudaFree(R);
@@ -150,7 +151,27 @@ DeviceGraph *create_device_graph(const int32_t *R, const int32_t *C, int32_t n, 
         g->RT = g->R;
         g->CT = g->C;
     }
-    GU_CUDA_CHECK(cudaStreamSynchronize(stream));
+    {
+        // static list of heavy vertices by in-degree
+        std::vector<int32_t> heavy;
+        if (directed) {
+            std::vector<int32_t> indeg((size_t)n, 0);
+            for (int64_t e = 0; e < m; ++e) indeg[C[e]]++;
+            for (int32_t v = 0; v < n; ++v)
+                if (indeg[v] > BU_HEAVY_DEGREE) heavy.push_back(v);
+        } else {
+            for (int32_t v = 0; v < n; ++v)
+                if (R[v + 1] - R[v] > BU_HEAVY_DEGREE) heavy.push_back(v);
+        }
+        g->nheavy = (int32_t)heavy.size();
+        if (!heavy.empty()) {
+            GU_CUDA_CHECK(cudaMalloc(&g->heavy, sizeof(int32_t) * heavy.size()));
+            GU_CUDA_CHECK(cudaMemcpyAsync(g->heavy, heavy.data(), sizeof(int32_t) * heavy.size(),
+                                          cudaMemcpyHostToDevice, stream));
+            g->bytes += sizeof(int32_t) * heavy.size();
+        }
+        GU_CUDA_CHECK(cudaStreamSynchronize(stream));
+    }
     return g.release();
 }
 

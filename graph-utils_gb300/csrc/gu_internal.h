@@ -19,6 +19,8 @@
 
 namespace gu {
 
+constexpr int BU_HEAVY_DEGREE = 64;
+
 // Device-side error codes written to a launch's control block.
 enum DevErr : int {
     DEV_OK = 0,
@@ -82,6 +84,10 @@ struct DeviceGraph {
     int32_t *RT = nullptr, *CT = nullptr;
     int32_t *F = nullptr;
     int32_t max_degree = 0;
+    // vertices whose in-degree exceeds BU_HEAVY_DEGREE, ascending (bottom-up
+    // levels scan their in-edges with a whole warp instead of one thread)
+    int32_t *heavy = nullptr;
+    int32_t nheavy = 0;
     size_t bytes = 0;
     std::mutex mu;  // serialises calls on one handle (workspace reuse)
     Workspace ws;  // kernel scratch
@@ -99,7 +105,7 @@ struct DeviceGraph {
 struct MsOptions {
     int variant = GU_BFS_AUTO;
     int batch_words = 1;  // 64-source words per batch
-    float alpha = 14.f;   // top-down -> bottom-up when frontier edges > unexplored / alpha
+    float alpha = 2.f;    // top-down -> bottom-up when frontier out-edges > m / alpha
     float beta = 24.f;    // bottom-up -> top-down when frontier vertices < n / beta
 };
 

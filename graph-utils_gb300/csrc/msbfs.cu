@@ -1,57 +1,64 @@
 // msbfs.cu -- batched multi-source BFS on sm_103a.
 //
-// One persistent, cooperatively launched kernel runs every batch of 64 sources
-// and every level of each batch; levels are separated by a bounded grid barrier
+// One persistent, cooperatively launched kernel runs every batch of sources and
+// every level of each batch; levels are separated by a bounded grid barrier
 // (device_utils.cuh), so a whole multi-source search is a single launch.
 //
-// Per vertex the engine keeps one 32-byte record (one DRAM sector / L2 sector):
-//   seen  : sources that have reached the vertex in an earlier level
-//   f[3]  : frontier bitmaps F_j, rotating over three levels
-// Bit i of every word stands for source row0+i of the current batch.  For a
-// batch of 64 sources and n = 2^20 the records take 32 MiB and stay in the
-// 126 MiB L2, so the random per-edge accesses are L2 hits; DRAM traffic is the
-// streamed CSR plus the distance rows.
+// A batch holds 64*W sources (W 64-bit words, W in {1,2,4}).  Bit i of word q
+// of every per-vertex record stands for source row0 + 64q + i.  State, in SoA
+// layout with the W words of one vertex contiguous (16/32-byte vector access):
+//   seen[n][W]    sources that reached the vertex in an earlier level
+//   f[3][n][W]    frontier bitmaps F_j, rotating over three levels
+//   stamp[n]      last level that appended the vertex to a queue (W > 1)
+//   q[3], qoff[3] frontier queues; qoff[i] = out-edges of q[0..i) (an exclusive
+//                 prefix sum reserved together with the slot, so the next level
+//                 can split the frontier's edges evenly without a scan)
+// For n = 2^20 and W = 4 a frontier array is 32 MiB and stays in the 126 MiB
+// L2, so the random per-edge reads of bottom-up levels are L2 hits.
 //
-// Phase j of a batch (one barrier per level):
-//   * finalise F_{j-1}: seen |= F_{j-1} and write distance j-1 for its bits
-//     (lazily, so that readers use seen|F_{j-1}, which is invariant in the phase)
+// Phase j of a batch (one grid barrier per level):
+//   * finalise F_{j-1}: seen |= F_{j-1}, write distance j-1 for its bits (done
+//     lazily; readers use seen|F_{j-1}, which is invariant during the phase)
 //   * clear F_{j-2}
-//   * discover F_j either top-down (gather the adjacency of the F_{j-1} queue
-//     with the variant's strategy; claim bits with 64-bit atomicOr on the
-//     L2-resident record, append a vertex to the F_j queue when its word goes
-//     from zero to non-zero) or bottom-up (every not-fully-seen vertex ORs its
-//     in-neighbours' F_{j-1} words, stopping when all batch bits are covered).
-// Direction choice follows Beamer et al. (SC'12): top-down -> bottom-up when the
-// frontier's edges exceed the unexplored edges / alpha, back when the frontier
-// holds fewer than n / beta vertices.
+//   * discover F_j top-down (gather the adjacency of the F_{j-1} queue and claim
+//     new bits with 64-bit atomicOr) or bottom-up (each vertex still missing
+//     some active source ORs its in-neighbours' F_{j-1} words, stopping as soon
+//     as every missing active source is found).
+// A source is active while its frontier is non-empty; the active mask of F_j is
+// OR-reduced per warp during phase j.  Direction: top-down -> bottom-up when the
+// frontier's out-edges exceed m / alpha, back when it holds fewer than n / beta
+// vertices (after Beamer, Asanovic, Patterson, SC'12).
 //
-// Gather strategies restate the reference's kernels' neighbour-gathering ideas
-// for warp-synchronous sm_103a code (file:line in include/gu.h).
+// Top-down gather strategies restate the reference kernels' neighbour gathering
+// (file:line in include/gu.h); AUTO uses the edge-balanced merge-path gather.
 #include "device_utils.cuh"
 #include "gu_internal.h"
 
 #include <climits>
+#include <cstdlib>
 
 namespace gu {
 
-struct __align__(32) VState {
-    u64 seen;
-    u64 f[3];
-};
+constexpr int MS_THREADS = 512;
+constexpr int MAXW = 4;
+constexpr int CTA_DEGREE_THRESHOLD = 2048;  // CTA_warp.cu:44
+constexpr int QPACK_SHIFT = 38;             // qpack = (count << 38) | edges
+constexpr u64 QPACK_EDGES = (1ull << QPACK_SHIFT) - 1ull;
+constexpr int LBS_CHUNK = 256;              // edges per warp task of the merge-path gather
 
-// Control block of one launch; slots rotate over four levels (see ms_kernel).
 struct __align__(128) MsCtl {
     unsigned bar;
     int err;
     int td_levels;
     int bu_levels;
-    int qlen[4];
-    int work[4];
-    u64 qedges[4];
-    u64 fulledges[4];
     int max_level;
-    int pad[3];
+    int pad0[3];
+    u64 qpack[4];
+    int work[4];
+    int pad1[4];
+    u64 active[4][MAXW];
 };
+static_assert(sizeof(MsCtl) <= 256, "control block must fit its reserved space");
 
 struct MsArgs {
     const int32_t *__restrict__ R;
@@ -59,32 +66,41 @@ struct MsArgs {
     const int32_t *__restrict__ RT;
     const int32_t *__restrict__ CT;
     const int32_t *__restrict__ F;
+    const int32_t *__restrict__ heavy;
     int32_t n;
+    int32_t nheavy;
     int64_t m;
     const int32_t *sources;
     int32_t k;
     int32_t *dist;
     int64_t ld;
-    VState *vs;
+    u64 *seen;
+    u64 *fr[3];
+    int32_t *stamp;
     int32_t *q[3];
+    int32_t *qoff[3];
     MsCtl *ctl;
     float alpha, beta;
+    int degbits;
 };
 
 struct Lvl {
     int cur, nxt, prv, slot;
     int qlen, qlen_prev;
+    long long qedges;
     const int32_t *qcur;
+    const int32_t *qcur_off;
     int32_t *qnxt;
+    int32_t *qnxt_off;
     const int32_t *qprev;
+    const u64 *fcur;
+    u64 *fnxt;
+    u64 *fprv;
     int32_t lev;  // distance value of F_{j-1}
+    int32_t tag;  // stamp of level j (j + 1)
     int row0;
-    u64 full;
+    u64 active[MAXW];
 };
-
-constexpr int MS_THREADS = 512;
-constexpr int CTA_DEGREE_THRESHOLD = 2048;  // CTA_warp.cu:44
-constexpr unsigned DEG_CAP = 1u << 26;      // keeps warp sums of degrees in 32 bits
 
 struct GridG {
     __device__ static long long rank() { return (long long)blockIdx.x * blockDim.x + threadIdx.x; }
@@ -93,20 +109,82 @@ struct GridG {
     __device__ static int nblk() { return gridDim.x; }
 };
 
-__device__ __forceinline__ unsigned capped_degree(const int32_t *R, int32_t v)
+// ---- W-word helpers -----------------------------------------------------------
+template <int W>
+__device__ __forceinline__ void ldw(const u64 *p, u64 (&x)[W])
 {
-    unsigned d = (unsigned)(__ldg(R + v + 1) - __ldg(R + v));
-    return d < DEG_CAP ? d : DEG_CAP;
+    if constexpr (W == 1) {
+        x[0] = __ldcg(p);
+    } else {
+#pragma unroll
+        for (int i = 0; i < W / 2; ++i) {
+            const ulonglong2 v = __ldcg(reinterpret_cast<const ulonglong2 *>(p) + i);
+            x[2 * i] = v.x;
+            x[2 * i + 1] = v.y;
+        }
+    }
 }
 
-__device__ __forceinline__ void warp_add_u64(u64 *p, unsigned x)
+template <int W>
+__device__ __forceinline__ void stw(u64 *p, const u64 (&x)[W])
 {
+    if constexpr (W == 1) {
+        p[0] = x[0];
+    } else {
+#pragma unroll
+        for (int i = 0; i < W / 2; ++i)
+            reinterpret_cast<ulonglong2 *>(p)[i] = make_ulonglong2(x[2 * i], x[2 * i + 1]);
+    }
+}
+
+template <int W>
+__device__ __forceinline__ bool anyw(const u64 (&x)[W])
+{
+    u64 o = 0;
+#pragma unroll
+    for (int q = 0; q < W; ++q) o |= x[q];
+    return o != 0;
+}
+
+__device__ __forceinline__ unsigned lanemask_lt() { return (1u << lane_id()) - 1u; }
+
+// ---- frontier queue append ------------------------------------------------------
+// Lanes of the calling (possibly partial) warp append their vertices; one
+// 64-bit atomicAdd reserves both the queue slots and the range of their
+// out-edges.  The exclusive prefix of the degrees over the active lanes is a
+// bit-sliced ballot sum (works for any active mask).
+__device__ __forceinline__ void append_vertex(const MsArgs &a, const Lvl &L, int32_t w)
+{
+    const unsigned deg = (unsigned)(__ldg(a.R + w + 1) - __ldg(a.R + w));
     const unsigned mask = __activemask();
-    const unsigned tot = __reduce_add_sync(mask, x);
-    if (lane_id() == __ffs(mask) - 1) atomicAdd(p, (u64)tot);
+    const int lane = lane_id();
+    const int leader = __ffs(mask) - 1;
+    const unsigned lt = lanemask_lt();
+    u64 excl = 0, tot = 0;
+    for (int b = 0; b < a.degbits; ++b) {
+        const unsigned v = __ballot_sync(mask, (deg >> b) & 1u);
+        excl += (u64)__popc(v & lt) << b;
+        tot += (u64)__popc(v) << b;
+    }
+    u64 old = 0;
+    if (lane == leader) old = atomicAdd(&a.ctl->qpack[L.slot], ((u64)__popc(mask) << QPACK_SHIFT) | tot);
+    old = __shfl_sync(mask, old, leader);
+    const int pos = (int)(old >> QPACK_SHIFT) + __popc(mask & lt);
+    L.qnxt[pos] = w;
+    L.qnxt_off[pos] = (int32_t)((old & QPACK_EDGES) + excl);
 }
 
-// ---- distance writes -------------------------------------------------------
+template <int W>
+__device__ __forceinline__ void flush_active(const MsArgs &a, int slot, const u64 (&disc)[W])
+{
+#pragma unroll
+    for (int q = 0; q < W; ++q) {
+        const u64 r = warp_or_u64(FULL_MASK, disc[q]);
+        if (lane_id() == 0 && r) atomicOr(&a.ctl->active[slot][q], r);
+    }
+}
+
+// ---- distance writes ---------------------------------------------------------------
 __device__ __forceinline__ void write_bits_serial(int32_t *dist, int64_t ld, int row0, int32_t v, u64 bits,
                                                   int32_t val)
 {
@@ -118,7 +196,7 @@ __device__ __forceinline__ void write_bits_serial(int32_t *dist, int64_t ld, int
 }
 
 // Lanes hold consecutive vertices: for each source bit the stores of the warp
-// fall into one contiguous row segment.
+// fall into one contiguous row segment.  Called by full warps.
 __device__ __forceinline__ void write_bits_sweep(int32_t *dist, int64_t ld, int row0, int32_t v, u64 bits,
                                                  int32_t val)
 {
@@ -136,11 +214,13 @@ __device__ void init_dist_rows(int32_t *dist, int64_t ld, int row0, int nb, int3
     const long long rank = G::rank(), size = G::size();
     if ((ld & 3) == 0 && (((uintptr_t)dist) & 15) == 0) {
         const long long n4 = n >> 2;
-        const long long tot = (long long)nb * n4;
         const int4 inf4 = make_int4(INT_MAX, INT_MAX, INT_MAX, INT_MAX);
-        for (long long idx = rank; idx < tot; idx += size) {
-            const long long r = idx / n4, c = idx - r * n4;
-            reinterpret_cast<int4 *>(dist + (int64_t)(row0 + r) * ld)[c] = inf4;
+        if (n4 > 0) {
+            const long long tot = (long long)nb * n4;
+            for (long long idx = rank; idx < tot; idx += size) {
+                const long long r = idx / n4, c = idx - r * n4;
+                reinterpret_cast<int4 *>(dist + (int64_t)(row0 + r) * ld)[c] = inf4;
+            }
         }
         const int tail = n & 3;
         for (long long idx = rank; idx < (long long)nb * tail; idx += size) {
@@ -156,75 +236,101 @@ __device__ void init_dist_rows(int32_t *dist, int64_t ld, int row0, int nb, int3
     }
 }
 
-// ---- top-down visit: frontier bits f arrive at vertex w over one edge ------
-__device__ __forceinline__ void td_visit(const MsArgs &a, const Lvl &L, u64 f, int32_t w)
+// ---- top-down visit: frontier bits f arrive at vertex w over one edge ----------------
+template <int W>
+__device__ __forceinline__ void td_visit(const MsArgs &a, const Lvl &L, const u64 (&f)[W], int32_t w,
+                                         u64 (&disc)[W])
 {
-    VState *s = a.vs + w;
-    const u64 known = __ldcg(&s->seen) | __ldcg(&s->f[L.cur]) | __ldcg(&s->f[L.nxt]);
-    const u64 nb = f & ~known;
-    if (nb) {
-        const u64 old = atomicOr(&s->f[L.nxt], nb);
-        if (old == 0) warp_append(w, L.qnxt, &a.ctl->qlen[L.slot], &a.ctl->qedges[L.slot], capped_degree(a.R, w));
+    const size_t o = (size_t)w * W;
+    u64 s[W], c[W], x[W];
+    ldw<W>(a.seen + o, s);
+    ldw<W>(L.fcur + o, c);
+    ldw<W>(L.fnxt + o, x);
+    bool found = false, first = false;
+#pragma unroll
+    for (int q = 0; q < W; ++q) {
+        const u64 nb = f[q] & ~(s[q] | c[q] | x[q]);
+        if (nb) {
+            const u64 old = atomicOr(L.fnxt + o + q, nb);
+            disc[q] |= nb;
+            found = true;
+            if (W == 1 && old == 0) first = true;
+        }
     }
+    if (W > 1 && found) first = atomicMax(a.stamp + w, L.tag) < L.tag;
+    if (first) append_vertex(a, L, w);
 }
 
-// Finalise F_{j-1} (queue order) and clear F_{j-2}.
-template <class G>
+// Finalise F_{j-1} in queue order and clear F_{j-2}.
+template <int W, class G>
 __device__ void td_update(const MsArgs &a, const Lvl &L)
 {
     const long long rank = G::rank(), size = G::size();
     for (long long i = rank; i < L.qlen; i += size) {
         const int32_t v = __ldcg(L.qcur + i);
-        VState *s = a.vs + v;
-        const u64 f = __ldcg(&s->f[L.cur]);
-        const u64 sn = __ldcg(&s->seen) | f;
-        s->seen = sn;
-        if (sn == L.full) warp_add_u64(&a.ctl->fulledges[L.slot], capped_degree(a.R, v));
-        write_bits_serial(a.dist, a.ld, L.row0, v, f, L.lev);
+        const size_t o = (size_t)v * W;
+        u64 f[W], s[W];
+        ldw<W>(L.fcur + o, f);
+        ldw<W>(a.seen + o, s);
+#pragma unroll
+        for (int q = 0; q < W; ++q) s[q] |= f[q];
+        stw<W>(a.seen + o, s);
+#pragma unroll
+        for (int q = 0; q < W; ++q) write_bits_serial(a.dist, a.ld, L.row0 + 64 * q, v, f[q], L.lev);
     }
+    const u64 zero[W] = {};
     for (long long i = rank; i < L.qlen_prev; i += size) {
         const int32_t v = __ldcg(L.qprev + i);
-        a.vs[v].f[L.prv] = 0;
+        stw<W>(L.fprv + (size_t)v * W, zero);
     }
 }
 
+template <int W>
+__device__ __forceinline__ void load_front(const Lvl &L, int32_t v, u64 (&f)[W])
+{
+    ldw<W>(L.fcur + (size_t)v * W, f);
+}
+
 // LINEAR: thread per frontier vertex, serial adjacency (linear_with_atomics.cu:122-135).
-template <class G>
-__device__ void gather_linear(const MsArgs &a, const Lvl &L)
+template <int W, class G>
+__device__ void gather_linear(const MsArgs &a, const Lvl &L, u64 (&disc)[W])
 {
     for (long long i = G::rank(); i < L.qlen; i += G::size()) {
         const int32_t v = __ldcg(L.qcur + i);
-        const u64 f = __ldcg(&a.vs[v].f[L.cur]);
+        u64 f[W];
+        load_front<W>(L, v, f);
         const int32_t e1 = __ldg(a.R + v + 1);
-        for (int32_t e = __ldg(a.R + v); e < e1; ++e) td_visit(a, L, f, __ldg(a.C + e));
+        for (int32_t e = __ldg(a.R + v); e < e1; ++e) td_visit<W>(a, L, f, __ldg(a.C + e), disc);
     }
 }
 
 // EDGE: every CSR entry every level, source vertex from the COO array
-// (edge_parallel.cu:77-88); one sweep serves all 64 sources of the batch.
-template <class G>
-__device__ void gather_edge(const MsArgs &a, const Lvl &L)
+// (edge_parallel.cu:77-88); one sweep serves every source of the batch.
+template <int W, class G>
+__device__ void gather_edge(const MsArgs &a, const Lvl &L, u64 (&disc)[W])
 {
     for (long long e = G::rank(); e < a.m; e += G::size()) {
         const int32_t u = __ldg(a.F + e);
-        const u64 f = __ldcg(&a.vs[u].f[L.cur]);
-        if (f) td_visit(a, L, f, __ldg(a.C + e));
+        u64 f[W];
+        load_front<W>(L, u, f);
+        if (anyw<W>(f)) td_visit<W>(a, L, f, __ldg(a.C + e), disc);
     }
 }
 
 // SHUFFLE: warp per frontier vertex; warps take the next vertex from a shared
 // counter when done (shuffle_based.cuh:192-223).
-template <class G>
-__device__ void gather_shuffle(const MsArgs &a, const Lvl &L)
+template <int W, class G>
+__device__ void gather_shuffle(const MsArgs &a, const Lvl &L, u64 (&disc)[W])
 {
     const int lane = lane_id();
     const long long nw = G::size() >> 5;
     long long kq = G::rank() >> 5;
     while (kq < L.qlen) {
         const int32_t v = __ldcg(L.qcur + kq);
-        const u64 f = __ldcg(&a.vs[v].f[L.cur]);
+        u64 f[W];
+        load_front<W>(L, v, f);
         const int32_t e1 = __ldg(a.R + v + 1);
-        for (int32_t e = __ldg(a.R + v) + lane; e < e1; e += 32) td_visit(a, L, f, __ldg(a.C + e));
+        for (int32_t e = __ldg(a.R + v) + lane; e < e1; e += 32) td_visit<W>(a, L, f, __ldg(a.C + e), disc);
         int nk = 0;
         if (lane == 0) nk = atomicAdd(&a.ctl->work[L.slot], 1);
         kq = nw + __shfl_sync(FULL_MASK, nk, 0);
@@ -234,56 +340,55 @@ __device__ void gather_shuffle(const MsArgs &a, const Lvl &L)
 // Warp strip-mining: each lane holds one frontier vertex; the warp elects the
 // highest lane with adjacency left (race_and_resolve) and gathers its list
 // together (warp_based.cu:109-145).
-__device__ __forceinline__ void warp_stripmine(const MsArgs &a, const Lvl &L, int32_t r, int32_t r_end, u64 f)
+template <int W>
+__device__ __forceinline__ void warp_stripmine(const MsArgs &a, const Lvl &L, int32_t r, int32_t r_end, int32_t v,
+                                               u64 (&disc)[W])
 {
     const int lane = lane_id();
     while (__any_sync(FULL_MASK, r < r_end)) {
         const int winner = race_and_resolve_warp(r < r_end);
         const int32_t rw = __shfl_sync(FULL_MASK, r, winner);
         const int32_t re = __shfl_sync(FULL_MASK, r_end, winner);
-        const u64 fw = __shfl_sync(FULL_MASK, f, winner);
+        const int32_t vw = __shfl_sync(FULL_MASK, v, winner);
         if (lane == winner) r = r_end;  // a lane cannot win twice
-        for (int32_t e = rw + lane; e < re; e += 32) td_visit(a, L, fw, __ldg(a.C + e));
+        u64 f[W];
+        load_front<W>(L, vw, f);
+        for (int32_t e = rw + lane; e < re; e += 32) td_visit<W>(a, L, f, __ldg(a.C + e), disc);
     }
 }
 
-template <class G>
-__device__ void gather_warp(const MsArgs &a, const Lvl &L)
+template <int W, class G>
+__device__ void gather_warp(const MsArgs &a, const Lvl &L, u64 (&disc)[W])
 {
     const int lane = lane_id();
     const long long nw = G::size() >> 5;
     for (long long base = (G::rank() >> 5) * 32; base < L.qlen; base += nw * 32) {
         const long long i = base + lane;
-        int32_t r = 0, r_end = 0;
-        u64 f = 0;
+        int32_t r = 0, r_end = 0, v = 0;
         if (i < L.qlen) {
-            const int32_t v = __ldcg(L.qcur + i);
+            v = __ldcg(L.qcur + i);
             r = __ldg(a.R + v);
             r_end = __ldg(a.R + v + 1);
-            f = __ldcg(&a.vs[v].f[L.cur]);
         }
-        warp_stripmine(a, L, r, r_end, f);
+        warp_stripmine<W>(a, L, r, r_end, v, disc);
     }
 }
 
 // CTA_WARP: lists longer than 2048 are gathered by the whole CTA, one at a
 // time (highest thread first), the rest by warp strip-mining (CTA_warp.cu:62-265).
-template <class G>
-__device__ void gather_cta_warp(const MsArgs &a, const Lvl &L)
+template <int W, class G>
+__device__ void gather_cta_warp(const MsArgs &a, const Lvl &L, u64 (&disc)[W])
 {
     __shared__ int s_winner;
-    __shared__ int32_t s_r, s_re;
-    __shared__ u64 s_f;
+    __shared__ int32_t s_r, s_re, s_v;
     const int BD = blockDim.x;
     for (long long base = (long long)G::blk() * BD; base < L.qlen; base += (long long)G::nblk() * BD) {
         const long long i = base + threadIdx.x;
-        int32_t r = 0, r_end = 0;
-        u64 f = 0;
+        int32_t r = 0, r_end = 0, v = 0;
         if (i < L.qlen) {
-            const int32_t v = __ldcg(L.qcur + i);
+            v = __ldcg(L.qcur + i);
             r = __ldg(a.R + v);
             r_end = __ldg(a.R + v + 1);
-            f = __ldcg(&a.vs[v].f[L.cur]);
         }
         while (true) {
             if (threadIdx.x == 0) s_winner = -1;
@@ -295,16 +400,17 @@ __device__ void gather_cta_warp(const MsArgs &a, const Lvl &L)
             if ((int)threadIdx.x == wt) {
                 s_r = r;
                 s_re = r_end;
-                s_f = f;
+                s_v = v;
                 r = r_end;
             }
             __syncthreads();
             const int32_t re = s_re;
-            const u64 fw = s_f;
-            for (int32_t e = s_r + threadIdx.x; e < re; e += BD) td_visit(a, L, fw, __ldg(a.C + e));
+            u64 f[W];
+            load_front<W>(L, s_v, f);
+            for (int32_t e = s_r + threadIdx.x; e < re; e += BD) td_visit<W>(a, L, f, __ldg(a.C + e), disc);
             __syncthreads();
         }
-        warp_stripmine(a, L, r, r_end, f);
+        warp_stripmine<W>(a, L, r, r_end, v, disc);
         __syncthreads();
     }
 }
@@ -322,14 +428,14 @@ __device__ __forceinline__ int block_exclusive_scan(int x, int *total, int *s_wa
     if (lane == 31) s_warp[wid] = incl;
     __syncthreads();
     if (wid == 0) {
-        int t = lane < nw ? s_warp[lane] : 0;
+        const int t = lane < nw ? s_warp[lane] : 0;
         int ti = t;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
             const int y = __shfl_up_sync(FULL_MASK, ti, o);
             if (lane >= o) ti += y;
         }
-        if (lane < nw) s_warp[lane] = ti - t;  // exclusive warp offsets
+        if (lane < nw) s_warp[lane] = ti - t;
         if (lane == 31) s_warp[32] = ti;
     }
     __syncthreads();
@@ -341,32 +447,29 @@ __device__ __forceinline__ int block_exclusive_scan(int x, int *total, int *s_wa
 
 // SCAN: the CTA ranks the adjacency lists of blockDim frontier vertices with an
 // exclusive scan, then threads take consecutive edge slots and find the owning
-// vertex by binary search over the scanned offsets (scan_based.cu:107-149; the
-// owner lookup is the load-balanced search of load_balanced_search.cu:176-191).
-template <class G>
-__device__ void gather_scan(const MsArgs &a, const Lvl &L)
+// vertex by binary search over the scanned offsets (scan_based.cu:107-149).
+template <int W, class G>
+__device__ void gather_scan(const MsArgs &a, const Lvl &L, u64 (&disc)[W])
 {
     __shared__ int s_off[MS_THREADS];
     __shared__ int32_t s_r[MS_THREADS];
-    __shared__ u64 s_f[MS_THREADS];
+    __shared__ int32_t s_v[MS_THREADS];
     __shared__ int s_warp[33];
     const int BD = blockDim.x;
     for (long long base = (long long)G::blk() * BD; base < L.qlen; base += (long long)G::nblk() * BD) {
         const long long i = base + threadIdx.x;
-        int32_t r = 0;
+        int32_t r = 0, v = 0;
         int deg = 0;
-        u64 f = 0;
         if (i < L.qlen) {
-            const int32_t v = __ldcg(L.qcur + i);
+            v = __ldcg(L.qcur + i);
             r = __ldg(a.R + v);
             deg = __ldg(a.R + v + 1) - r;
-            f = __ldcg(&a.vs[v].f[L.cur]);
         }
         int total;
         const int off = block_exclusive_scan(deg, &total, s_warp);
         s_off[threadIdx.x] = off;
         s_r[threadIdx.x] = r;
-        s_f[threadIdx.x] = f;
+        s_v[threadIdx.x] = v;
         __syncthreads();
         for (int e = threadIdx.x; e < total; e += BD) {
             int lo = 0, hi = BD - 1;
@@ -375,138 +478,271 @@ __device__ void gather_scan(const MsArgs &a, const Lvl &L)
                 if (s_off[mid] <= e) lo = mid;
                 else hi = mid - 1;
             }
-            td_visit(a, L, s_f[lo], __ldg(a.C + s_r[lo] + (e - s_off[lo])));
+            u64 f[W];
+            load_front<W>(L, s_v[lo], f);
+            td_visit<W>(a, L, f, __ldg(a.C + s_r[lo] + (e - s_off[lo])), disc);
         }
         __syncthreads();
     }
 }
 
-// Bottom-up level: every vertex (coalesced sweep) finalises its own F_{j-1}
-// bits, clears F_{j-2}, and, if some batch source has not reached it, ORs the
-// F_{j-1} words of its in-neighbours until all missing bits are found.
-template <class G>
-__device__ void bu_sweep(const MsArgs &a, const Lvl &L)
+// Merge-path gather (AUTO): the frontier's out-edges, ranked by the edge
+// offsets reserved at append time, are cut into chunks of LBS_CHUNK; a warp
+// takes a chunk, brackets its owners [k0, k1] by two binary searches, and each
+// lane finds the owner of its edge slot within that bracket (the
+// load-balanced search of load_balanced_search.cu:123-192, grid-wide).
+__device__ __forceinline__ int owner_search(const int32_t *off, int lo, int hi, long long e)
 {
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if ((long long)__ldcg(off + mid) <= e) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+template <int W, class G>
+__device__ void gather_lbs(const MsArgs &a, const Lvl &L, u64 (&disc)[W])
+{
+    const long long E = L.qedges;
+    if (E == 0) return;
+    const long long ntask = (E + LBS_CHUNK - 1) / LBS_CHUNK;
+    const long long nw = G::size() >> 5;
     const int lane = lane_id();
-    const long long size = G::size();
-    for (long long base = G::rank() - lane; base < a.n; base += size) {
-        const int32_t w = (int32_t)(base + lane);
-        const bool valid = w < a.n;
-        u64 seen = 0, f = 0;
-        if (valid) {
-            VState *s = a.vs + w;
-            const ulonglong2 x = __ldcg(reinterpret_cast<const ulonglong2 *>(s));
-            const ulonglong2 y = __ldcg(reinterpret_cast<const ulonglong2 *>(s) + 1);
-            seen = x.x;
-            f = L.cur == 0 ? x.y : (L.cur == 1 ? y.x : y.y);
-            const u64 fp = L.prv == 0 ? x.y : (L.prv == 1 ? y.x : y.y);
-            if (f) {
-                seen |= f;
-                s->seen = seen;
-                if (seen == L.full) warp_add_u64(&a.ctl->fulledges[L.slot], capped_degree(a.R, w));
-            }
-            if (fp) s->f[L.prv] = 0;
-        }
-        write_bits_sweep(a.dist, a.ld, L.row0, w, f, L.lev);
-        if (valid && seen != L.full) {
-            u64 acc = 0;
-            const int32_t e1 = __ldg(a.RT + w + 1);
-            for (int32_t e = __ldg(a.RT + w); e < e1; ++e) {
-                acc |= __ldcg(&a.vs[__ldg(a.CT + e)].f[L.cur]);
-                if ((acc | seen) == L.full) break;
-            }
-            const u64 nb = acc & ~seen;
-            if (nb) {
-                a.vs[w].f[L.nxt] = nb;
-                warp_append(w, L.qnxt, &a.ctl->qlen[L.slot], &a.ctl->qedges[L.slot], capped_degree(a.R, w));
-            }
+    for (long long t = G::rank() >> 5; t < ntask; t += nw) {
+        const long long e0 = t * LBS_CHUNK;
+        const long long e1 = min(E, e0 + LBS_CHUNK);
+        const int k0 = owner_search(L.qcur_off, 0, L.qlen - 1, e0);
+        const int k1 = owner_search(L.qcur_off, k0, L.qlen - 1, e1 - 1);
+        for (long long e = e0 + lane; e < e1; e += 32) {
+            const int k = owner_search(L.qcur_off, k0, k1, e);
+            const int32_t v = __ldcg(L.qcur + k);
+            u64 f[W];
+            load_front<W>(L, v, f);
+            const int32_t w = __ldg(a.C + __ldg(a.R + v) + (int32_t)(e - __ldcg(L.qcur_off + k)));
+            td_visit<W>(a, L, f, w, disc);
         }
     }
 }
 
-template <int VARIANT>
+// Bottom-up level: every vertex (coalesced sweep) finalises its own F_{j-1}
+// bits and clears F_{j-2}; a light vertex still missing an active source ORs
+// its in-neighbours' F_{j-1} words itself (four independent loads in flight),
+// stopping once every missing active source is found.
+template <int W>
+__device__ __forceinline__ bool covers(const u64 (&acc)[W], const u64 (&need)[W])
+{
+    bool ok = true;
+#pragma unroll
+    for (int q = 0; q < W; ++q) ok &= (acc[q] & need[q]) == need[q];
+    return ok;
+}
+
+template <int W>
+__device__ __forceinline__ void or_front(const Lvl &L, int32_t v, u64 (&acc)[W])
+{
+    u64 x[W];
+    ldw<W>(L.fcur + (size_t)v * W, x);
+#pragma unroll
+    for (int q = 0; q < W; ++q) acc[q] |= x[q];
+}
+
+template <int W, class G>
+__device__ void bu_sweep(const MsArgs &a, const Lvl &L, u64 (&disc)[W])
+{
+    const int lane = lane_id();
+    const long long size = G::size();
+    const u64 zero[W] = {};
+    for (long long base = G::rank() - lane; base < a.n; base += size) {
+        const int32_t w = (int32_t)(base + lane);
+        const bool valid = w < a.n;
+        u64 s[W] = {}, f[W] = {};
+        if (valid) {
+            const size_t o = (size_t)w * W;
+            ldw<W>(a.seen + o, s);
+            ldw<W>(L.fcur + o, f);
+            if (anyw<W>(f)) {
+#pragma unroll
+                for (int q = 0; q < W; ++q) s[q] |= f[q];
+                stw<W>(a.seen + o, s);
+            }
+            stw<W>(L.fprv + o, zero);
+        }
+#pragma unroll
+        for (int q = 0; q < W; ++q) write_bits_sweep(a.dist, a.ld, L.row0 + 64 * q, w, f[q], L.lev);
+        if (!valid) continue;
+        u64 need[W];
+#pragma unroll
+        for (int q = 0; q < W; ++q) need[q] = L.active[q] & ~s[q];
+        if (!anyw<W>(need)) continue;
+        const int32_t e0 = __ldg(a.RT + w), e1 = __ldg(a.RT + w + 1);
+        if (e1 - e0 > BU_HEAVY_DEGREE || e1 == e0) continue;  // heavy: bu_heavy
+        u64 acc[W] = {};
+        for (int32_t e = e0; e < e1; e += 4) {
+            const int32_t c0 = __ldg(a.CT + e);
+            const int32_t c1 = e + 1 < e1 ? __ldg(a.CT + e + 1) : -1;
+            const int32_t c2 = e + 2 < e1 ? __ldg(a.CT + e + 2) : -1;
+            const int32_t c3 = e + 3 < e1 ? __ldg(a.CT + e + 3) : -1;
+            or_front<W>(L, c0, acc);
+            if (c1 >= 0) or_front<W>(L, c1, acc);
+            if (c2 >= 0) or_front<W>(L, c2, acc);
+            if (c3 >= 0) or_front<W>(L, c3, acc);
+            if (covers<W>(acc, need)) break;
+        }
+        u64 nb[W];
+#pragma unroll
+        for (int q = 0; q < W; ++q) nb[q] = acc[q] & need[q];
+        if (anyw<W>(nb)) {
+            stw<W>(L.fnxt + (size_t)w * W, nb);
+#pragma unroll
+            for (int q = 0; q < W; ++q) disc[q] |= nb[q];
+            append_vertex(a, L, w);
+        }
+    }
+}
+
+// Heavy vertices (in-degree > BU_HEAVY_DEGREE): a warp per vertex ORs 32
+// in-neighbours per step and stops once every missing active source is found.
+template <int W, class G>
+__device__ void bu_heavy(const MsArgs &a, const Lvl &L, u64 (&disc)[W])
+{
+    const int lane = lane_id();
+    const long long nw = G::size() >> 5;
+    for (long long i = G::rank() >> 5; i < a.nheavy; i += nw) {
+        const int32_t w = __ldg(a.heavy + i);
+        const size_t o = (size_t)w * W;
+        u64 s[W], f[W], need[W];
+        ldw<W>(a.seen + o, s);
+        ldw<W>(L.fcur + o, f);
+#pragma unroll
+        for (int q = 0; q < W; ++q) need[q] = L.active[q] & ~(s[q] | f[q]);
+        if (!anyw<W>(need)) continue;
+        const int32_t e0 = __ldg(a.RT + w), e1 = __ldg(a.RT + w + 1);
+        u64 acc[W] = {};
+        for (int32_t eb = e0; eb < e1; eb += 32) {
+            u64 x[W] = {};
+            const int32_t e = eb + lane;
+            if (e < e1) ldw<W>(L.fcur + (size_t)__ldg(a.CT + e) * W, x);
+#pragma unroll
+            for (int q = 0; q < W; ++q) acc[q] |= warp_or_u64(FULL_MASK, x[q]);
+            if (covers<W>(acc, need)) break;
+        }
+        u64 nb[W];
+#pragma unroll
+        for (int q = 0; q < W; ++q) nb[q] = acc[q] & need[q];
+        if (lane == 0 && anyw<W>(nb)) {
+            stw<W>(L.fnxt + o, nb);
+#pragma unroll
+            for (int q = 0; q < W; ++q) disc[q] |= nb[q];
+            append_vertex(a, L, w);
+        }
+    }
+}
+
+template <int VARIANT, int W>
 __global__ void __launch_bounds__(MS_THREADS) ms_grid_kernel(MsArgs a)
 {
     unsigned epoch = 0;
     MsCtl *ctl = a.ctl;
     const long long rank = GridG::rank(), size = GridG::size();
-    const int nbatch = (a.k + 63) >> 6;
+    const int bsz = 64 * W;
+    const int nbatch = (a.k + bsz - 1) / bsz;
     for (int b = 0; b < nbatch; ++b) {
-        const int row0 = b << 6;
-        const int nb = min(64, a.k - row0);
-        const u64 full = nb == 64 ? ~0ull : ((1ull << nb) - 1ull);
-        for (long long w = rank; w < a.n; w += size) {
-            ulonglong2 *p = reinterpret_cast<ulonglong2 *>(a.vs + w);
-            p[0] = make_ulonglong2(0ull, 0ull);
-            p[1] = make_ulonglong2(0ull, 0ull);
+        const int row0 = b * bsz;
+        const int nb = min(bsz, a.k - row0);
+        {
+            const u64 zero[W] = {};
+            for (long long w = rank; w < a.n; w += size) {
+                const size_t o = (size_t)w * W;
+                stw<W>(a.seen + o, zero);
+                stw<W>(a.fr[0] + o, zero);
+                stw<W>(a.fr[1] + o, zero);
+                stw<W>(a.fr[2] + o, zero);
+                if (W > 1) a.stamp[w] = 0;
+            }
         }
         init_dist_rows<GridG>(a.dist, a.ld, row0, nb, a.n);
-        if (rank == 0) {
-            for (int s = 0; s < 4; ++s) {
-                ctl->qlen[s] = 0;
-                ctl->work[s] = 0;
-                ctl->qedges[s] = 0;
-                ctl->fulledges[s] = 0;
-            }
+        if (rank < 4) {
+            ctl->qpack[rank] = 0;
+            ctl->work[rank] = 0;
+#pragma unroll
+            for (int q = 0; q < MAXW; ++q) ctl->active[rank][q] = 0;
         }
         if (!grid_barrier(&ctl->bar, &ctl->err, epoch)) return;
         if (rank < nb) {
             const int32_t s = __ldg(a.sources + row0 + rank);
-            const u64 old = atomicOr(&a.vs[s].f[0], 1ull << rank);
-            if (old == 0) warp_append(s, a.q[0], &ctl->qlen[0], &ctl->qedges[0], capped_degree(a.R, s));
+            const int q = (int)rank >> 6;
+            const u64 bit = 1ull << (rank & 63);
+            const u64 old = atomicOr(a.fr[0] + (size_t)s * W + q, bit);
+            atomicOr(&ctl->active[0][q], bit);
+            bool first;
+            if (W == 1) first = old == 0;
+            else first = atomicMax(a.stamp + s, 1) < 1;
+            if (first) {
+                Lvl L0;
+                L0.slot = 0;
+                L0.qnxt = a.q[0];
+                L0.qnxt_off = a.qoff[0];
+                append_vertex(a, L0, s);
+            }
         }
         if (!grid_barrier(&ctl->bar, &ctl->err, epoch)) return;
 
-        u64 fulltotal = 0;
         bool prev_bu = false;
         for (int j = 1;; ++j) {
             Lvl L;
             const int sc = (j - 1) & 3, sp = (j - 2) & 3;
-            L.qlen = ld_volatile_i32(&ctl->qlen[sc]);
+            const u64 pk = ld_volatile_u64(&ctl->qpack[sc]);
+            L.qlen = (int)(pk >> QPACK_SHIFT);
             if (L.qlen == 0) break;
-            L.qlen_prev = j >= 2 ? ld_volatile_i32(&ctl->qlen[sp]) : 0;
-            const u64 qedges = ld_volatile_u64(&ctl->qedges[sc]);
-            fulltotal += ld_volatile_u64(&ctl->fulledges[sc]);
+            L.qedges = (long long)(pk & QPACK_EDGES);
+            L.qlen_prev = j >= 2 ? (int)(ld_volatile_u64(&ctl->qpack[sp]) >> QPACK_SHIFT) : 0;
+#pragma unroll
+            for (int q = 0; q < MAXW; ++q) L.active[q] = q < W ? ld_volatile_u64(&ctl->active[sc][q]) : 0ull;
             L.slot = j & 3;
             L.cur = (j - 1) % 3;
             L.nxt = j % 3;
             L.prv = (j + 1) % 3;
             L.qcur = a.q[L.cur];
+            L.qcur_off = a.qoff[L.cur];
             L.qnxt = a.q[L.nxt];
+            L.qnxt_off = a.qoff[L.nxt];
             L.qprev = a.q[L.prv];
+            L.fcur = a.fr[L.cur];
+            L.fnxt = a.fr[L.nxt];
+            L.fprv = a.fr[L.prv];
             L.lev = j - 1;
+            L.tag = j + 1;
             L.row0 = row0;
-            L.full = full;
             if (rank == 0) {
                 const int z = (j + 1) & 3;
-                ctl->qlen[z] = 0;
+                ctl->qpack[z] = 0;
                 ctl->work[z] = 0;
-                ctl->qedges[z] = 0;
-                ctl->fulledges[z] = 0;
+#pragma unroll
+                for (int q = 0; q < MAXW; ++q) ctl->active[z][q] = 0;
             }
             bool bu = false;
-            int policy = VARIANT;
             if (VARIANT == GU_BFS_BOTTOM_UP) {
                 bu = j > 1;
             } else if (VARIANT == GU_BFS_AUTO) {
-                const double unexplored = (double)a.m - (double)fulltotal;
-                if (!prev_bu) bu = j > 1 && (double)qedges > unexplored / (double)a.alpha;
-                else bu = (double)L.qlen >= (double)a.n / (double)a.beta;
-                const double avg = (double)qedges / (double)L.qlen;
-                policy = avg <= 8.0 ? GU_BFS_LINEAR : GU_BFS_SHUFFLE;
+                if (!prev_bu) bu = j > 1 && (double)L.qedges * (double)a.alpha > (double)a.m;
+                else bu = (double)L.qlen * (double)a.beta > (double)a.n;
             }
+            u64 disc[W] = {};
             if (bu) {
-                bu_sweep<GridG>(a, L);
+                bu_sweep<W, GridG>(a, L, disc);
+                if (a.nheavy) bu_heavy<W, GridG>(a, L, disc);
             } else {
-                td_update<GridG>(a, L);
-                if (VARIANT == GU_BFS_EDGE) gather_edge<GridG>(a, L);
-                else if (VARIANT == GU_BFS_WARP) gather_warp<GridG>(a, L);
-                else if (VARIANT == GU_BFS_CTA_WARP) gather_cta_warp<GridG>(a, L);
-                else if (VARIANT == GU_BFS_SCAN) gather_scan<GridG>(a, L);
-                else if (VARIANT == GU_BFS_SHUFFLE || VARIANT == GU_BFS_BOTTOM_UP) gather_shuffle<GridG>(a, L);
-                else if (VARIANT == GU_BFS_AUTO && policy == GU_BFS_SHUFFLE) gather_shuffle<GridG>(a, L);
-                else gather_linear<GridG>(a, L);
+                td_update<W, GridG>(a, L);
+                if (VARIANT == GU_BFS_EDGE) gather_edge<W, GridG>(a, L, disc);
+                else if (VARIANT == GU_BFS_WARP) gather_warp<W, GridG>(a, L, disc);
+                else if (VARIANT == GU_BFS_CTA_WARP) gather_cta_warp<W, GridG>(a, L, disc);
+                else if (VARIANT == GU_BFS_SCAN) gather_scan<W, GridG>(a, L, disc);
+                else if (VARIANT == GU_BFS_SHUFFLE) gather_shuffle<W, GridG>(a, L, disc);
+                else if (VARIANT == GU_BFS_LINEAR) gather_linear<W, GridG>(a, L, disc);
+                else gather_lbs<W, GridG>(a, L, disc);  // AUTO, BOTTOM_UP level 1
             }
+            flush_active<W>(a, L.slot, disc);
             if (rank == 0) {
                 if (bu) ctl->bu_levels++;
                 else ctl->td_levels++;
@@ -518,19 +754,46 @@ __global__ void __launch_bounds__(MS_THREADS) ms_grid_kernel(MsArgs a)
     }
 }
 
-// ---- host side ---------------------------------------------------------------
-template <int V>
-static void launch_variant(const MsArgs &a, int sms, cudaStream_t stream)
+// ---- host side ---------------------------------------------------------------------
+template <int V, int W>
+static void launch_one(const MsArgs &a, int sms, cudaStream_t stream)
 {
     static int blocks_per_sm = -1;
     if (blocks_per_sm < 0) {
-        GU_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, ms_grid_kernel<V>, MS_THREADS, 0));
+        GU_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, ms_grid_kernel<V, W>, MS_THREADS, 0));
         if (blocks_per_sm < 1) throw gu_error(GU_ERR_INTERNAL, "msbfs kernel cannot be resident");
     }
     dim3 grid(sms * blocks_per_sm), block(MS_THREADS);
     MsArgs args = a;
     void *params[] = {&args};
-    GU_CUDA_CHECK(cudaLaunchCooperativeKernel((const void *)ms_grid_kernel<V>, grid, block, params, 0, stream));
+    GU_CUDA_CHECK(cudaLaunchCooperativeKernel((const void *)ms_grid_kernel<V, W>, grid, block, params, 0, stream));
+}
+
+template <int V>
+static void launch_words(const MsArgs &a, int W, int sms, cudaStream_t stream)
+{
+    if (W == 1) launch_one<V, 1>(a, sms, stream);
+    else if (W == 2) launch_one<V, 2>(a, sms, stream);
+    else launch_one<V, 4>(a, sms, stream);
+}
+
+static float env_float(const char *name, float dflt)
+{
+    const char *s = std::getenv(name);
+    if (!s || !*s) return dflt;
+    return std::strtof(s, nullptr);
+}
+
+int msbfs_words_for(int32_t k)
+{
+    const char *s = std::getenv("GU_MS_WORDS");
+    if (s && *s) {
+        const int w = std::atoi(s);
+        if (w == 1 || w == 2 || w == 4) return w;
+    }
+    if (k <= 64) return 1;
+    if (k <= 128) return 2;
+    return 4;
 }
 
 void launch_msbfs(DeviceGraph &g, const int32_t *sources, int32_t k, int32_t *dist, int64_t ld,
@@ -538,42 +801,61 @@ void launch_msbfs(DeviceGraph &g, const int32_t *sources, int32_t k, int32_t *di
 {
     (void)dev_err_out;
     if (opt.variant == GU_BFS_EDGE) ensure_coo(g, stream);
+    const int W = msbfs_words_for(k);
     const size_t n = (size_t)g.n;
-    const size_t vs_bytes = ((n * sizeof(VState) + 255) / 256) * 256;
-    const size_t q_bytes = ((n * sizeof(int32_t) + 255) / 256) * 256;
+    auto up = [](size_t b) { return ((b + 255) / 256) * 256; };
+    const size_t words_bytes = up(n * W * sizeof(u64));
+    const size_t i32_bytes = up(n * sizeof(int32_t));
     const size_t ctl_bytes = 256;
-    char *ws = (char *)g.ws.get(ctl_bytes + vs_bytes + 3 * q_bytes);
+    char *ws = (char *)g.ws.get(ctl_bytes + 4 * words_bytes + 7 * i32_bytes);
     MsArgs a;
     a.R = g.R;
     a.C = g.C;
     a.RT = g.RT;
     a.CT = g.CT;
     a.F = g.F;
+    a.heavy = g.heavy;
     a.n = g.n;
+    a.nheavy = g.nheavy;
     a.m = g.m;
     a.sources = sources;
     a.k = k;
     a.dist = dist;
     a.ld = ld;
-    a.ctl = reinterpret_cast<MsCtl *>(ws);
-    a.vs = reinterpret_cast<VState *>(ws + ctl_bytes);
-    a.q[0] = reinterpret_cast<int32_t *>(ws + ctl_bytes + vs_bytes);
-    a.q[1] = reinterpret_cast<int32_t *>(ws + ctl_bytes + vs_bytes + q_bytes);
-    a.q[2] = reinterpret_cast<int32_t *>(ws + ctl_bytes + vs_bytes + 2 * q_bytes);
-    a.alpha = opt.alpha;
-    a.beta = opt.beta;
+    char *p = ws;
+    a.ctl = reinterpret_cast<MsCtl *>(p);
+    p += ctl_bytes;
+    a.seen = reinterpret_cast<u64 *>(p);
+    p += words_bytes;
+    for (int i = 0; i < 3; ++i) {
+        a.fr[i] = reinterpret_cast<u64 *>(p);
+        p += words_bytes;
+    }
+    a.stamp = reinterpret_cast<int32_t *>(p);
+    p += i32_bytes;
+    for (int i = 0; i < 3; ++i) {
+        a.q[i] = reinterpret_cast<int32_t *>(p);
+        p += i32_bytes;
+        a.qoff[i] = reinterpret_cast<int32_t *>(p);
+        p += i32_bytes;
+    }
+    a.alpha = env_float("GU_MS_ALPHA", opt.alpha);
+    a.beta = env_float("GU_MS_BETA", opt.beta);
+    int degbits = 1;
+    while (degbits < 31 && (1ll << degbits) <= (long long)g.max_degree) ++degbits;
+    a.degbits = degbits;
     GU_CUDA_CHECK(cudaMemsetAsync(a.ctl, 0, sizeof(MsCtl), stream));
     const int sms = g.sm_count;
     g.mark_start(stream);
     switch (opt.variant) {
-    case GU_BFS_AUTO: launch_variant<GU_BFS_AUTO>(a, sms, stream); break;
-    case GU_BFS_LINEAR: launch_variant<GU_BFS_LINEAR>(a, sms, stream); break;
-    case GU_BFS_EDGE: launch_variant<GU_BFS_EDGE>(a, sms, stream); break;
-    case GU_BFS_WARP: launch_variant<GU_BFS_WARP>(a, sms, stream); break;
-    case GU_BFS_CTA_WARP: launch_variant<GU_BFS_CTA_WARP>(a, sms, stream); break;
-    case GU_BFS_SCAN: launch_variant<GU_BFS_SCAN>(a, sms, stream); break;
-    case GU_BFS_SHUFFLE: launch_variant<GU_BFS_SHUFFLE>(a, sms, stream); break;
-    case GU_BFS_BOTTOM_UP: launch_variant<GU_BFS_BOTTOM_UP>(a, sms, stream); break;
+    case GU_BFS_AUTO: launch_words<GU_BFS_AUTO>(a, W, sms, stream); break;
+    case GU_BFS_LINEAR: launch_words<GU_BFS_LINEAR>(a, W, sms, stream); break;
+    case GU_BFS_EDGE: launch_words<GU_BFS_EDGE>(a, W, sms, stream); break;
+    case GU_BFS_WARP: launch_words<GU_BFS_WARP>(a, W, sms, stream); break;
+    case GU_BFS_CTA_WARP: launch_words<GU_BFS_CTA_WARP>(a, W, sms, stream); break;
+    case GU_BFS_SCAN: launch_words<GU_BFS_SCAN>(a, W, sms, stream); break;
+    case GU_BFS_SHUFFLE: launch_words<GU_BFS_SHUFFLE>(a, W, sms, stream); break;
+    case GU_BFS_BOTTOM_UP: launch_words<GU_BFS_BOTTOM_UP>(a, W, sms, stream); break;
     default: throw gu_error(GU_ERR_INVALID_ARGUMENT, "unknown BFS variant");
     }
     g.mark_stop(stream);
