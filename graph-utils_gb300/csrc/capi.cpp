@@ -13,6 +13,8 @@ namespace gu {
 DeviceGraph *create_device_graph(const int32_t *R, const int32_t *C, int32_t n, int64_t m, bool directed,
                                  cudaStream_t stream);
 void msbfs_read_status(DeviceGraph &g, int *dev_err, int *td_levels, int *bu_levels, int *max_level);
+int msbfs_read_timeline(DeviceGraph &g, int max_entries, int32_t *batch, int32_t *level, int32_t *kind,
+                        int64_t *frontier_vertices, int64_t *frontier_edges, double *t_ms);
 
 static thread_local std::string t_last_error;
 void set_last_error(const std::string &msg) { t_last_error = msg; }
@@ -278,6 +280,21 @@ gu_status gu_graph_last_launch(gu_graph g, double *kernel_seconds, int *td_level
         if (td_levels) *td_levels = td;
         if (bu_levels) *bu_levels = bu;
         if (max_level) *max_level = ml;
+    });
+}
+
+gu_status gu_graph_level_profile(gu_graph g, int max_entries, int32_t *batch, int32_t *level, int32_t *kind,
+                                 int64_t *frontier_vertices, int64_t *frontier_edges, double *t_ms, int *count)
+{
+    return guarded([&] {
+        if (!g || max_entries < 0) throw gu_error(GU_ERR_INVALID_ARGUMENT, "bad arguments");
+        DeviceGraph &dg = *g->g;
+        std::lock_guard<std::mutex> lk(dg.mu);
+        DeviceScope ds(dg.device);
+        if (!dg.timed || !dg.ws.ptr) throw gu_error(GU_ERR_INVALID_ARGUMENT, "no launch recorded on this graph yet");
+        GU_CUDA_CHECK(cudaEventSynchronize(dg.ev_stop));
+        const int c = msbfs_read_timeline(dg, max_entries, batch, level, kind, frontier_vertices, frontier_edges, t_ms);
+        if (count) *count = c;
     });
 }
 

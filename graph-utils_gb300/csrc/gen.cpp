@@ -305,6 +305,20 @@ std::vector<int32_t> gen_sources(int32_t n, int32_t k, uint64_t seed)
     return idx;
 }
 
+// Reorders every adjacency list C[R[v]..R[v+1]) by descending key[neighbour]
+// (ties by ascending id).  Search results do not depend on the order of a
+// list; bottom-up levels stop scanning a list early once its first entries
+// cover every missing source, and high-degree neighbours are the likeliest to.
+void sort_adjacency_by_key(const int32_t *R, int32_t *C, int32_t n, const int32_t *key)
+{
+    parallel_for(n, [&](int64_t lo, int64_t hi) {
+        for (int64_t v = lo; v < hi; ++v)
+            std::sort(C + R[v], C + R[v + 1], [&](int32_t x, int32_t y) {
+                return key[x] != key[y] ? key[x] > key[y] : x < y;
+            });
+    });
+}
+
 HostGraph transpose(const HostGraph &g)
 {
     HostGraph t;

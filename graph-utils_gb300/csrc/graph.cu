@@ -79,6 +79,7 @@ DeviceGraph::~DeviceGraph()
     io.release();
     if (F) cudaFree(F);
     if (heavy) cudaFree(heavy);
+    if (mid) cudaFree(mid);
     if (RT && RT != R) cudaFree(RT);
     if (CT && CT != C) cudaFree(CT);
     if (R) cudaFree(R);
@@ -130,10 +131,17 @@ DeviceGraph *create_device_graph(const int32_t *R, const int32_t *C, int32_t n, 
     g->m = m;
     g->directed = directed;
     g->max_degree = maxdeg;
+    // Adjacency lists are stored by descending neighbour out-degree (ties by
+    // id): search results are independent of list order, and bottom-up scans
+    // meet the hubs, which most sources reach first, at the head of each list.
+    std::vector<int32_t> outdeg((size_t)n);
+    for (int32_t v = 0; v < n; ++v) outdeg[v] = R[v + 1] - R[v];
+    std::vector<int32_t> Cs(C, C + m);
+    sort_adjacency_by_key(R, Cs.data(), n, outdeg.data());
     GU_CUDA_CHECK(cudaMalloc(&g->R, sizeof(int32_t) * ((size_t)n + 1)));
     GU_CUDA_CHECK(cudaMalloc(&g->C, sizeof(int32_t) * (size_t)(m > 0 ? m : 1)));
     GU_CUDA_CHECK(cudaMemcpyAsync(g->R, R, sizeof(int32_t) * ((size_t)n + 1), cudaMemcpyHostToDevice, stream));
-    if (m > 0) GU_CUDA_CHECK(cudaMemcpyAsync(g->C, C, sizeof(int32_t) * (size_t)m, cudaMemcpyHostToDevice, stream));
+    if (m > 0) GU_CUDA_CHECK(cudaMemcpyAsync(g->C, Cs.data(), sizeof(int32_t) * (size_t)m, cudaMemcpyHostToDevice, stream));
     g->bytes = sizeof(int32_t) * ((size_t)n + 1 + (size_t)m);
     if (directed) {
         HostGraph h;
@@ -141,6 +149,7 @@ DeviceGraph *create_device_graph(const int32_t *R, const int32_t *C, int32_t n, 
         h.R.assign(R, R + n + 1);
         h.C.assign(C, C + m);
         HostGraph t = transpose(h);
+        sort_adjacency_by_key(t.R.data(), t.C.data(), n, outdeg.data());
         GU_CUDA_CHECK(cudaMalloc(&g->RT, sizeof(int32_t) * ((size_t)n + 1)));
         GU_CUDA_CHECK(cudaMalloc(&g->CT, sizeof(int32_t) * (size_t)(m > 0 ? m : 1)));
         GU_CUDA_CHECK(cudaMemcpyAsync(g->RT, t.R.data(), sizeof(int32_t) * ((size_t)n + 1), cudaMemcpyHostToDevice, stream));
@@ -152,24 +161,27 @@ DeviceGraph *create_device_graph(const int32_t *R, const int32_t *C, int32_t n, 
         g->CT = g->C;
     }
     {
-        // static list of heavy vertices by in-degree
-        std::vector<int32_t> heavy;
+        // static lists of the bottom-up degree classes, by in-degree
+        std::vector<int32_t> heavy, mid;
+        std::vector<int32_t> indeg((size_t)n, 0);
         if (directed) {
-            std::vector<int32_t> indeg((size_t)n, 0);
             for (int64_t e = 0; e < m; ++e) indeg[C[e]]++;
-            for (int32_t v = 0; v < n; ++v)
-                if (indeg[v] > BU_HEAVY_DEGREE) heavy.push_back(v);
         } else {
-            for (int32_t v = 0; v < n; ++v)
-                if (R[v + 1] - R[v] > BU_HEAVY_DEGREE) heavy.push_back(v);
+            for (int32_t v = 0; v < n; ++v) indeg[v] = R[v + 1] - R[v];
         }
-        g->nheavy = (int32_t)heavy.size();
-        if (!heavy.empty()) {
-            GU_CUDA_CHECK(cudaMalloc(&g->heavy, sizeof(int32_t) * heavy.size()));
-            GU_CUDA_CHECK(cudaMemcpyAsync(g->heavy, heavy.data(), sizeof(int32_t) * heavy.size(),
-                                          cudaMemcpyHostToDevice, stream));
-            g->bytes += sizeof(int32_t) * heavy.size();
+        for (int32_t v = 0; v < n; ++v) {
+            if (indeg[v] > BU_HEAVY_DEGREE) heavy.push_back(v);
+            else if (indeg[v] > BU_LIGHT_DEGREE) mid.push_back(v);
         }
+        auto upload = [&](const std::vector<int32_t> &src, int32_t *&dst, int32_t &cnt) {
+            cnt = (int32_t)src.size();
+            if (src.empty()) return;
+            GU_CUDA_CHECK(cudaMalloc(&dst, sizeof(int32_t) * src.size()));
+            GU_CUDA_CHECK(cudaMemcpyAsync(dst, src.data(), sizeof(int32_t) * src.size(), cudaMemcpyHostToDevice, stream));
+            g->bytes += sizeof(int32_t) * src.size();
+        };
+        upload(heavy, g->heavy, g->nheavy);
+        upload(mid, g->mid, g->nmid);
         GU_CUDA_CHECK(cudaStreamSynchronize(stream));
     }
     return g.release();

@@ -19,7 +19,13 @@
 
 namespace gu {
 
-constexpr int BU_HEAVY_DEGREE = 64;
+// Bottom-up degree classes (by in-degree): <= BU_LIGHT_DEGREE one thread per
+// vertex, <= BU_HEAVY_DEGREE eight lanes per vertex, above that a whole warp.
+constexpr int BU_LIGHT_DEGREE = 8;
+constexpr int BU_HEAVY_DEGREE = 128;
+// Every workspace starts with this many bytes of launch control block and
+// profiling timeline; kernel scratch follows.
+constexpr size_t WS_CONTROL_BYTES = 65536;
 
 // Device-side error codes written to a launch's control block.
 enum DevErr : int {
@@ -59,6 +65,7 @@ HostGraph gen_grid(int32_t rows, int32_t cols, double p_delete, uint64_t seed);
 HostGraph gen_dag(int32_t n, int64_t m, uint64_t seed);
 std::vector<int32_t> gen_sources(int32_t n, int32_t k, uint64_t seed);
 HostGraph transpose(const HostGraph &g);
+void sort_adjacency_by_key(const int32_t *R, int32_t *C, int32_t n, const int32_t *key);
 void build_csr(int32_t n, const std::vector<int32_t> &eu, const std::vector<int32_t> &ev, bool symmetric,
                std::vector<int32_t> &R, std::vector<int32_t> &C);
 
@@ -88,6 +95,9 @@ struct DeviceGraph {
     // levels scan their in-edges with a whole warp instead of one thread)
     int32_t *heavy = nullptr;
     int32_t nheavy = 0;
+    // vertices with BU_LIGHT_DEGREE < in-degree <= BU_HEAVY_DEGREE, ascending
+    int32_t *mid = nullptr;
+    int32_t nmid = 0;
     size_t bytes = 0;
     std::mutex mu;  // serialises calls on one handle (workspace reuse)
     Workspace ws;  // kernel scratch

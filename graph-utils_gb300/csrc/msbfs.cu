@@ -7,27 +7,30 @@
 // A batch holds 64*W sources (W 64-bit words, W in {1,2,4}).  Bit i of word q
 // of every per-vertex record stands for source row0 + 64q + i.  State, in SoA
 // layout with the W words of one vertex contiguous (16/32-byte vector access):
-//   seen[n][W]    sources that reached the vertex in an earlier level
-//   f[3][n][W]    frontier bitmaps F_j, rotating over three levels
-//   stamp[n]      last level that appended the vertex to a queue (W > 1)
-//   q[3], qoff[3] frontier queues; qoff[i] = out-edges of q[0..i) (an exclusive
-//                 prefix sum reserved together with the slot, so the next level
-//                 can split the frontier's edges evenly without a scan)
-// For n = 2^20 and W = 4 a frontier array is 32 MiB and stays in the 126 MiB
-// L2, so the random per-edge reads of bottom-up levels are L2 hits.
+//   seen[n][W]      sources that reached the vertex in an earlier level
+//   f[3][n][W]      frontier bitmaps F_j, rotating over three levels
+//   plane[P][n][W]  bit b of the BFS level of every (source, vertex) pair
+//   stamp[n]        last level that appended the vertex to a queue (W > 1)
+//   q[3], qoff[3]   frontier queues; qoff[i] = out-edges of q[0..i) (an
+//                   exclusive prefix sum reserved together with the slot, so
+//                   the next level splits the frontier's edges evenly)
+// For n = 2^20 and W = 4 one bitmap array is 32 MiB, so the arrays touched at
+// random during a level stay in the 126 MiB L2.  Distances are not written
+// during the search: the level bit-planes are transposed into the int32
+// distance rows once per batch, each row segment written whole and coalesced.
 //
 // Phase j of a batch (one grid barrier per level):
-//   * finalise F_{j-1}: seen |= F_{j-1}, write distance j-1 for its bits (done
-//     lazily; readers use seen|F_{j-1}, which is invariant during the phase)
+//   * finalise F_{j-1}: seen |= F_{j-1}, set the level bits of j-1 in the
+//     planes (lazily; readers use seen|F_{j-1}, invariant during the phase)
 //   * clear F_{j-2}
 //   * discover F_j top-down (gather the adjacency of the F_{j-1} queue and claim
 //     new bits with 64-bit atomicOr) or bottom-up (each vertex still missing
 //     some active source ORs its in-neighbours' F_{j-1} words, stopping as soon
 //     as every missing active source is found).
 // A source is active while its frontier is non-empty; the active mask of F_j is
-// OR-reduced per warp during phase j.  Direction: top-down -> bottom-up when the
-// frontier's out-edges exceed m / alpha, back when it holds fewer than n / beta
-// vertices (after Beamer, Asanovic, Patterson, SC'12).
+// OR-reduced per CTA in shared memory during phase j.  Direction: top-down ->
+// bottom-up when the frontier's out-edges exceed m / alpha, back when it holds
+// fewer than n / beta vertices (after Beamer, Asanovic, Patterson, SC'12).
 //
 // Top-down gather strategies restate the reference kernels' neighbour gathering
 // (file:line in include/gu.h); AUTO uses the edge-balanced merge-path gather.
@@ -40,11 +43,13 @@
 namespace gu {
 
 constexpr int MS_THREADS = 512;
+constexpr int MS_MIN_BLOCKS = 2;  // <= 64 registers: 2 CTAs (1024 threads) per SM
 constexpr int MAXW = 4;
+constexpr int MAX_PLANES = 31;              // levels < 2^31
+constexpr int EAGER_PLANES = 4;             // zeroed with the batch (levels < 16)
 constexpr int CTA_DEGREE_THRESHOLD = 2048;  // CTA_warp.cu:44
 constexpr int QPACK_SHIFT = 38;             // qpack = (count << 38) | edges
 constexpr u64 QPACK_EDGES = (1ull << QPACK_SHIFT) - 1ull;
-constexpr int LBS_CHUNK = 256;              // edges per warp task of the merge-path gather
 
 struct __align__(128) MsCtl {
     unsigned bar;
@@ -60,6 +65,34 @@ struct __align__(128) MsCtl {
 };
 static_assert(sizeof(MsCtl) <= 256, "control block must fit its reserved space");
 
+// Per-phase timeline (profiling hook).  Every CTA's thread 0 stamps the end of
+// its share of phase i (atomicMax of the global timer, so t_last_ns is the
+// slowest CTA); thread 0 of the grid also records what the phase was.
+constexpr int TIMELINE_MAX = 1024;
+struct MsEvent {
+    u64 t_last_ns;
+    int32_t batch, level;
+    int32_t bottom_up, qlen;
+    long long qedges;
+};
+constexpr size_t CTL_REGION = 256 + sizeof(MsEvent) * TIMELINE_MAX + sizeof(int) * 4;
+
+__device__ __forceinline__ void record_event(MsCtl *ctl, int i, bool describe, int batch, int level, int bu,
+                                             int qlen, long long qedges)
+{
+    MsEvent *ev = reinterpret_cast<MsEvent *>(reinterpret_cast<char *>(ctl) + 256);
+    if (i >= TIMELINE_MAX) return;
+    atomicMax(&ev[i].t_last_ns, global_timer_ns());
+    if (describe) {
+        ev[i].batch = batch;
+        ev[i].level = level;
+        ev[i].bottom_up = bu;
+        ev[i].qlen = qlen;
+        ev[i].qedges = qedges;
+        *reinterpret_cast<int *>(ev + TIMELINE_MAX) = i + 1;
+    }
+}
+
 struct MsArgs {
     const int32_t *__restrict__ R;
     const int32_t *__restrict__ C;
@@ -67,8 +100,10 @@ struct MsArgs {
     const int32_t *__restrict__ CT;
     const int32_t *__restrict__ F;
     const int32_t *__restrict__ heavy;
+    const int32_t *__restrict__ mid;
     int32_t n;
     int32_t nheavy;
+    int32_t nmid;
     int64_t m;
     const int32_t *sources;
     int32_t k;
@@ -76,6 +111,8 @@ struct MsArgs {
     int64_t ld;
     u64 *seen;
     u64 *fr[3];
+    u64 *plane;  // [nplanes][n][W]
+    int nplanes;
     int32_t *stamp;
     int32_t *q[3];
     int32_t *qoff[3];
@@ -96,9 +133,9 @@ struct Lvl {
     const u64 *fcur;
     u64 *fnxt;
     u64 *fprv;
-    int32_t lev;  // distance value of F_{j-1}
+    u64 *sact;    // shared-memory active-source accumulator of this CTA
+    int32_t lev;  // BFS level of F_{j-1}
     int32_t tag;  // stamp of level j (j + 1)
-    int row0;
     u64 active[MAXW];
 };
 
@@ -138,6 +175,13 @@ __device__ __forceinline__ void stw(u64 *p, const u64 (&x)[W])
 }
 
 template <int W>
+__device__ __forceinline__ void zerow(u64 *p)
+{
+    const u64 z[W] = {};
+    stw<W>(p, z);
+}
+
+template <int W>
 __device__ __forceinline__ bool anyw(const u64 (&x)[W])
 {
     u64 o = 0;
@@ -153,7 +197,8 @@ __device__ __forceinline__ unsigned lanemask_lt() { return (1u << lane_id()) - 1
 // 64-bit atomicAdd reserves both the queue slots and the range of their
 // out-edges.  The exclusive prefix of the degrees over the active lanes is a
 // bit-sliced ballot sum (works for any active mask).
-__device__ __forceinline__ void append_vertex(const MsArgs &a, const Lvl &L, int32_t w)
+__device__ __forceinline__ void append_vertex(const MsArgs &a, int slot, int32_t *qnxt, int32_t *qnxt_off,
+                                              int32_t w)
 {
     const unsigned deg = (unsigned)(__ldg(a.R + w + 1) - __ldg(a.R + w));
     const unsigned mask = __activemask();
@@ -167,79 +212,16 @@ __device__ __forceinline__ void append_vertex(const MsArgs &a, const Lvl &L, int
         tot += (u64)__popc(v) << b;
     }
     u64 old = 0;
-    if (lane == leader) old = atomicAdd(&a.ctl->qpack[L.slot], ((u64)__popc(mask) << QPACK_SHIFT) | tot);
+    if (lane == leader) old = atomicAdd(&a.ctl->qpack[slot], ((u64)__popc(mask) << QPACK_SHIFT) | tot);
     old = __shfl_sync(mask, old, leader);
     const int pos = (int)(old >> QPACK_SHIFT) + __popc(mask & lt);
-    L.qnxt[pos] = w;
-    L.qnxt_off[pos] = (int32_t)((old & QPACK_EDGES) + excl);
-}
-
-template <int W>
-__device__ __forceinline__ void flush_active(const MsArgs &a, int slot, const u64 (&disc)[W])
-{
-#pragma unroll
-    for (int q = 0; q < W; ++q) {
-        const u64 r = warp_or_u64(FULL_MASK, disc[q]);
-        if (lane_id() == 0 && r) atomicOr(&a.ctl->active[slot][q], r);
-    }
-}
-
-// ---- distance writes ---------------------------------------------------------------
-__device__ __forceinline__ void write_bits_serial(int32_t *dist, int64_t ld, int row0, int32_t v, u64 bits,
-                                                  int32_t val)
-{
-    while (bits) {
-        const int i = __ffsll((long long)bits) - 1;
-        bits &= bits - 1;
-        dist[(int64_t)(row0 + i) * ld + v] = val;
-    }
-}
-
-// Lanes hold consecutive vertices: for each source bit the stores of the warp
-// fall into one contiguous row segment.  Called by full warps.
-__device__ __forceinline__ void write_bits_sweep(int32_t *dist, int64_t ld, int row0, int32_t v, u64 bits,
-                                                 int32_t val)
-{
-    u64 u = warp_or_u64(FULL_MASK, bits);
-    while (u) {
-        const int i = __ffsll((long long)u) - 1;
-        u &= u - 1;
-        if ((bits >> i) & 1ull) dist[(int64_t)(row0 + i) * ld + v] = val;
-    }
-}
-
-template <class G>
-__device__ void init_dist_rows(int32_t *dist, int64_t ld, int row0, int nb, int32_t n)
-{
-    const long long rank = G::rank(), size = G::size();
-    if ((ld & 3) == 0 && (((uintptr_t)dist) & 15) == 0) {
-        const long long n4 = n >> 2;
-        const int4 inf4 = make_int4(INT_MAX, INT_MAX, INT_MAX, INT_MAX);
-        if (n4 > 0) {
-            const long long tot = (long long)nb * n4;
-            for (long long idx = rank; idx < tot; idx += size) {
-                const long long r = idx / n4, c = idx - r * n4;
-                reinterpret_cast<int4 *>(dist + (int64_t)(row0 + r) * ld)[c] = inf4;
-            }
-        }
-        const int tail = n & 3;
-        for (long long idx = rank; idx < (long long)nb * tail; idx += size) {
-            const long long r = idx / tail, c = idx - r * tail;
-            dist[(int64_t)(row0 + r) * ld + (n4 << 2) + c] = INT_MAX;
-        }
-    } else {
-        const long long tot = (long long)nb * n;
-        for (long long idx = rank; idx < tot; idx += size) {
-            const long long r = idx / n, c = idx - r * n;
-            dist[(int64_t)(row0 + r) * ld + c] = INT_MAX;
-        }
-    }
+    qnxt[pos] = w;
+    qnxt_off[pos] = (int32_t)((old & QPACK_EDGES) + excl);
 }
 
 // ---- top-down visit: frontier bits f arrive at vertex w over one edge ----------------
 template <int W>
-__device__ __forceinline__ void td_visit(const MsArgs &a, const Lvl &L, const u64 (&f)[W], int32_t w,
-                                         u64 (&disc)[W])
+__device__ __forceinline__ void td_visit(const MsArgs &a, const Lvl &L, const u64 (&f)[W], int32_t w)
 {
     const size_t o = (size_t)w * W;
     u64 s[W], c[W], x[W];
@@ -252,13 +234,46 @@ __device__ __forceinline__ void td_visit(const MsArgs &a, const Lvl &L, const u6
         const u64 nb = f[q] & ~(s[q] | c[q] | x[q]);
         if (nb) {
             const u64 old = atomicOr(L.fnxt + o + q, nb);
-            disc[q] |= nb;
             found = true;
             if (W == 1 && old == 0) first = true;
         }
     }
     if (W > 1 && found) first = atomicMax(a.stamp + w, L.tag) < L.tag;
-    if (first) append_vertex(a, L, w);
+    if (first) append_vertex(a, L.slot, L.qnxt, L.qnxt_off, w);
+}
+
+// Finalise F_{j-1} bits of one vertex: seen and the level bit-planes.  Only the
+// thread that owns the vertex in this phase calls it.
+template <int W>
+__device__ __forceinline__ void finalise(const MsArgs &a, int32_t lev, size_t o, const u64 (&f)[W], u64 (&s)[W])
+{
+#pragma unroll
+    for (int q = 0; q < W; ++q) s[q] |= f[q];
+    stw<W>(a.seen + o, s);
+    const size_t pstride = (size_t)a.n * W;
+    for (int b = 0; (lev >> b) != 0; ++b) {
+        if (!((lev >> b) & 1)) continue;
+        u64 *pp = a.plane + (size_t)b * pstride + o;
+        u64 pv[W];
+        ldw<W>(pp, pv);
+#pragma unroll
+        for (int q = 0; q < W; ++q) pv[q] |= f[q];
+        stw<W>(pp, pv);
+    }
+}
+
+// Sources with a non-empty F_{j-1}: OR of the finalised words, reduced per warp
+// and per CTA (shared), then once per CTA into the phase's control slot.  Read
+// at the start of phase j+1 it is a superset of the sources active in F_j,
+// which is all the bottom-up early exit needs.
+template <int W>
+__device__ __forceinline__ void flush_active(const Lvl &L, const u64 (&act)[W])
+{
+#pragma unroll
+    for (int q = 0; q < W; ++q) {
+        const u64 r = warp_or_u64(FULL_MASK, act[q]);
+        if (lane_id() == 0 && r) atomicOr(L.sact + q, r);
+    }
 }
 
 // Finalise F_{j-1} in queue order and clear F_{j-2}.
@@ -266,23 +281,19 @@ template <int W, class G>
 __device__ void td_update(const MsArgs &a, const Lvl &L)
 {
     const long long rank = G::rank(), size = G::size();
+    u64 act[W] = {};
     for (long long i = rank; i < L.qlen; i += size) {
         const int32_t v = __ldcg(L.qcur + i);
         const size_t o = (size_t)v * W;
         u64 f[W], s[W];
         ldw<W>(L.fcur + o, f);
         ldw<W>(a.seen + o, s);
+        finalise<W>(a, L.lev, o, f, s);
 #pragma unroll
-        for (int q = 0; q < W; ++q) s[q] |= f[q];
-        stw<W>(a.seen + o, s);
-#pragma unroll
-        for (int q = 0; q < W; ++q) write_bits_serial(a.dist, a.ld, L.row0 + 64 * q, v, f[q], L.lev);
+        for (int q = 0; q < W; ++q) act[q] |= f[q];
     }
-    const u64 zero[W] = {};
-    for (long long i = rank; i < L.qlen_prev; i += size) {
-        const int32_t v = __ldcg(L.qprev + i);
-        stw<W>(L.fprv + (size_t)v * W, zero);
-    }
+    flush_active<W>(L, act);
+    for (long long i = rank; i < L.qlen_prev; i += size) zerow<W>(L.fprv + (size_t)__ldcg(L.qprev + i) * W);
 }
 
 template <int W>
@@ -293,34 +304,34 @@ __device__ __forceinline__ void load_front(const Lvl &L, int32_t v, u64 (&f)[W])
 
 // LINEAR: thread per frontier vertex, serial adjacency (linear_with_atomics.cu:122-135).
 template <int W, class G>
-__device__ void gather_linear(const MsArgs &a, const Lvl &L, u64 (&disc)[W])
+__device__ void gather_linear(const MsArgs &a, const Lvl &L)
 {
     for (long long i = G::rank(); i < L.qlen; i += G::size()) {
         const int32_t v = __ldcg(L.qcur + i);
         u64 f[W];
         load_front<W>(L, v, f);
         const int32_t e1 = __ldg(a.R + v + 1);
-        for (int32_t e = __ldg(a.R + v); e < e1; ++e) td_visit<W>(a, L, f, __ldg(a.C + e), disc);
+        for (int32_t e = __ldg(a.R + v); e < e1; ++e) td_visit<W>(a, L, f, __ldg(a.C + e));
     }
 }
 
 // EDGE: every CSR entry every level, source vertex from the COO array
 // (edge_parallel.cu:77-88); one sweep serves every source of the batch.
 template <int W, class G>
-__device__ void gather_edge(const MsArgs &a, const Lvl &L, u64 (&disc)[W])
+__device__ void gather_edge(const MsArgs &a, const Lvl &L)
 {
     for (long long e = G::rank(); e < a.m; e += G::size()) {
         const int32_t u = __ldg(a.F + e);
         u64 f[W];
         load_front<W>(L, u, f);
-        if (anyw<W>(f)) td_visit<W>(a, L, f, __ldg(a.C + e), disc);
+        if (anyw<W>(f)) td_visit<W>(a, L, f, __ldg(a.C + e));
     }
 }
 
 // SHUFFLE: warp per frontier vertex; warps take the next vertex from a shared
 // counter when done (shuffle_based.cuh:192-223).
 template <int W, class G>
-__device__ void gather_shuffle(const MsArgs &a, const Lvl &L, u64 (&disc)[W])
+__device__ void gather_shuffle(const MsArgs &a, const Lvl &L)
 {
     const int lane = lane_id();
     const long long nw = G::size() >> 5;
@@ -330,7 +341,7 @@ __device__ void gather_shuffle(const MsArgs &a, const Lvl &L, u64 (&disc)[W])
         u64 f[W];
         load_front<W>(L, v, f);
         const int32_t e1 = __ldg(a.R + v + 1);
-        for (int32_t e = __ldg(a.R + v) + lane; e < e1; e += 32) td_visit<W>(a, L, f, __ldg(a.C + e), disc);
+        for (int32_t e = __ldg(a.R + v) + lane; e < e1; e += 32) td_visit<W>(a, L, f, __ldg(a.C + e));
         int nk = 0;
         if (lane == 0) nk = atomicAdd(&a.ctl->work[L.slot], 1);
         kq = nw + __shfl_sync(FULL_MASK, nk, 0);
@@ -341,8 +352,7 @@ __device__ void gather_shuffle(const MsArgs &a, const Lvl &L, u64 (&disc)[W])
 // highest lane with adjacency left (race_and_resolve) and gathers its list
 // together (warp_based.cu:109-145).
 template <int W>
-__device__ __forceinline__ void warp_stripmine(const MsArgs &a, const Lvl &L, int32_t r, int32_t r_end, int32_t v,
-                                               u64 (&disc)[W])
+__device__ __forceinline__ void warp_stripmine(const MsArgs &a, const Lvl &L, int32_t r, int32_t r_end, int32_t v)
 {
     const int lane = lane_id();
     while (__any_sync(FULL_MASK, r < r_end)) {
@@ -353,12 +363,12 @@ __device__ __forceinline__ void warp_stripmine(const MsArgs &a, const Lvl &L, in
         if (lane == winner) r = r_end;  // a lane cannot win twice
         u64 f[W];
         load_front<W>(L, vw, f);
-        for (int32_t e = rw + lane; e < re; e += 32) td_visit<W>(a, L, f, __ldg(a.C + e), disc);
+        for (int32_t e = rw + lane; e < re; e += 32) td_visit<W>(a, L, f, __ldg(a.C + e));
     }
 }
 
 template <int W, class G>
-__device__ void gather_warp(const MsArgs &a, const Lvl &L, u64 (&disc)[W])
+__device__ void gather_warp(const MsArgs &a, const Lvl &L)
 {
     const int lane = lane_id();
     const long long nw = G::size() >> 5;
@@ -370,14 +380,14 @@ __device__ void gather_warp(const MsArgs &a, const Lvl &L, u64 (&disc)[W])
             r = __ldg(a.R + v);
             r_end = __ldg(a.R + v + 1);
         }
-        warp_stripmine<W>(a, L, r, r_end, v, disc);
+        warp_stripmine<W>(a, L, r, r_end, v);
     }
 }
 
 // CTA_WARP: lists longer than 2048 are gathered by the whole CTA, one at a
 // time (highest thread first), the rest by warp strip-mining (CTA_warp.cu:62-265).
 template <int W, class G>
-__device__ void gather_cta_warp(const MsArgs &a, const Lvl &L, u64 (&disc)[W])
+__device__ void gather_cta_warp(const MsArgs &a, const Lvl &L)
 {
     __shared__ int s_winner;
     __shared__ int32_t s_r, s_re, s_v;
@@ -407,10 +417,10 @@ __device__ void gather_cta_warp(const MsArgs &a, const Lvl &L, u64 (&disc)[W])
             const int32_t re = s_re;
             u64 f[W];
             load_front<W>(L, s_v, f);
-            for (int32_t e = s_r + threadIdx.x; e < re; e += BD) td_visit<W>(a, L, f, __ldg(a.C + e), disc);
+            for (int32_t e = s_r + threadIdx.x; e < re; e += BD) td_visit<W>(a, L, f, __ldg(a.C + e));
             __syncthreads();
         }
-        warp_stripmine<W>(a, L, r, r_end, v, disc);
+        warp_stripmine<W>(a, L, r, r_end, v);
         __syncthreads();
     }
 }
@@ -449,7 +459,7 @@ __device__ __forceinline__ int block_exclusive_scan(int x, int *total, int *s_wa
 // exclusive scan, then threads take consecutive edge slots and find the owning
 // vertex by binary search over the scanned offsets (scan_based.cu:107-149).
 template <int W, class G>
-__device__ void gather_scan(const MsArgs &a, const Lvl &L, u64 (&disc)[W])
+__device__ void gather_scan(const MsArgs &a, const Lvl &L)
 {
     __shared__ int s_off[MS_THREADS];
     __shared__ int32_t s_r[MS_THREADS];
@@ -480,16 +490,15 @@ __device__ void gather_scan(const MsArgs &a, const Lvl &L, u64 (&disc)[W])
             }
             u64 f[W];
             load_front<W>(L, s_v[lo], f);
-            td_visit<W>(a, L, f, __ldg(a.C + s_r[lo] + (e - s_off[lo])), disc);
+            td_visit<W>(a, L, f, __ldg(a.C + s_r[lo] + (e - s_off[lo])));
         }
         __syncthreads();
     }
 }
 
 // Merge-path gather (AUTO): the frontier's out-edges, ranked by the edge
-// offsets reserved at append time, are cut into chunks of LBS_CHUNK; a warp
-// takes a chunk, brackets its owners [k0, k1] by two binary searches, and each
-// lane finds the owner of its edge slot within that bracket (the
+// offsets reserved at append time, are cut into equal tasks, and the owner of
+// every edge slot is found by binary search over those offsets (the
 // load-balanced search of load_balanced_search.cu:123-192, grid-wide).
 __device__ __forceinline__ int owner_search(const int32_t *off, int lo, int hi, long long e)
 {
@@ -501,27 +510,63 @@ __device__ __forceinline__ int owner_search(const int32_t *off, int lo, int hi, 
     return lo;
 }
 
+// A CTA takes MP_TASK consecutive edge slots; two threads bracket the owners
+// [k0, k1] by binary search in global memory, the CTA stages the owners' ids,
+// offsets and CSR starts in shared memory, and every thread then resolves its
+// edge slots by binary search in shared memory.  Tasks whose bracket exceeds
+// the shared capacity (many tiny lists) are walked owner by owner.
+constexpr int MP_TASK = MS_THREADS * 8;
+constexpr int MP_STAGE = 1024;
+
 template <int W, class G>
-__device__ void gather_lbs(const MsArgs &a, const Lvl &L, u64 (&disc)[W])
+__device__ void gather_mp(const MsArgs &a, const Lvl &L)
 {
+    __shared__ int32_t s_off[MP_STAGE];
+    __shared__ int32_t s_v[MP_STAGE];
+    __shared__ int32_t s_r[MP_STAGE];
+    __shared__ int s_k[2];
     const long long E = L.qedges;
     if (E == 0) return;
-    const long long ntask = (E + LBS_CHUNK - 1) / LBS_CHUNK;
-    const long long nw = G::size() >> 5;
-    const int lane = lane_id();
-    for (long long t = G::rank() >> 5; t < ntask; t += nw) {
-        const long long e0 = t * LBS_CHUNK;
-        const long long e1 = min(E, e0 + LBS_CHUNK);
-        const int k0 = owner_search(L.qcur_off, 0, L.qlen - 1, e0);
-        const int k1 = owner_search(L.qcur_off, k0, L.qlen - 1, e1 - 1);
-        for (long long e = e0 + lane; e < e1; e += 32) {
-            const int k = owner_search(L.qcur_off, k0, k1, e);
-            const int32_t v = __ldcg(L.qcur + k);
-            u64 f[W];
-            load_front<W>(L, v, f);
-            const int32_t w = __ldg(a.C + __ldg(a.R + v) + (int32_t)(e - __ldcg(L.qcur_off + k)));
-            td_visit<W>(a, L, f, w, disc);
+    const long long ntask = (E + MP_TASK - 1) / MP_TASK;
+    for (long long t = G::blk(); t < ntask; t += G::nblk()) {
+        const long long e0 = t * MP_TASK;
+        const long long e1 = min(E, e0 + MP_TASK);
+        if (threadIdx.x == 0) s_k[0] = owner_search(L.qcur_off, 0, L.qlen - 1, e0);
+        if (threadIdx.x == 32) s_k[1] = owner_search(L.qcur_off, 0, L.qlen - 1, e1 - 1);
+        __syncthreads();
+        const int k0 = s_k[0], nk = s_k[1] - k0 + 1;
+        if (nk <= MP_STAGE) {
+            for (int i = threadIdx.x; i < nk; i += blockDim.x) {
+                const int32_t v = __ldcg(L.qcur + k0 + i);
+                s_v[i] = v;
+                s_off[i] = __ldcg(L.qcur_off + k0 + i);
+                s_r[i] = __ldg(a.R + v);
+            }
+            __syncthreads();
+            for (long long e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
+                int lo = 0, hi = nk - 1;
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if ((long long)s_off[mid] <= e) lo = mid;
+                    else hi = mid - 1;
+                }
+                u64 f[W];
+                load_front<W>(L, s_v[lo], f);
+                td_visit<W>(a, L, f, __ldg(a.C + s_r[lo] + (int32_t)(e - s_off[lo])));
+            }
+        } else {
+            for (int i = threadIdx.x; i < nk; i += blockDim.x) {
+                const int32_t v = __ldcg(L.qcur + k0 + i);
+                const long long off = __ldcg(L.qcur_off + k0 + i);
+                const int32_t r = __ldg(a.R + v), deg = __ldg(a.R + v + 1) - r;
+                const long long lo_e = max(off, e0), hi_e = min(off + deg, e1);
+                if (lo_e >= hi_e) continue;
+                u64 f[W];
+                load_front<W>(L, v, f);
+                for (long long e = lo_e; e < hi_e; ++e) td_visit<W>(a, L, f, __ldg(a.C + r + (int32_t)(e - off)));
+            }
         }
+        __syncthreads();
     }
 }
 
@@ -548,35 +593,28 @@ __device__ __forceinline__ void or_front(const Lvl &L, int32_t v, u64 (&acc)[W])
 }
 
 template <int W, class G>
-__device__ void bu_sweep(const MsArgs &a, const Lvl &L, u64 (&disc)[W])
+__device__ void bu_sweep(const MsArgs &a, const Lvl &L)
 {
-    const int lane = lane_id();
     const long long size = G::size();
-    const u64 zero[W] = {};
-    for (long long base = G::rank() - lane; base < a.n; base += size) {
-        const int32_t w = (int32_t)(base + lane);
-        const bool valid = w < a.n;
-        u64 s[W] = {}, f[W] = {};
-        if (valid) {
-            const size_t o = (size_t)w * W;
-            ldw<W>(a.seen + o, s);
-            ldw<W>(L.fcur + o, f);
-            if (anyw<W>(f)) {
+    u64 act[W] = {};
+    for (long long wl = G::rank(); wl < a.n; wl += size) {
+        const int32_t w = (int32_t)wl;
+        const size_t o = (size_t)w * W;
+        u64 s[W], f[W];
+        ldw<W>(a.seen + o, s);
+        ldw<W>(L.fcur + o, f);
+        if (anyw<W>(f)) {
+            finalise<W>(a, L.lev, o, f, s);
 #pragma unroll
-                for (int q = 0; q < W; ++q) s[q] |= f[q];
-                stw<W>(a.seen + o, s);
-            }
-            stw<W>(L.fprv + o, zero);
+            for (int q = 0; q < W; ++q) act[q] |= f[q];
         }
-#pragma unroll
-        for (int q = 0; q < W; ++q) write_bits_sweep(a.dist, a.ld, L.row0 + 64 * q, w, f[q], L.lev);
-        if (!valid) continue;
+        zerow<W>(L.fprv + o);
         u64 need[W];
 #pragma unroll
         for (int q = 0; q < W; ++q) need[q] = L.active[q] & ~s[q];
         if (!anyw<W>(need)) continue;
         const int32_t e0 = __ldg(a.RT + w), e1 = __ldg(a.RT + w + 1);
-        if (e1 - e0 > BU_HEAVY_DEGREE || e1 == e0) continue;  // heavy: bu_heavy
+        if (e1 - e0 > BU_LIGHT_DEGREE || e1 == e0) continue;  // mid / heavy classes: bu_mid, bu_heavy
         u64 acc[W] = {};
         for (int32_t e = e0; e < e1; e += 4) {
             const int32_t c0 = __ldg(a.CT + e);
@@ -593,18 +631,57 @@ __device__ void bu_sweep(const MsArgs &a, const Lvl &L, u64 (&disc)[W])
 #pragma unroll
         for (int q = 0; q < W; ++q) nb[q] = acc[q] & need[q];
         if (anyw<W>(nb)) {
-            stw<W>(L.fnxt + (size_t)w * W, nb);
+            stw<W>(L.fnxt + o, nb);
+            append_vertex(a, L.slot, L.qnxt, L.qnxt_off, w);
+        }
+    }
+    flush_active<W>(L, act);
+}
+
+// Mid-degree vertices (BU_LIGHT_DEGREE < in-degree <= BU_HEAVY_DEGREE): eight
+// lanes per vertex OR eight in-neighbours per step; the group stops once every
+// missing active source is found.
+template <int W, class G>
+__device__ void bu_mid(const MsArgs &a, const Lvl &L)
+{
+    const int lane = lane_id();
+    const int sub = lane & 7;
+    const unsigned gmask = 0xFFu << (lane & ~7);
+    const long long ngroups = G::size() >> 3;
+    for (long long i = G::rank() >> 3; i < a.nmid; i += ngroups) {
+        const int32_t w = __ldg(a.mid + i);
+        const size_t o = (size_t)w * W;
+        u64 s[W], f[W], need[W];
+        ldw<W>(a.seen + o, s);
+        ldw<W>(L.fcur + o, f);
 #pragma unroll
-            for (int q = 0; q < W; ++q) disc[q] |= nb[q];
-            append_vertex(a, L, w);
+        for (int q = 0; q < W; ++q) need[q] = L.active[q] & ~(s[q] | f[q]);
+        if (!anyw<W>(need)) continue;
+        const int32_t e0 = __ldg(a.RT + w), e1 = __ldg(a.RT + w + 1);
+        u64 acc[W] = {};
+        for (int32_t eb = e0; eb < e1; eb += 8) {
+            u64 x[W] = {};
+            const int32_t e = eb + sub;
+            if (e < e1) ldw<W>(L.fcur + (size_t)__ldg(a.CT + e) * W, x);
+#pragma unroll
+            for (int q = 0; q < W; ++q) acc[q] |= warp_or_u64(gmask, x[q]);
+            if (covers<W>(acc, need)) break;
+        }
+        u64 nb[W];
+#pragma unroll
+        for (int q = 0; q < W; ++q) nb[q] = acc[q] & need[q];
+        if (sub == 0 && anyw<W>(nb)) {
+            stw<W>(L.fnxt + o, nb);
+            append_vertex(a, L.slot, L.qnxt, L.qnxt_off, w);
         }
     }
 }
 
-// Heavy vertices (in-degree > BU_HEAVY_DEGREE): a warp per vertex ORs 32
-// in-neighbours per step and stops once every missing active source is found.
+// Heavy vertices (in-degree > BU_HEAVY_DEGREE): a warp per vertex ORs 64
+// in-neighbours per step (two loads in flight per lane) and stops once every
+// missing active source is found.
 template <int W, class G>
-__device__ void bu_heavy(const MsArgs &a, const Lvl &L, u64 (&disc)[W])
+__device__ void bu_heavy(const MsArgs &a, const Lvl &L)
 {
     const int lane = lane_id();
     const long long nw = G::size() >> 5;
@@ -619,10 +696,13 @@ __device__ void bu_heavy(const MsArgs &a, const Lvl &L, u64 (&disc)[W])
         if (!anyw<W>(need)) continue;
         const int32_t e0 = __ldg(a.RT + w), e1 = __ldg(a.RT + w + 1);
         u64 acc[W] = {};
-        for (int32_t eb = e0; eb < e1; eb += 32) {
+        for (int32_t eb = e0; eb < e1; eb += 64) {
             u64 x[W] = {};
-            const int32_t e = eb + lane;
-            if (e < e1) ldw<W>(L.fcur + (size_t)__ldg(a.CT + e) * W, x);
+            const int32_t ea = eb + lane, ebb = eb + 32 + lane;
+            const int32_t ca = ea < e1 ? __ldg(a.CT + ea) : -1;
+            const int32_t cb = ebb < e1 ? __ldg(a.CT + ebb) : -1;
+            if (ca >= 0) or_front<W>(L, ca, x);
+            if (cb >= 0) or_front<W>(L, cb, x);
 #pragma unroll
             for (int q = 0; q < W; ++q) acc[q] |= warp_or_u64(FULL_MASK, x[q]);
             if (covers<W>(acc, need)) break;
@@ -632,36 +712,134 @@ __device__ void bu_heavy(const MsArgs &a, const Lvl &L, u64 (&disc)[W])
         for (int q = 0; q < W; ++q) nb[q] = acc[q] & need[q];
         if (lane == 0 && anyw<W>(nb)) {
             stw<W>(L.fnxt + o, nb);
+            append_vertex(a, L.slot, L.qnxt, L.qnxt_off, w);
+        }
+    }
+}
+
+// Distance rows of one batch from seen and the level bit-planes.
+//
+// Fast path (levels < 256, 16-byte aligned rows): a CTA takes a tile of
+// blockDim consecutive vertices and one 64-source word; each thread decodes its
+// vertex's levels 16 rows at a time into a shared [16][blockDim] tile, and the
+// CTA writes each row's segment (2 KiB for 512 vertices) with contiguous int4
+// stores.  Otherwise lanes hold consecutive vertices and store one int each.
+constexpr int WD_ROWS = 16;
+
+template <int W, class G>
+__device__ void write_distances(const MsArgs &a, int row0, int nb, int nplanes_used)
+{
+    __shared__ __align__(16) int32_t tile[WD_ROWS][MS_THREADS];
+    const int BD = blockDim.x;
+    if (nplanes_used <= 8 && (a.ld & 3) == 0 && (((uintptr_t)a.dist) & 15) == 0 && BD == MS_THREADS) {
+        const size_t pstride = (size_t)a.n * W;
+        const long long ntile = ((long long)a.n + BD - 1) / BD;
+        const int nq = (nb + 63) / 64;
+        for (long long t = G::blk(); t < ntile * nq; t += G::nblk()) {
+            const int q = (int)(t % nq);
+            const int32_t vbase = (int32_t)((t / nq) * BD);
+            const int32_t v = vbase + threadIdx.x;
+            const bool valid = v < a.n;
+            const size_t o = (size_t)v * W + q;
+            const u64 s = valid ? __ldcg(a.seen + o) : 0ull;
+            u64 pl[8];
 #pragma unroll
-            for (int q = 0; q < W; ++q) disc[q] |= nb[q];
-            append_vertex(a, L, w);
+            for (int b = 0; b < 8; ++b) pl[b] = (b < nplanes_used && valid) ? __ldcg(a.plane + b * pstride + o) : 0ull;
+            const int rows = min(64, nb - 64 * q);
+            const int nv = min(BD, a.n - vbase);  // vertices in this tile
+            for (int r0 = 0; r0 < rows; r0 += WD_ROWS) {
+#pragma unroll
+                for (int i = 0; i < WD_ROWS; ++i) {
+                    const int bit = r0 + i;
+                    int32_t lvl = 0;
+#pragma unroll
+                    for (int b = 0; b < 8; ++b) lvl |= (int32_t)((pl[b] >> bit) & 1ull) << b;
+                    tile[i][threadIdx.x] = ((s >> bit) & 1ull) ? lvl : INT_MAX;
+                }
+                __syncthreads();
+                const int nr = min(WD_ROWS, rows - r0);
+                const int nv4 = nv >> 2;
+                for (int k = threadIdx.x; k < nr * (BD >> 2); k += BD) {
+                    const int r = k / (BD >> 2), c4 = k - r * (BD >> 2);
+                    int32_t *drow = a.dist + (int64_t)(row0 + 64 * q + r0 + r) * a.ld + vbase;
+                    if (c4 < nv4) {
+                        reinterpret_cast<int4 *>(drow)[c4] = reinterpret_cast<const int4 *>(&tile[r][0])[c4];
+                    } else if (c4 == nv4) {
+                        for (int x = 4 * c4; x < nv; ++x) drow[x] = tile[r][x];
+                    }
+                }
+                __syncthreads();
+            }
+        }
+        return;
+    }
+    const int lane = lane_id();
+    const long long size = G::size();
+    const size_t pstride = (size_t)a.n * W;
+    for (long long base = G::rank() - lane; base < a.n; base += size) {
+        const int32_t v = (int32_t)(base + lane);
+        const bool valid = v < a.n;
+        for (int q = 0; q < W && 64 * q < nb; ++q) {
+            const size_t o = (size_t)v * W + q;
+            const u64 s = valid ? __ldcg(a.seen + o) : 0ull;
+            const int rows = min(64, nb - 64 * q);
+            int32_t *drow = a.dist + (int64_t)(row0 + 64 * q) * a.ld + v;
+            if (nplanes_used <= 8) {  // levels < 256: all planes in registers
+                u64 pl[8];
+#pragma unroll
+                for (int b = 0; b < 8; ++b)
+                    pl[b] = (b < nplanes_used && valid) ? __ldcg(a.plane + b * pstride + o) : 0ull;
+                for (int i = 0; i < rows; ++i) {
+                    int32_t lvl = 0;
+#pragma unroll
+                    for (int b = 0; b < 8; ++b) lvl |= (int32_t)((pl[b] >> i) & 1ull) << b;
+                    if (valid) drow[(int64_t)i * a.ld] = ((s >> i) & 1ull) ? lvl : INT_MAX;
+                }
+            } else {  // deep searches: 8 rows at a time, planes streamed
+                for (int i0 = 0; i0 < rows; i0 += 8) {
+                    int32_t lvl[8] = {};
+                    for (int b = 0; b < nplanes_used; ++b) {
+                        const u64 w8 = valid ? (__ldcg(a.plane + b * pstride + o) >> i0) : 0ull;
+#pragma unroll
+                        for (int t = 0; t < 8; ++t) lvl[t] |= (int32_t)((w8 >> t) & 1ull) << b;
+                    }
+#pragma unroll
+                    for (int t = 0; t < 8; ++t)
+                        if (valid && i0 + t < rows)
+                            drow[(int64_t)(i0 + t) * a.ld] = ((s >> (i0 + t)) & 1ull) ? lvl[t] : INT_MAX;
+                }
+            }
         }
     }
 }
 
 template <int VARIANT, int W>
-__global__ void __launch_bounds__(MS_THREADS) ms_grid_kernel(MsArgs a)
+__global__ void __launch_bounds__(MS_THREADS, MS_MIN_BLOCKS) ms_grid_kernel(MsArgs a)
 {
+    __shared__ u64 s_act[MAXW];
     unsigned epoch = 0;
+    int ev_idx = 0;
     MsCtl *ctl = a.ctl;
     const long long rank = GridG::rank(), size = GridG::size();
+    const size_t pstride = (size_t)a.n * W;
+    if (threadIdx.x < MAXW) s_act[threadIdx.x] = 0;
     const int bsz = 64 * W;
     const int nbatch = (a.k + bsz - 1) / bsz;
     for (int b = 0; b < nbatch; ++b) {
         const int row0 = b * bsz;
         const int nb = min(bsz, a.k - row0);
+        const int eager = min(EAGER_PLANES, a.nplanes);
         {
-            const u64 zero[W] = {};
-            for (long long w = rank; w < a.n; w += size) {
-                const size_t o = (size_t)w * W;
-                stw<W>(a.seen + o, zero);
-                stw<W>(a.fr[0] + o, zero);
-                stw<W>(a.fr[1] + o, zero);
-                stw<W>(a.fr[2] + o, zero);
-                if (W > 1) a.stamp[w] = 0;
-            }
+            // seen, f[0..2] and the eager planes are one contiguous region
+            // (256-byte aligned start): zero it with consecutive 16-byte stores
+            const size_t cnt = (size_t)((a.plane + eager * pstride) - a.seen);
+            ulonglong2 *v2 = reinterpret_cast<ulonglong2 *>(a.seen);
+            const ulonglong2 z2 = make_ulonglong2(0ull, 0ull);
+            for (long long i = rank; i < (long long)(cnt >> 1); i += size) v2[i] = z2;
+            if ((cnt & 1) && rank == 0) a.seen[cnt - 1] = 0ull;
+            if (W > 1)
+                for (long long w = rank; w < a.n; w += size) a.stamp[w] = 0;
         }
-        init_dist_rows<GridG>(a.dist, a.ld, row0, nb, a.n);
         if (rank < 4) {
             ctl->qpack[rank] = 0;
             ctl->work[rank] = 0;
@@ -678,18 +856,15 @@ __global__ void __launch_bounds__(MS_THREADS) ms_grid_kernel(MsArgs a)
             bool first;
             if (W == 1) first = old == 0;
             else first = atomicMax(a.stamp + s, 1) < 1;
-            if (first) {
-                Lvl L0;
-                L0.slot = 0;
-                L0.qnxt = a.q[0];
-                L0.qnxt_off = a.qoff[0];
-                append_vertex(a, L0, s);
-            }
+            if (first) append_vertex(a, 0, a.q[0], a.qoff[0], s);
         }
+        if (threadIdx.x == 0) record_event(ctl, ev_idx, rank == 0, b, 0, 4, nb, 0);  // batch initialised, seeded
+        ++ev_idx;
         if (!grid_barrier(&ctl->bar, &ctl->err, epoch)) return;
 
         bool prev_bu = false;
-        for (int j = 1;; ++j) {
+        int j = 1;
+        for (;; ++j) {
             Lvl L;
             const int sc = (j - 1) & 3, sp = (j - 2) & 3;
             const u64 pk = ld_volatile_u64(&ctl->qpack[sc]);
@@ -711,15 +886,21 @@ __global__ void __launch_bounds__(MS_THREADS) ms_grid_kernel(MsArgs a)
             L.fcur = a.fr[L.cur];
             L.fnxt = a.fr[L.nxt];
             L.fprv = a.fr[L.prv];
+            L.sact = s_act;
             L.lev = j - 1;
             L.tag = j + 1;
-            L.row0 = row0;
             if (rank == 0) {
                 const int z = (j + 1) & 3;
                 ctl->qpack[z] = 0;
                 ctl->work[z] = 0;
 #pragma unroll
                 for (int q = 0; q < MAXW; ++q) ctl->active[z][q] = 0;
+            }
+            // plane b is first written in phase 2^b + 1; clear it one phase earlier
+            if ((j & (j - 1)) == 0) {
+                const int pb = __ffs(j) - 1;
+                if (pb >= EAGER_PLANES && pb < a.nplanes)
+                    for (long long w = rank; w < a.n; w += size) zerow<W>(a.plane + pb * pstride + (size_t)w * W);
             }
             bool bu = false;
             if (VARIANT == GU_BFS_BOTTOM_UP) {
@@ -728,29 +909,43 @@ __global__ void __launch_bounds__(MS_THREADS) ms_grid_kernel(MsArgs a)
                 if (!prev_bu) bu = j > 1 && (double)L.qedges * (double)a.alpha > (double)a.m;
                 else bu = (double)L.qlen * (double)a.beta > (double)a.n;
             }
-            u64 disc[W] = {};
             if (bu) {
-                bu_sweep<W, GridG>(a, L, disc);
-                if (a.nheavy) bu_heavy<W, GridG>(a, L, disc);
+                bu_sweep<W, GridG>(a, L);
+                if (a.nmid) bu_mid<W, GridG>(a, L);
+                if (a.nheavy) bu_heavy<W, GridG>(a, L);
             } else {
                 td_update<W, GridG>(a, L);
-                if (VARIANT == GU_BFS_EDGE) gather_edge<W, GridG>(a, L, disc);
-                else if (VARIANT == GU_BFS_WARP) gather_warp<W, GridG>(a, L, disc);
-                else if (VARIANT == GU_BFS_CTA_WARP) gather_cta_warp<W, GridG>(a, L, disc);
-                else if (VARIANT == GU_BFS_SCAN) gather_scan<W, GridG>(a, L, disc);
-                else if (VARIANT == GU_BFS_SHUFFLE) gather_shuffle<W, GridG>(a, L, disc);
-                else if (VARIANT == GU_BFS_LINEAR) gather_linear<W, GridG>(a, L, disc);
-                else gather_lbs<W, GridG>(a, L, disc);  // AUTO, BOTTOM_UP level 1
+                if (VARIANT == GU_BFS_EDGE) gather_edge<W, GridG>(a, L);
+                else if (VARIANT == GU_BFS_WARP) gather_warp<W, GridG>(a, L);
+                else if (VARIANT == GU_BFS_CTA_WARP) gather_cta_warp<W, GridG>(a, L);
+                else if (VARIANT == GU_BFS_SCAN) gather_scan<W, GridG>(a, L);
+                else if (VARIANT == GU_BFS_SHUFFLE) gather_shuffle<W, GridG>(a, L);
+                else if (VARIANT == GU_BFS_LINEAR) gather_linear<W, GridG>(a, L);
+                else gather_mp<W, GridG>(a, L);  // AUTO, BOTTOM_UP level 1
             }
-            flush_active<W>(a, L.slot, disc);
+            __syncthreads();
+            if (threadIdx.x < W) {
+                const u64 r = s_act[threadIdx.x];
+                if (r) atomicOr(&ctl->active[L.slot][threadIdx.x], r);
+                s_act[threadIdx.x] = 0;
+            }
             if (rank == 0) {
                 if (bu) ctl->bu_levels++;
                 else ctl->td_levels++;
                 if (j - 1 > ctl->max_level) ctl->max_level = j - 1;
             }
+            if (threadIdx.x == 0) record_event(ctl, ev_idx, rank == 0, b, j, bu ? 1 : 0, L.qlen, L.qedges);
+            ++ev_idx;
             prev_bu = bu;
             if (!grid_barrier(&ctl->bar, &ctl->err, epoch)) return;
         }
+        // F_{j-1} is empty: levels of this batch are 0..j-2
+        int used = 0;
+        while (used < 31 && ((j - 2) >> used) != 0) ++used;
+        write_distances<W, GridG>(a, row0, nb, used);
+        if (threadIdx.x == 0) record_event(ctl, ev_idx, rank == 0, b, j, 2, 0, 0);  // distance rows written
+        ++ev_idx;
+        if (!grid_barrier(&ctl->bar, &ctl->err, epoch)) return;
     }
 }
 
@@ -803,11 +998,15 @@ void launch_msbfs(DeviceGraph &g, const int32_t *sources, int32_t k, int32_t *di
     if (opt.variant == GU_BFS_EDGE) ensure_coo(g, stream);
     const int W = msbfs_words_for(k);
     const size_t n = (size_t)g.n;
+    // every BFS level is at most n - 1: bit-length of n - 1 planes suffice
+    int nplanes = 1;
+    while (nplanes < MAX_PLANES && ((int64_t)(n > 0 ? n - 1 : 0) >> nplanes) != 0) ++nplanes;
     auto up = [](size_t b) { return ((b + 255) / 256) * 256; };
     const size_t words_bytes = up(n * W * sizeof(u64));
     const size_t i32_bytes = up(n * sizeof(int32_t));
-    const size_t ctl_bytes = 256;
-    char *ws = (char *)g.ws.get(ctl_bytes + 4 * words_bytes + 7 * i32_bytes);
+    static_assert(CTL_REGION <= WS_CONTROL_BYTES, "timeline must fit the control region");
+    const size_t ctl_bytes = WS_CONTROL_BYTES;
+    char *ws = (char *)g.ws.get(ctl_bytes + (4 + (size_t)nplanes) * words_bytes + 7 * i32_bytes);
     MsArgs a;
     a.R = g.R;
     a.C = g.C;
@@ -817,6 +1016,8 @@ void launch_msbfs(DeviceGraph &g, const int32_t *sources, int32_t k, int32_t *di
     a.heavy = g.heavy;
     a.n = g.n;
     a.nheavy = g.nheavy;
+    a.mid = g.mid;
+    a.nmid = g.nmid;
     a.m = g.m;
     a.sources = sources;
     a.k = k;
@@ -831,6 +1032,9 @@ void launch_msbfs(DeviceGraph &g, const int32_t *sources, int32_t k, int32_t *di
         a.fr[i] = reinterpret_cast<u64 *>(p);
         p += words_bytes;
     }
+    a.plane = reinterpret_cast<u64 *>(p);
+    a.nplanes = nplanes;
+    p += (size_t)nplanes * words_bytes;
     a.stamp = reinterpret_cast<int32_t *>(p);
     p += i32_bytes;
     for (int i = 0; i < 3; ++i) {
@@ -844,7 +1048,7 @@ void launch_msbfs(DeviceGraph &g, const int32_t *sources, int32_t k, int32_t *di
     int degbits = 1;
     while (degbits < 31 && (1ll << degbits) <= (long long)g.max_degree) ++degbits;
     a.degbits = degbits;
-    GU_CUDA_CHECK(cudaMemsetAsync(a.ctl, 0, sizeof(MsCtl), stream));
+    GU_CUDA_CHECK(cudaMemsetAsync(a.ctl, 0, CTL_REGION, stream));
     const int sms = g.sm_count;
     g.mark_start(stream);
     switch (opt.variant) {
@@ -870,6 +1074,26 @@ void msbfs_read_status(DeviceGraph &g, int *dev_err, int *td_levels, int *bu_lev
     if (td_levels) *td_levels = c.td_levels;
     if (bu_levels) *bu_levels = c.bu_levels;
     if (max_level) *max_level = c.max_level;
+}
+
+// Copies the per-phase timeline of the last batched launch (after a stream sync).
+int msbfs_read_timeline(DeviceGraph &g, int max_entries, int32_t *batch, int32_t *level, int32_t *kind,
+                        int64_t *frontier_vertices, int64_t *frontier_edges, double *t_ms)
+{
+    std::vector<char> buf(CTL_REGION);
+    GU_CUDA_CHECK(cudaMemcpy(buf.data(), g.ws.ptr, CTL_REGION, cudaMemcpyDeviceToHost));
+    const MsEvent *ev = reinterpret_cast<const MsEvent *>(buf.data() + 256);
+    const int cnt = *reinterpret_cast<const int *>(ev + TIMELINE_MAX);
+    const int nout = cnt < max_entries ? cnt : max_entries;
+    for (int i = 0; i < nout; ++i) {
+        if (batch) batch[i] = ev[i].batch;
+        if (level) level[i] = ev[i].level;
+        if (kind) kind[i] = ev[i].bottom_up;
+        if (frontier_vertices) frontier_vertices[i] = ev[i].qlen;
+        if (frontier_edges) frontier_edges[i] = ev[i].qedges;
+        if (t_ms) t_ms[i] = (double)(ev[i].t_last_ns - ev[0].t_last_ns) * 1e-6;
+    }
+    return nout;
 }
 
 }  // namespace gu

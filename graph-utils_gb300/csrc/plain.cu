@@ -87,10 +87,11 @@ void launch_plain_bfs(DeviceGraph &g, const int32_t *sources, int32_t k, int32_t
     int grid = g.sm_count * blocks_per_sm;
     if (grid > k) grid = k;
     if (grid < 1) grid = 1;
-    const size_t need = (size_t)grid * 2 * (size_t)g.n * sizeof(int32_t) + 256;
+    const size_t need = (size_t)grid * 2 * (size_t)g.n * sizeof(int32_t) + WS_CONTROL_BYTES;
     char *ws = (char *)g.ws.get(need);
-    int32_t *qbuf = reinterpret_cast<int32_t *>(ws + 256);
-    GU_CUDA_CHECK(cudaMemsetAsync(ws, 0, 256, stream));  // no level statistics for this form
+    int32_t *qbuf = reinterpret_cast<int32_t *>(ws + WS_CONTROL_BYTES);
+    // no level statistics or timeline for this form
+    GU_CUDA_CHECK(cudaMemsetAsync(ws, 0, WS_CONTROL_BYTES, stream));
     g.mark_start(stream);
     plain_bfs_kernel<<<grid, PLAIN_THREADS, 0, stream>>>(g.R, g.C, g.n, sources, k, dist, ld, qbuf);
     GU_CUDA_CHECK(cudaGetLastError());

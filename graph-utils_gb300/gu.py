@@ -74,6 +74,8 @@ def lib():
                              ctypes.POINTER(_vp)], ctypes.c_int),
         "gu_graph_last_launch": ([_vp, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int),
                                   ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
+        "gu_graph_level_profile": ([_vp, ctypes.c_int, _i32p, _i32p, _i32p, _i64p, _i64p,
+                                    ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
         "gu_bfs": ([_vp, ctypes.c_int, _vp, ctypes.c_int32, _vp, ctypes.c_int64, _vp], ctypes.c_int),
         "gu_bfs_host": ([_vp, ctypes.c_int, _i32p, ctypes.c_int32, _i32p, ctypes.c_int64, _vp], ctypes.c_int),
     }
@@ -200,6 +202,20 @@ class Graph:
         check(lib().gu_graph_last_launch(self._h, ctypes.byref(t), ctypes.byref(td), ctypes.byref(bu),
                                          ctypes.byref(ml)))
         return t.value, td.value, bu.value, ml.value
+
+    def level_profile(self, max_entries=1024):
+        """Per-phase timeline of the last batched search: list of dicts."""
+        b, lv, kd = (np.zeros(max_entries, np.int32) for _ in range(3))
+        fv, fe = np.zeros(max_entries, np.int64), np.zeros(max_entries, np.int64)
+        t = np.zeros(max_entries, np.float64)
+        cnt = ctypes.c_int()
+        check(lib().gu_graph_level_profile(self._h, max_entries, _ptr(b), _ptr(lv), _ptr(kd),
+                                           fv.ctypes.data_as(_i64p), fe.ctypes.data_as(_i64p),
+                                           t.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), ctypes.byref(cnt)))
+        kinds = {0: "top-down", 1: "bottom-up", 2: "rows", 4: "init"}
+        return [dict(batch=int(b[i]), level=int(lv[i]), kind=kinds.get(int(kd[i]), "?"),
+                     frontier_vertices=int(fv[i]), frontier_edges=int(fe[i]), t_ms=float(t[i]))
+                for i in range(cnt.value)]
 
     def bfs(self, sources_dev, dist_dev, variant="auto", ld=None, stream=None):
         """Device form: sources_dev (int32 cuda tensor, k), dist_dev (int32 cuda tensor, k x ld)."""

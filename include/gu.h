@@ -123,6 +123,14 @@ gu_status gu_graph_arrays(gu_graph g, const int32_t **R_dev, const int32_t **C_d
  * (e.g. shuffle_based.cu:42-44). */
 gu_status gu_graph_last_launch(gu_graph g, double *kernel_seconds, int *td_levels, int *bu_levels, int *max_level);
 
+/* Profiling hook: the per-phase timeline of the last batched search on g (up to
+ * max_entries phases).  Entry i: batch, level j of the phase, kind (0 top-down,
+ * 1 bottom-up, 2 distance write-out, 3 end), vertices and out-edges of the
+ * frontier it expanded, and its start time in ms from the first phase.  No
+ * reference counterpart (the reference times whole calls only). */
+gu_status gu_graph_level_profile(gu_graph g, int max_entries, int32_t *batch, int32_t *level, int32_t *kind,
+                                 int64_t *frontier_vertices, int64_t *frontier_edges, double *t_ms, int *count);
+
 /* ---- multi-source BFS ------------------------------------------------------ */
 /* Row i of dist (row stride ld >= n elements) receives the distances from
  * sources[i]; GU_DIST_UNREACHABLE where unreachable.  Replaces
