@@ -1096,4 +1096,174 @@ int msbfs_read_timeline(DeviceGraph &g, int max_entries, int32_t *batch, int32_t
     return nout;
 }
 
+// ---- allocation-free multi-source BFS (gu_bfs_noalloc) -------------------------------
+// Some callers may not allocate device memory at the time they search: code that
+// runs inside a host process whose allocator owns and accounts for every byte of
+// the GPU (a database, an inference server, a framework's caching pool), services
+// that fix their memory budget at start-up, and paths that must not pay for the
+// implicit device synchronisation of cudaMalloc/cudaFree.  For them the batched
+// engine can run with its scratch in the fixed-size array below instead of a
+// graph handle's workspace: top-down levels only (so neither an in-edge CSR nor the
+// degree-class lists are needed), one 64-bit word per vertex, the caller's own
+// device CSR, sources and distance rows.
+
+constexpr int32_t NOALLOC_MAX_VERTICES = 32768;
+constexpr size_t NOALLOC_SCRATCH_BYTES = (size_t)6 << 20;  // 6 MiB per device
+constexpr size_t NOALLOC_FLAG_OFFSET = WS_CONTROL_BYTES - 64;
+
+// Reserved on every device when the library's device code is loaded there and
+// held until the process exits; all gu_bfs_noalloc calls on a device share it.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_SCRATCH_BYTES];
+
+static size_t noalloc_layout_bytes(int32_t n, int *nplanes_out)
+{
+    auto up = [](size_t b) { return ((b + 255) / 256) * 256; };
+    int nplanes = 1;
+    while (nplanes < MAX_PLANES && ((int64_t)(n > 0 ? n - 1 : 0) >> nplanes) != 0) ++nplanes;
+    if (nplanes_out) *nplanes_out = nplanes;
+    return WS_CONTROL_BYTES + (4 + (size_t)nplanes) * up((size_t)n * sizeof(u64)) + 7 * up((size_t)n * sizeof(int32_t));
+}
+
+// Flags malformed inputs instead of letting the search index out of bounds:
+// 1 = R not a valid offset array, 2 = column index out of range, 4 = source out of range.
+__global__ void noalloc_validate_kernel(const int32_t *R, const int32_t *C, int32_t n, int64_t m,
+                                        const int32_t *sources, int32_t k, int *flag)
+{
+    const long long rank = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long size = (long long)gridDim.x * blockDim.x;
+    if (rank == 0 && (R[0] != 0 || (int64_t)R[n] != m)) atomicOr(flag, 1);
+    for (long long v = rank; v < n; v += size)
+        if (R[v + 1] < R[v]) atomicOr(flag, 1);
+    for (long long e = rank; e < m; e += size) {
+        const int32_t c = C[e];
+        if (c < 0 || c >= n) atomicOr(flag, 2);
+    }
+    for (long long i = rank; i < k; i += size) {
+        const int32_t s = sources[i];
+        if (s < 0 || s >= n) atomicOr(flag, 4);
+    }
+}
+
+// Device address of the scratch array for the current device.  The host-side
+// name g_noalloc_scratch is only a stand-in: the address is looked up once per
+// device (with that device current) and cached.
+static char *noalloc_scratch_for_current_device()
+{
+    static std::mutex mu;
+    static void *addr[128] = {};
+    int dev = 0;
+    GU_CUDA_CHECK(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 128) throw gu_error(GU_ERR_UNSUPPORTED, "device ordinal out of range");
+    std::lock_guard<std::mutex> lk(mu);
+    if (!addr[dev]) {
+        void *p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p)
+            throw gu_error(GU_ERR_CUDA, std::string("cudaGetSymbolAddress(g_noalloc_scratch): ") + cudaGetErrorString(e));
+        addr[dev] = p;
+    }
+    return static_cast<char *>(addr[dev]);
+}
+
+static void bfs_noalloc(const int32_t *R, const int32_t *C, int32_t n, int64_t m, const int32_t *sources, int32_t k,
+                        int32_t *dist, int64_t ld, cudaStream_t st)
+{
+    if (n < 0 || m < 0 || m > INT32_MAX || k < 0) throw gu_error(GU_ERR_INVALID_ARGUMENT, "negative size or m > INT32_MAX");
+    if (n > NOALLOC_MAX_VERTICES)
+        throw gu_error(GU_ERR_CAPACITY, "gu_bfs_noalloc handles at most " + std::to_string(NOALLOC_MAX_VERTICES) +
+                                            " vertices (its static scratch is 6 MiB per device); got n = " +
+                                            std::to_string(n));
+    if (ld < n) throw gu_error(GU_ERR_INVALID_ARGUMENT, "ld must be >= n");
+    if (k == 0) return;
+    if (n == 0) throw gu_error(GU_ERR_INVALID_ARGUMENT, "source vertex out of range (graph has no vertices)");
+    if (!R || (m > 0 && !C) || !sources || !dist) throw gu_error(GU_ERR_INVALID_ARGUMENT, "null device buffer");
+    int nplanes = 1;
+    if (noalloc_layout_bytes(n, &nplanes) > NOALLOC_SCRATCH_BYTES)
+        throw gu_error(GU_ERR_INTERNAL, "static scratch smaller than its layout");
+    char *scratch = noalloc_scratch_for_current_device();
+    int dev = 0;
+    GU_CUDA_CHECK(cudaGetDevice(&dev));
+    const int sms = device_sm_count(dev);
+
+    int *flag = reinterpret_cast<int *>(scratch + NOALLOC_FLAG_OFFSET);
+    GU_CUDA_CHECK(cudaMemsetAsync(flag, 0, sizeof(int), st));
+    noalloc_validate_kernel<<<sms * 4, 256, 0, st>>>(R, C, n, m, sources, k, flag);
+    GU_CUDA_CHECK(cudaGetLastError());
+    int hflag = 0;
+    GU_CUDA_CHECK(cudaMemcpyAsync(&hflag, flag, sizeof(int), cudaMemcpyDeviceToHost, st));
+    GU_CUDA_CHECK(cudaStreamSynchronize(st));
+    if (hflag & 1) throw gu_error(GU_ERR_INVALID_ARGUMENT, "R must start at 0, be non-decreasing and end at m");
+    if (hflag & 2) throw gu_error(GU_ERR_INVALID_ARGUMENT, "column index out of range");
+    if (hflag & 4) throw gu_error(GU_ERR_INVALID_ARGUMENT, "source vertex out of range");
+
+    auto up = [](size_t b) { return ((b + 255) / 256) * 256; };
+    const size_t words_bytes = up((size_t)n * sizeof(u64));
+    const size_t i32_bytes = up((size_t)n * sizeof(int32_t));
+    MsArgs a;
+    a.R = R;
+    a.C = C;
+    a.RT = R;  // never read: top-down levels only
+    a.CT = C;
+    a.F = nullptr;
+    a.heavy = nullptr;
+    a.mid = nullptr;
+    a.n = n;
+    a.nheavy = 0;
+    a.nmid = 0;
+    a.m = m;
+    a.sources = sources;
+    a.k = k;
+    a.dist = dist;
+    a.ld = ld;
+    char *p = scratch;
+    a.ctl = reinterpret_cast<MsCtl *>(p);
+    p += WS_CONTROL_BYTES;
+    a.seen = reinterpret_cast<u64 *>(p);
+    p += words_bytes;
+    for (int i = 0; i < 3; ++i) {
+        a.fr[i] = reinterpret_cast<u64 *>(p);
+        p += words_bytes;
+    }
+    a.plane = reinterpret_cast<u64 *>(p);
+    a.nplanes = nplanes;
+    p += (size_t)nplanes * words_bytes;
+    a.stamp = reinterpret_cast<int32_t *>(p);
+    p += i32_bytes;
+    for (int i = 0; i < 3; ++i) {
+        a.q[i] = reinterpret_cast<int32_t *>(p);
+        p += i32_bytes;
+        a.qoff[i] = reinterpret_cast<int32_t *>(p);
+        p += i32_bytes;
+    }
+    a.alpha = 0.f;  // never switch to bottom-up
+    a.beta = 24.f;
+    int degbits = 1;
+    while (degbits < 31 && (1ll << degbits) <= (long long)m) ++degbits;
+    a.degbits = degbits;
+    // the previous call's contents stay in the array: clear the control block
+    GU_CUDA_CHECK(cudaMemsetAsync(a.ctl, 0, CTL_REGION, st));
+    launch_one<GU_BFS_AUTO, 1>(a, sms, st);
+    int err = 0;
+    GU_CUDA_CHECK(cudaMemcpyAsync(&err, &a.ctl->err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    GU_CUDA_CHECK(cudaStreamSynchronize(st));
+    if (err == DEV_ERR_BARRIER_TIMEOUT) throw gu_error(GU_ERR_TIMEOUT, "a device-side wait exceeded its limit");
+    if (err != 0) throw gu_error(GU_ERR_INTERNAL, "device reported error code " + std::to_string(err));
+}
+
 }  // namespace gu
+
+extern "C" gu_status gu_bfs_noalloc(const int32_t *R_dev, const int32_t *C_dev, int32_t n, int64_t m,
+                                    const int32_t *sources_dev, int32_t k, int32_t *dist_dev, int64_t ld,
+                                    void *stream)
+{
+    try {
+        gu::bfs_noalloc(R_dev, C_dev, n, m, sources_dev, k, dist_dev, ld, (cudaStream_t)stream);
+        return GU_OK;
+    } catch (const gu::gu_error &e) {
+        gu::set_last_error(e.what());
+        return e.code;
+    } catch (const std::exception &e) {
+        gu::set_last_error(e.what());
+        return GU_ERR_INTERNAL;
+    }
+}

@@ -78,6 +78,8 @@ def lib():
                                     ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
         "gu_bfs": ([_vp, ctypes.c_int, _vp, ctypes.c_int32, _vp, ctypes.c_int64, _vp], ctypes.c_int),
         "gu_bfs_host": ([_vp, ctypes.c_int, _i32p, ctypes.c_int32, _i32p, ctypes.c_int64, _vp], ctypes.c_int),
+        "gu_bfs_noalloc": ([_vp, _vp, ctypes.c_int32, ctypes.c_int64, _vp, ctypes.c_int32, _vp, ctypes.c_int64, _vp],
+                           ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)

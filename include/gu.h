@@ -144,6 +144,30 @@ gu_status gu_bfs(gu_graph g, int variant, const int32_t *sources_dev, int32_t k,
 gu_status gu_bfs_host(gu_graph g, int variant, const int32_t *sources_host, int32_t k, int32_t *dist_host,
                       int64_t ld, void *stream);
 
+/* Multi-source BFS that allocates no device memory.  No counterpart in the
+ * reference: it exists for callers that may not call cudaMalloc while they
+ * search -- code living in a process whose allocator owns every byte of the GPU
+ * (a database or inference server, a framework's caching pool), services whose
+ * memory budget is fixed at start-up, and paths that cannot afford the implicit
+ * device synchronisation of cudaMalloc/cudaFree.
+ *
+ * The caller passes its own device CSR (R_dev: n+1 offsets, C_dev: m neighbours,
+ * directed or undirected), device sources and device rows, as for gu_bfs; the
+ * rows are identical to gu_bfs's.  Scratch is a fixed 6 MiB array compiled into
+ * the library, which every device that loads the library holds until the process
+ * exits; it limits n to 32768 vertices (larger graphs: GU_ERR_CAPACITY, nothing
+ * launched).  The search runs top-down levels only.  Malformed CSR arrays and
+ * out-of-range sources are rejected with GU_ERR_INVALID_ARGUMENT before the
+ * search.  The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress, with that device current); make that first call before
+ * any stream capture.  All calls on a device share the one array and it keeps
+ * the previous call's contents (each call clears what must start at zero):
+ * calls whose work overlaps on the GPU -- on different streams or from several
+ * host threads -- race and must be serialised by the caller.  Synchronises
+ * `stream` before returning. */
+gu_status gu_bfs_noalloc(const int32_t *R_dev, const int32_t *C_dev, int32_t n, int64_t m,
+                         const int32_t *sources_dev, int32_t k, int32_t *dist_dev, int64_t ld, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
