@@ -1,0 +1,548 @@
+// bc.cu -- batched shortest-path counting (sigma) and Brandes betweenness
+// centrality on sm_103a.
+//
+// Restates, for a batch of B = 64*W sources per pass, the reference's designed
+// (commented-out) GPU kernels: the forward sweep counting shortest paths
+// (multi_search/shuffle_based.cu:113-151, 164-214) and the backward dependency
+// accumulation delta_s(w) = sum over successors v of sigma_s(w)/sigma_s(v) *
+// (1 + delta_s(v)) (shuffle_based.cu:217-354), then bc[v] += delta_s(v)
+// (shuffle_based.cu:350-353).  By design: sigma is uint64 and bit-exact (integer
+// sums do not depend on order), delta and bc are FP64, and every floating-point
+// sum runs in a fixed order -- CSR neighbour order inside a work item, work
+// items of a vertex in order, a fixed-shape warp tree over the batch's sources,
+// batches in order -- so results do not depend on scheduling.  No float atomics.
+//
+// Layout (workspace, per graph handle):
+//   seen[n][W]          sources known at a vertex (lags one level, see below)
+//   lvl[L+1][n][W]      lvl[j] = bitmap of the sources whose BFS level of v is j
+//   sigma[n][B] uint64  shortest-path counts, sources of the batch contiguous
+//   delta[n][B] double  dependencies
+//   part[slots][W][64]  backward partial sums of vertices split into several items
+//   bc[n] double        accumulated over batches (output)
+// Work items (graph-static, ChunkMap): one per <= 256 edges of a vertex's in-
+// (forward) or out-adjacency (backward), times the W source words; a warp per
+// item, lane l owning sources 64q+l and 64q+32+l of word q.  One grid barrier
+// per level (two for backward levels with split vertices).
+#include "device_utils.cuh"
+#include "gu_internal.h"
+
+#include <climits>
+#include <cstdlib>
+#include <memory>
+
+namespace gu {
+
+constexpr int BC_THREADS = 512;
+
+struct __align__(128) BcCtl {
+    unsigned bar;
+    int err;
+    int max_level;  // deepest forward level over all batches
+    int pad0;
+    int found[2];   // forward: any new bit at level j (by parity)
+    int pad1[2];
+    u64 active[2][16];  // sources with a non-empty level, by parity
+};
+static_assert(sizeof(BcCtl) <= 512, "control block");
+
+enum : int { DEV_ERR_LEVELS = 3 };
+
+struct DevChunks {
+    const int32_t *v, *e0, *e1, *slot;
+    int32_t nchunks;
+    const int32_t *mv, *mfirst, *mcount;
+    int32_t nmulti;
+};
+
+struct BcArgs {
+    const int32_t *__restrict__ R;
+    const int32_t *__restrict__ C;
+    const int32_t *__restrict__ RT;
+    const int32_t *__restrict__ CT;
+    DevChunks cin, cout;
+    int32_t n;
+    int32_t W;        // words per batch (1..16)
+    int32_t max_lvl;  // capacity of lvl[] minus one
+    const int32_t *sources;
+    int32_t k;
+    u64 *seen;
+    u64 *lvl;
+    u64 *sigma;
+    double *delta;
+    double *beta;  // (1 + delta) / sigma
+    double *part;
+    double *bc;           // n, accumulated
+    int32_t *dist_rows;   // optional k x ld
+    u64 *sigma_rows;      // optional k x ld
+    double *delta_rows;   // optional k x ld
+    int64_t ld;
+    BcCtl *ctl;
+};
+
+// Takes the next (up to) four set lanes of a ballot in ascending lane order; a
+// missing one is reported as -1.
+__device__ __forceinline__ void next4(unsigned &bal, int (&src)[4])
+{
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+        src[t] = bal ? __ffs(bal) - 1 : -1;
+        if (bal) bal &= bal - 1;
+    }
+}
+
+__device__ __forceinline__ long long gwarp() { return ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; }
+__device__ __forceinline__ long long nwarps() { return ((long long)gridDim.x * blockDim.x) >> 5; }
+
+// Forward level j, word q, one work item (a range of w's in-edges): new bits =
+// sources of an in-neighbour's level j-1 not known at w (levels <= j-1);
+// sigma(w) += sum of the in-neighbours' sigma, each lane for its two sources.
+// seen lags one level: known = seen | lvl[j-1] is invariant while the first
+// item of w folds lvl[j-1] into seen.
+__device__ void bc_forward_item(const BcArgs &a, int j, int q, int c, u64 act, u64 &found_any)
+{
+    const int lane = lane_id();
+    const int B = 64 * a.W;
+    const size_t nW = (size_t)a.n * a.W;
+    const int32_t w = __ldg(a.cin.v + c);
+    const size_t wo = (size_t)w * a.W + q;
+    const u64 prevw = __ldcg(a.lvl + (size_t)(j - 1) * nW + wo);
+    const u64 known = __ldcg(a.seen + wo) | prevw;
+    const int32_t e0 = __ldg(a.cin.e0 + c), e1 = __ldg(a.cin.e1 + c);
+    const bool first_item = e0 == __ldg(a.RT + w);
+    if (first_item && lane == 0 && prevw) a.seen[wo] = known;
+    if ((act & ~known) == 0) return;
+    const u64 *prev = a.lvl + (size_t)(j - 1) * nW;
+    u64 nb = 0, acc0 = 0, acc1 = 0;
+    for (int32_t eb = e0; eb < e1; eb += 32) {
+        const int32_t e = eb + lane;
+        int32_t v = -1;
+        u64 m = 0;
+        if (e < e1) {
+            v = __ldg(a.CT + e);
+            m = __ldcg(prev + (size_t)v * a.W + q) & ~known;
+        }
+        unsigned bal = __ballot_sync(FULL_MASK, m != 0);
+        while (bal) {  // four in-neighbours per trip: eight loads in flight per lane
+            int src[4];
+            next4(bal, src);
+            u64 x0[4], x1[4];
+#pragma unroll
+            for (int t = 0; t < 4; ++t) {
+                const int sl = src[t] < 0 ? src[0] : src[t];
+                const int32_t vv = __shfl_sync(FULL_MASK, v, sl);
+                const u64 mm = src[t] < 0 ? 0ull : __shfl_sync(FULL_MASK, m, sl);
+                nb |= mm;
+                const u64 *sv = a.sigma + (size_t)vv * B + 64 * q;
+                x0[t] = ((mm >> lane) & 1ull) ? __ldcg(sv + lane) : 0ull;
+                x1[t] = ((mm >> (lane + 32)) & 1ull) ? __ldcg(sv + lane + 32) : 0ull;
+            }
+            acc0 += (x0[0] + x0[1]) + (x0[2] + x0[3]);
+            acc1 += (x1[0] + x1[1]) + (x1[2] + x1[3]);
+        }
+    }
+    if (!nb) return;
+    const bool split = __ldg(a.cin.slot + c) >= 0;
+    u64 *sw = a.sigma + (size_t)w * B + 64 * q;
+    u64 *lw = a.lvl + (size_t)j * nW + wo;
+    if (split) {  // sigma rows of split vertices were zeroed for the batch
+        if ((nb >> lane) & 1ull) atomicAdd(sw + lane, acc0);
+        if ((nb >> (lane + 32)) & 1ull) atomicAdd(sw + lane + 32, acc1);
+        if (lane == 0) atomicOr(lw, nb);
+    } else {
+        if ((nb >> lane) & 1ull) sw[lane] = acc0;
+        if ((nb >> (lane + 32)) & 1ull) sw[lane + 32] = acc1;
+        if (lane == 0) *lw = nb;
+    }
+    found_any |= nb;
+}
+
+// Backward dependencies are carried as beta_s(v) = (1 + delta_s(v)) / sigma_s(v):
+// delta_s(w) = sigma_s(w) * sum over successors v of beta_s(v), so a successor
+// costs one FP64 add and each (vertex, source) pair one division (FP64 is the
+// scarce unit on this part).  finish_delta turns the successor sum S of the
+// sources owned by a lane into delta and beta.
+__device__ __forceinline__ void finish_delta(const BcArgs &a, size_t o, double S)
+{
+    const double sg = (double)__ldcg(a.sigma + o);
+    const double d = sg * S;
+    a.delta[o] = d;
+    a.beta[o] = (1.0 + d) / sg;
+}
+
+// Backward level l, word q, one work item (a range of w's out-edges): for the
+// sources whose level of w is l, sum beta over successors v (level l+1) in CSR
+// order.  Unsplit vertices finish delta/beta directly; split ones store
+// per-item partial sums, added in item order by bc_combine_item after a barrier.
+__device__ void bc_backward_item(const BcArgs &a, int l, int L, int q, int c)
+{
+    const int lane = lane_id();
+    const int B = 64 * a.W;
+    const size_t nW = (size_t)a.n * a.W;
+    const int32_t w = __ldg(a.cout.v + c);
+    const u64 lm = __ldcg(a.lvl + (size_t)l * nW + (size_t)w * a.W + q);
+    if (lm == 0) return;
+    const bool own0 = (lm >> lane) & 1ull, own1 = (lm >> (lane + 32)) & 1ull;
+    double acc0 = 0.0, acc1 = 0.0;
+    if (l < L) {
+        const u64 *next = a.lvl + (size_t)(l + 1) * nW;
+        const int32_t e0 = __ldg(a.cout.e0 + c), e1 = __ldg(a.cout.e1 + c);
+        for (int32_t eb = e0; eb < e1; eb += 32) {
+            const int32_t e = eb + lane;
+            int32_t v = -1;
+            u64 m = 0;
+            if (e < e1) {
+                v = __ldg(a.C + e);
+                m = __ldcg(next + (size_t)v * a.W + q) & lm;
+            }
+            unsigned bal = __ballot_sync(FULL_MASK, m != 0);
+            while (bal) {  // four successors per trip, added in CSR order
+                int src[4];
+                next4(bal, src);
+                double b0[4], b1[4];
+                bool h0[4], h1[4];
+#pragma unroll
+                for (int t = 0; t < 4; ++t) {
+                    const int sl = src[t] < 0 ? src[0] : src[t];
+                    const int32_t vv = __shfl_sync(FULL_MASK, v, sl);
+                    const u64 mm = src[t] < 0 ? 0ull : __shfl_sync(FULL_MASK, m, sl);
+                    const double *bv = a.beta + (size_t)vv * B + 64 * q;
+                    h0[t] = (mm >> lane) & 1ull;
+                    h1[t] = (mm >> (lane + 32)) & 1ull;
+                    b0[t] = h0[t] ? __ldcg(bv + lane) : 0.0;
+                    b1[t] = h1[t] ? __ldcg(bv + lane + 32) : 0.0;
+                }
+#pragma unroll
+                for (int t = 0; t < 4; ++t) {
+                    if (h0[t]) acc0 += b0[t];
+                    if (h1[t]) acc1 += b1[t];
+                }
+            }
+        }
+    }
+    const int32_t slot = __ldg(a.cout.slot + c);
+    if (slot >= 0) {
+        double *p = a.part + ((size_t)slot * a.W + q) * 64;
+        p[lane] = own0 ? acc0 : 0.0;
+        p[lane + 32] = own1 ? acc1 : 0.0;
+    } else {
+        const size_t o = (size_t)w * B + 64 * q;
+        if (own0) finish_delta(a, o + lane, acc0);
+        if (own1) finish_delta(a, o + lane + 32, acc1);
+    }
+}
+
+// delta of a split vertex = its items' partials added in item order.
+__device__ void bc_combine_item(const BcArgs &a, int l, int q, int i)
+{
+    const int lane = lane_id();
+    const int B = 64 * a.W;
+    const size_t nW = (size_t)a.n * a.W;
+    const int32_t w = __ldg(a.cout.mv + i);
+    const u64 lm = __ldcg(a.lvl + (size_t)l * nW + (size_t)w * a.W + q);
+    if (lm == 0) return;
+    const int32_t c0 = __ldg(a.cout.mfirst + i), nc = __ldg(a.cout.mcount + i);
+    double s0 = 0.0, s1 = 0.0;
+    for (int32_t c = c0; c < c0 + nc; ++c) {
+        const double *p = a.part + ((size_t)__ldg(a.cout.slot + c) * a.W + q) * 64;
+        s0 += __ldcg(p + lane);
+        s1 += __ldcg(p + lane + 32);
+    }
+    const size_t o = (size_t)w * B + 64 * q;
+    if ((lm >> lane) & 1ull) finish_delta(a, o + lane, s0);
+    if ((lm >> (lane + 32)) & 1ull) finish_delta(a, o + lane + 32, s1);
+}
+
+// bc[w] += sum of delta over the batch's sources whose level of w is >= 1, as a
+// fixed-shape tree: each lane sums its own sources word by word, then a
+// butterfly over the 32 lanes.
+__device__ void bc_accumulate_item(const BcArgs &a, int32_t w, int nb)
+{
+    const int lane = lane_id();
+    const int B = 64 * a.W;
+    double s = 0.0;
+    for (int q = 0; q < a.W && 64 * q < nb; ++q) {
+        const u64 counted = __ldcg(a.seen + (size_t)w * a.W + q) & ~__ldcg(a.lvl + (size_t)w * a.W + q);
+        const double *dw = a.delta + (size_t)w * B + 64 * q;
+        if ((counted >> lane) & 1ull) s += __ldcg(dw + lane);
+        if ((counted >> (lane + 32)) & 1ull) s += __ldcg(dw + lane + 32);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(FULL_MASK, s, o);
+    if (lane == 0) a.bc[w] += s;
+}
+
+// Optional per-source rows (dist, sigma, delta) of this batch: lane l writes
+// vertex w for sources 64q+l and 64q+l+32; levels from the level bitmaps.
+__device__ void bc_rows_item(const BcArgs &a, int32_t w, int q, int row0, int nb, int maxl)
+{
+    const int lane = lane_id();
+    const int B = 64 * a.W;
+    const size_t nW = (size_t)a.n * a.W;
+    const u64 seen = __ldcg(a.seen + (size_t)w * a.W + q);
+    const u64 lvl0 = __ldcg(a.lvl + (size_t)w * a.W + q);
+    for (int h = 0; h < 2; ++h) {
+        const int bit = lane + 32 * h;
+        if (64 * q + bit >= nb) continue;
+        const int row = row0 + 64 * q + bit;
+        const bool reached = (seen >> bit) & 1ull;
+        int32_t level = INT_MAX;
+        if (reached && a.dist_rows) {
+            for (int l = 0; l <= maxl; ++l)
+                if ((__ldcg(a.lvl + (size_t)l * nW + (size_t)w * a.W + q) >> bit) & 1ull) {
+                    level = l;
+                    break;
+                }
+        }
+        const size_t o = (size_t)w * B + 64 * q + bit;
+        if (a.dist_rows) a.dist_rows[(int64_t)row * a.ld + w] = level;
+        if (a.sigma_rows) a.sigma_rows[(int64_t)row * a.ld + w] = reached ? __ldcg(a.sigma + o) : 0ull;
+        if (a.delta_rows) {
+            const bool is_src = (lvl0 >> bit) & 1ull;
+            a.delta_rows[(int64_t)row * a.ld + w] = (reached && !is_src) ? __ldcg(a.delta + o) : 0.0;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(BC_THREADS, 2) bc_grid_kernel(BcArgs a, int do_backward)
+{
+    __shared__ u64 s_act[16];
+    unsigned epoch = 0;
+    BcCtl *ctl = a.ctl;
+    const long long rank = (long long)blockIdx.x * blockDim.x + threadIdx.x, size = (long long)gridDim.x * blockDim.x;
+    const int W = a.W, B = 64 * W;
+    const size_t nW = (size_t)a.n * W;
+    const int nbatch = (a.k + B - 1) / B;
+    for (long long i = rank; i < a.n; i += size) a.bc[i] = 0.0;
+    if (threadIdx.x < 16) s_act[threadIdx.x] = 0;
+    for (int b = 0; b < nbatch; ++b) {
+        const int row0 = b * B;
+        const int nb = min(B, a.k - row0);
+        for (size_t i = (size_t)rank; i < nW; i += (size_t)size) {
+            a.seen[i] = 0;
+            a.lvl[i] = 0;
+        }
+        // sigma rows of split vertices are accumulated with atomics: clear them
+        for (long long i = rank; i < (long long)a.cin.nmulti * B; i += size)
+            a.sigma[(size_t)__ldg(a.cin.mv + i / B) * B + (i % B)] = 0ull;
+        if (rank == 0) {
+            ctl->found[0] = ctl->found[1] = 0;
+            for (int q = 0; q < 16; ++q) ctl->active[0][q] = ctl->active[1][q] = 0;
+        }
+        if (!grid_barrier(&ctl->bar, &ctl->err, epoch)) return;
+        if (rank < nb) {
+            const int32_t s = __ldg(a.sources + row0 + rank);
+            const int q = (int)rank >> 6;
+            const u64 bit = 1ull << (rank & 63);
+            atomicOr(a.lvl + (size_t)s * W + q, bit);
+            a.sigma[(size_t)s * B + rank] = 1ull;
+            atomicOr(&ctl->active[0][q], bit);
+        }
+        if (!grid_barrier(&ctl->bar, &ctl->err, epoch)) return;
+        // forward levels
+        int L = 0;
+        for (int j = 1;; ++j) {
+            if (j > a.max_lvl) {
+                if (rank == 0) atomicCAS(&ctl->err, 0, (int)DEV_ERR_LEVELS);
+                grid_barrier(&ctl->bar, &ctl->err, epoch);
+                return;
+            }
+            for (size_t i = (size_t)rank; i < nW; i += (size_t)size) a.lvl[(size_t)j * nW + i] = 0;
+            if (rank == 0) {
+                ctl->found[j & 1] = 0;
+                for (int q = 0; q < 16; ++q) ctl->active[j & 1][q] = 0;
+            }
+            if (!grid_barrier(&ctl->bar, &ctl->err, epoch)) return;
+            for (int q = 0; q < W; ++q) {
+                const u64 act = ld_volatile_u64(&ctl->active[(j - 1) & 1][q]);
+                u64 found = 0;
+                for (long long c = gwarp(); c < a.cin.nchunks; c += nwarps())
+                    bc_forward_item(a, j, q, (int)c, act, found);
+                if (lane_id() == 0 && found) atomicOr(&s_act[q], found);
+            }
+            __syncthreads();
+            if (threadIdx.x < W && s_act[threadIdx.x]) {
+                atomicOr(&ctl->active[j & 1][threadIdx.x], s_act[threadIdx.x]);
+                atomicOr(&ctl->found[j & 1], 1);
+                s_act[threadIdx.x] = 0;
+            }
+            if (!grid_barrier(&ctl->bar, &ctl->err, epoch)) return;
+            if (ld_volatile_i32(&ctl->found[j & 1]) == 0) {
+                L = j - 1;  // this pass also folded lvl[L] into seen
+                break;
+            }
+        }
+        if (rank == 0 && L > ctl->max_level) ctl->max_level = L;
+        if (do_backward) {
+            for (int l = L; l >= 1; --l) {
+                for (int q = 0; q < W; ++q)
+                    for (long long c = gwarp(); c < a.cout.nchunks; c += nwarps()) bc_backward_item(a, l, L, q, (int)c);
+                if (!grid_barrier(&ctl->bar, &ctl->err, epoch)) return;
+                if (a.cout.nmulti) {
+                    for (int q = 0; q < W; ++q)
+                        for (long long i = gwarp(); i < a.cout.nmulti; i += nwarps()) bc_combine_item(a, l, q, (int)i);
+                    if (!grid_barrier(&ctl->bar, &ctl->err, epoch)) return;
+                }
+            }
+            for (long long w = gwarp(); w < a.n; w += nwarps()) bc_accumulate_item(a, (int32_t)w, nb);
+        }
+        if (a.dist_rows || a.sigma_rows || a.delta_rows) {
+            for (int q = 0; q < W; ++q)
+                for (long long w = gwarp(); w < a.n; w += nwarps()) bc_rows_item(a, (int32_t)w, q, row0, nb, L);
+        }
+        if (!grid_barrier(&ctl->bar, &ctl->err, epoch)) return;
+    }
+}
+
+// ---- host ----------------------------------------------------------------------------
+static void build_chunks(DeviceGraph &g, const std::vector<int32_t> &R, ChunkMap &cm)
+{
+    const int32_t n = g.n;
+    std::vector<int32_t> v, e0, e1, slot, mv, mfirst, mcount;
+    int32_t nslots = 0;
+    for (int32_t w = 0; w < n; ++w) {
+        const int32_t a = R[w], b = R[w + 1];
+        const int32_t nc = b > a ? (b - a + BC_CHUNK_EDGES - 1) / BC_CHUNK_EDGES : 1;
+        if (nc > 1) {
+            mv.push_back(w);
+            mfirst.push_back((int32_t)v.size());
+            mcount.push_back(nc);
+        }
+        for (int32_t c = 0; c < nc; ++c) {
+            v.push_back(w);
+            e0.push_back(a + c * BC_CHUNK_EDGES);
+            e1.push_back(std::min(b, a + (c + 1) * BC_CHUNK_EDGES));
+            slot.push_back(nc > 1 ? nslots++ : -1);
+        }
+    }
+    auto up = [&](const std::vector<int32_t> &src, int32_t *&dst) {
+        if (src.empty()) return;
+        GU_CUDA_CHECK(cudaMalloc(&dst, sizeof(int32_t) * src.size()));
+        g.extra_allocs.push_back(dst);
+        GU_CUDA_CHECK(cudaMemcpy(dst, src.data(), sizeof(int32_t) * src.size(), cudaMemcpyHostToDevice));
+        g.bytes += sizeof(int32_t) * src.size();
+    };
+    up(v, cm.v);
+    up(e0, cm.e0);
+    up(e1, cm.e1);
+    up(slot, cm.slot);
+    up(mv, cm.mv);
+    up(mfirst, cm.mfirst);
+    up(mcount, cm.mcount);
+    cm.nchunks = (int32_t)v.size();
+    cm.nmulti = (int32_t)mv.size();
+    cm.nslots = nslots;
+    cm.built = true;
+}
+
+static void ensure_chunks(DeviceGraph &g)
+{
+    if (!g.bc_out.built) build_chunks(g, g.host_R, g.bc_out);
+    if (!g.bc_in.built) {
+        if (g.directed) build_chunks(g, g.host_RT, g.bc_in);
+        else g.bc_in = g.bc_out;
+    }
+}
+
+static int bc_words_for(int32_t k, int requested)
+{
+    int W = requested;
+    if (W <= 0) {
+        const char *s = std::getenv("GU_BC_WORDS");
+        W = (s && *s) ? std::atoi(s) : 4;
+    }
+    if (W != 1 && W != 2 && W != 4 && W != 8 && W != 16)
+        throw gu_error(GU_ERR_INVALID_ARGUMENT, "BC batch must be 64, 128, 256, 512 or 1024 sources");
+    while (W > 1 && 64 * (W / 2) >= k) W /= 2;  // no wider than the request needs
+    return W;
+}
+
+static DevChunks dev_chunks(const ChunkMap &c)
+{
+    DevChunks d;
+    d.v = c.v;
+    d.e0 = c.e0;
+    d.e1 = c.e1;
+    d.slot = c.slot;
+    d.nchunks = c.nchunks;
+    d.mv = c.mv;
+    d.mfirst = c.mfirst;
+    d.mcount = c.mcount;
+    d.nmulti = c.nmulti;
+    return d;
+}
+
+void launch_bc(DeviceGraph &g, const int32_t *sources, int32_t k, int batch, double *bc, int32_t *dist_rows,
+               uint64_t *sigma_rows, double *delta_rows, int64_t ld, bool backward, cudaStream_t stream)
+{
+    if (batch > 0 && batch % 64) throw gu_error(GU_ERR_INVALID_ARGUMENT, "batch must be a multiple of 64");
+    const int W = bc_words_for(k, batch > 0 ? batch / 64 : 0);
+    ensure_chunks(g);
+    const size_t n = (size_t)g.n, B = 64 * (size_t)W;
+    auto up = [](size_t x) { return ((x + 255) / 256) * 256; };
+    const size_t words = up(n * W * sizeof(u64));
+    const size_t sig = up(n * B * sizeof(u64));
+    const size_t del = backward ? 2 * up(n * B * sizeof(double)) : 0;  // delta and beta
+    const size_t prt = backward ? up((size_t)g.bc_out.nslots * W * 64 * sizeof(double)) : 0;
+    const size_t bcb = up(n * sizeof(double));
+    // level store: as many levels as fit a budget (a BFS level is at most n - 1)
+    size_t budget = (size_t)8 << 30;
+    if (const char *s = std::getenv("GU_BC_LEVEL_BUDGET_MB")) budget = (size_t)std::atoll(s) << 20;
+    size_t maxl = budget / (words ? words : 1);
+    if (maxl < 2) maxl = 2;
+    if (maxl > n + 1) maxl = n + 1;
+    const size_t need = WS_CONTROL_BYTES + words + maxl * words + sig + del + prt + bcb;
+    char *ws = (char *)g.ws.get(need);
+    BcArgs a;
+    a.R = g.R;
+    a.C = g.C;
+    a.RT = g.RT;
+    a.CT = g.CT;
+    a.cin = dev_chunks(g.bc_in);
+    a.cout = dev_chunks(g.bc_out);
+    a.n = g.n;
+    a.W = W;
+    a.max_lvl = (int32_t)(maxl - 1);
+    a.sources = sources;
+    a.k = k;
+    char *p = ws;
+    a.ctl = reinterpret_cast<BcCtl *>(p);
+    p += WS_CONTROL_BYTES;
+    a.seen = reinterpret_cast<u64 *>(p);
+    p += words;
+    a.lvl = reinterpret_cast<u64 *>(p);
+    p += maxl * words;
+    a.sigma = reinterpret_cast<u64 *>(p);
+    p += sig;
+    a.delta = backward ? reinterpret_cast<double *>(p) : nullptr;
+    a.beta = backward ? reinterpret_cast<double *>(p + del / 2) : nullptr;
+    p += del;
+    a.part = backward ? reinterpret_cast<double *>(p) : nullptr;
+    p += prt;
+    a.bc = bc ? bc : reinterpret_cast<double *>(p);
+    a.dist_rows = dist_rows;
+    a.sigma_rows = reinterpret_cast<u64 *>(sigma_rows);
+    a.delta_rows = delta_rows;
+    a.ld = ld;
+    GU_CUDA_CHECK(cudaMemsetAsync(a.ctl, 0, sizeof(BcCtl), stream));
+    static int blocks_per_sm = -1;
+    if (blocks_per_sm < 0) {
+        GU_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, bc_grid_kernel, BC_THREADS, 0));
+        if (blocks_per_sm < 1) throw gu_error(GU_ERR_INTERNAL, "bc kernel cannot be resident");
+    }
+    dim3 grid(g.sm_count * blocks_per_sm), block(BC_THREADS);
+    int do_backward = backward ? 1 : 0;
+    void *params[] = {&a, &do_backward};
+    g.mark_start(stream);
+    GU_CUDA_CHECK(cudaLaunchCooperativeKernel((const void *)bc_grid_kernel, grid, block, params, 0, stream));
+    g.mark_stop(stream);
+}
+
+void bc_read_status(DeviceGraph &g, int *dev_err, int *max_level)
+{
+    BcCtl c;
+    GU_CUDA_CHECK(cudaMemcpy(&c, g.ws.ptr, sizeof(BcCtl), cudaMemcpyDeviceToHost));
+    if (dev_err) *dev_err = c.err;
+    if (max_level) *max_level = c.max_level;
+}
+
+}  // namespace gu

@@ -386,4 +386,89 @@ gu_status gu_bfs_host(gu_graph g, int variant, const int32_t *sources_host, int3
     });
 }
 
+// ---- shortest-path counts, betweenness, diameter, reachability -------------------------
+static void check_sources_device(DeviceGraph &dg, const int32_t *sources_dev, int32_t k, cudaStream_t st)
+{
+    if (k < 0) throw gu_error(GU_ERR_INVALID_ARGUMENT, "k must be >= 0");
+    if (k > 0 && !sources_dev) throw gu_error(GU_ERR_INVALID_ARGUMENT, "null sources");
+    std::vector<int32_t> hs((size_t)k);
+    if (k > 0) {
+        GU_CUDA_CHECK(cudaMemcpyAsync(hs.data(), sources_dev, sizeof(int32_t) * (size_t)k, cudaMemcpyDeviceToHost, st));
+        GU_CUDA_CHECK(cudaStreamSynchronize(st));
+    }
+    validate_sources_host(hs.data(), k, dg.n);
+}
+
+static void finish_bc(DeviceGraph &dg, cudaStream_t st)
+{
+    GU_CUDA_CHECK(cudaStreamSynchronize(st));
+    GU_CUDA_CHECK(cudaGetLastError());
+    int err = 0;
+    bc_read_status(dg, &err, nullptr);
+    if (err == DEV_ERR_BARRIER_TIMEOUT) throw gu_error(GU_ERR_TIMEOUT, "a device-side wait exceeded its limit");
+    if (err == 3) throw gu_error(GU_ERR_CAPACITY, "BFS deeper than the level store (raise GU_BC_LEVEL_BUDGET_MB)");
+    if (err != 0) throw gu_error(GU_ERR_INTERNAL, "device reported error code " + std::to_string(err));
+}
+
+gu_status gu_sigma(gu_graph g, const int32_t *sources_dev, int32_t k, int32_t *dist_dev, uint64_t *sigma_dev,
+                   int64_t ld, void *stream)
+{
+    return guarded([&] {
+        if (!g) throw gu_error(GU_ERR_INVALID_ARGUMENT, "null graph");
+        DeviceGraph &dg = *g->g;
+        if (ld < dg.n) throw gu_error(GU_ERR_INVALID_ARGUMENT, "ld must be >= n");
+        if (k > 0 && !sigma_dev) throw gu_error(GU_ERR_INVALID_ARGUMENT, "null sigma rows");
+        std::lock_guard<std::mutex> lk(dg.mu);
+        DeviceScope ds(dg.device);
+        cudaStream_t st = (cudaStream_t)stream;
+        check_sources_device(dg, sources_dev, k, st);
+        if (k == 0) return;
+        launch_bc(dg, sources_dev, k, 0, nullptr, dist_dev, sigma_dev, nullptr, ld, false, st);
+        finish_bc(dg, st);
+    });
+}
+
+gu_status gu_bc(gu_graph g, const int32_t *sources_dev, int32_t k, int32_t batch, double *bc_dev, double *delta_dev,
+                int64_t ld, void *stream)
+{
+    return guarded([&] {
+        if (!g) throw gu_error(GU_ERR_INVALID_ARGUMENT, "null graph");
+        DeviceGraph &dg = *g->g;
+        if (!bc_dev) throw gu_error(GU_ERR_INVALID_ARGUMENT, "null bc output");
+        if (delta_dev && ld < dg.n) throw gu_error(GU_ERR_INVALID_ARGUMENT, "ld must be >= n");
+        std::lock_guard<std::mutex> lk(dg.mu);
+        DeviceScope ds(dg.device);
+        cudaStream_t st = (cudaStream_t)stream;
+        check_sources_device(dg, sources_dev, k, st);
+        if (k == 0) {
+            GU_CUDA_CHECK(cudaMemsetAsync(bc_dev, 0, sizeof(double) * (size_t)dg.n, st));
+            GU_CUDA_CHECK(cudaStreamSynchronize(st));
+            return;
+        }
+        launch_bc(dg, sources_dev, k, batch, bc_dev, nullptr, nullptr, delta_dev, ld, true, st);
+        finish_bc(dg, st);
+    });
+}
+
+gu_status gu_diameter(gu_graph g, const int32_t *sources_dev, int32_t k, int32_t *diameter, void *stream)
+{
+    return guarded([&] {
+        if (!g || !diameter) throw gu_error(GU_ERR_INVALID_ARGUMENT, "null argument");
+        DeviceGraph &dg = *g->g;
+        std::lock_guard<std::mutex> lk(dg.mu);
+        DeviceScope ds(dg.device);
+        cudaStream_t st = (cudaStream_t)stream;
+        check_sources_device(dg, sources_dev, k, st);
+        *diameter = 0;
+        if (k == 0) return;
+        MsOptions opt;
+        opt.variant = GU_BFS_AUTO;
+        launch_msbfs(dg, sources_dev, k, nullptr, dg.n, opt, st, nullptr);
+        check_dev_status(dg, st);
+        int err = 0, td = 0, bu = 0, ml = 0;
+        msbfs_read_status(dg, &err, &td, &bu, &ml);
+        *diameter = ml;
+    });
+}
+
 }  // extern "C"

@@ -78,6 +78,7 @@ DeviceGraph::~DeviceGraph()
     ws.release();
     io.release();
     if (F) cudaFree(F);
+    for (void *p : extra_allocs) cudaFree(p);
     if (heavy) cudaFree(heavy);
     if (mid) cudaFree(mid);
     if (RT && RT != R) cudaFree(RT);
@@ -138,6 +139,7 @@ DeviceGraph *create_device_graph(const int32_t *R, const int32_t *C, int32_t n, 
     for (int32_t v = 0; v < n; ++v) outdeg[v] = R[v + 1] - R[v];
     std::vector<int32_t> Cs(C, C + m);
     sort_adjacency_by_key(R, Cs.data(), n, outdeg.data());
+    g->host_R.assign(R, R + n + 1);
     GU_CUDA_CHECK(cudaMalloc(&g->R, sizeof(int32_t) * ((size_t)n + 1)));
     GU_CUDA_CHECK(cudaMalloc(&g->C, sizeof(int32_t) * (size_t)(m > 0 ? m : 1)));
     GU_CUDA_CHECK(cudaMemcpyAsync(g->R, R, sizeof(int32_t) * ((size_t)n + 1), cudaMemcpyHostToDevice, stream));
@@ -150,6 +152,7 @@ DeviceGraph *create_device_graph(const int32_t *R, const int32_t *C, int32_t n, 
         h.C.assign(C, C + m);
         HostGraph t = transpose(h);
         sort_adjacency_by_key(t.R.data(), t.C.data(), n, outdeg.data());
+        g->host_RT = t.R;
         GU_CUDA_CHECK(cudaMalloc(&g->RT, sizeof(int32_t) * ((size_t)n + 1)));
         GU_CUDA_CHECK(cudaMalloc(&g->CT, sizeof(int32_t) * (size_t)(m > 0 ? m : 1)));
         GU_CUDA_CHECK(cudaMemcpyAsync(g->RT, t.R.data(), sizeof(int32_t) * ((size_t)n + 1), cudaMemcpyHostToDevice, stream));

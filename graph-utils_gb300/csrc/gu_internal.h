@@ -78,6 +78,23 @@ struct Workspace {
     void release();
 };
 
+// Adjacency cut into work items of at most BC_CHUNK_EDGES edges (every vertex
+// has at least one, possibly empty, item).  Device arrays; built on first use.
+constexpr int BC_CHUNK_EDGES = 256;
+struct ChunkMap {
+    int32_t *v = nullptr;      // [nchunks] vertex of the item
+    int32_t *e0 = nullptr;     // [nchunks] first edge
+    int32_t *e1 = nullptr;     // [nchunks] end edge
+    int32_t *slot = nullptr;   // [nchunks] partial slot of a split vertex's item, -1 if not split
+    int32_t nchunks = 0;
+    int32_t *mv = nullptr;     // [nmulti] vertices split into several items
+    int32_t *mfirst = nullptr; // [nmulti] their first item
+    int32_t *mcount = nullptr; // [nmulti] their number of items
+    int32_t nmulti = 0;
+    int32_t nslots = 0;        // items of split vertices
+    bool built = false;
+};
+
 // Device-resident graph (the reference's device_graph, device_graph.h:7-22):
 // 256-byte-aligned int32 arrays in HBM.  RT/CT is the transposed (in-edge)
 // CSR, identical to R/C for undirected graphs.  F (COO source of every CSR
@@ -103,6 +120,11 @@ struct DeviceGraph {
     Workspace ws;  // kernel scratch
     Workspace io;  // device staging for calls that take host buffers
     int sm_count = 0;
+    // BC work items over in-edges (forward) and out-edges (backward); for
+    // undirected graphs bc_out aliases bc_in
+    ChunkMap bc_in, bc_out;
+    std::vector<int32_t> host_R, host_RT;  // offsets kept on the host for building work items
+    std::vector<void *> extra_allocs;  // freed with the graph
     // events bracketing the last main kernel launch (kernel-only timing)
     cudaEvent_t ev_start = nullptr, ev_stop = nullptr;
     bool timed = false;
@@ -124,6 +146,11 @@ void launch_msbfs(DeviceGraph &g, const int32_t *sources, int32_t k, int32_t *di
                   const MsOptions &opt, cudaStream_t stream, int *dev_err_out);
 void launch_plain_bfs(DeviceGraph &g, const int32_t *sources, int32_t k, int32_t *dist, int64_t ld,
                       cudaStream_t stream);
+// Batched sigma / Brandes: bc (n doubles, may be null), optional rows (k x ld).
+void launch_bc(DeviceGraph &g, const int32_t *sources, int32_t k, int batch, double *bc, int32_t *dist_rows,
+               uint64_t *sigma_rows, double *delta_rows, int64_t ld, bool backward, cudaStream_t stream);
+void bc_read_status(DeviceGraph &g, int *dev_err, int *max_level);
+void msbfs_read_status(DeviceGraph &g, int *dev_err, int *td_levels, int *bu_levels, int *max_level);
 void ensure_coo(DeviceGraph &g, cudaStream_t stream);
 int device_sm_count(int device);
 

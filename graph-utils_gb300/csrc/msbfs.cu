@@ -942,7 +942,7 @@ __global__ void __launch_bounds__(MS_THREADS, MS_MIN_BLOCKS) ms_grid_kernel(MsAr
         // F_{j-1} is empty: levels of this batch are 0..j-2
         int used = 0;
         while (used < 31 && ((j - 2) >> used) != 0) ++used;
-        write_distances<W, GridG>(a, row0, nb, used);
+        if (a.dist) write_distances<W, GridG>(a, row0, nb, used);  // no rows: diameter queries
         if (threadIdx.x == 0) record_event(ctl, ev_idx, rank == 0, b, j, 2, 0, 0);  // distance rows written
         ++ev_idx;
         if (!grid_barrier(&ctl->bar, &ctl->err, epoch)) return;

@@ -78,6 +78,9 @@ def lib():
                                     ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
         "gu_bfs": ([_vp, ctypes.c_int, _vp, ctypes.c_int32, _vp, ctypes.c_int64, _vp], ctypes.c_int),
         "gu_bfs_host": ([_vp, ctypes.c_int, _i32p, ctypes.c_int32, _i32p, ctypes.c_int64, _vp], ctypes.c_int),
+        "gu_sigma": ([_vp, _vp, ctypes.c_int32, _vp, _vp, ctypes.c_int64, _vp], ctypes.c_int),
+        "gu_bc": ([_vp, _vp, ctypes.c_int32, ctypes.c_int32, _vp, _vp, ctypes.c_int64, _vp], ctypes.c_int),
+        "gu_diameter": ([_vp, _vp, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32), _vp], ctypes.c_int),
         "gu_bfs_noalloc": ([_vp, _vp, ctypes.c_int32, ctypes.c_int64, _vp, ctypes.c_int32, _vp, ctypes.c_int64, _vp],
                            ctypes.c_int),
     }
@@ -226,6 +229,27 @@ class Graph:
         check(lib().gu_bfs(self._h, VARIANTS[variant] if isinstance(variant, str) else variant,
                            sources_dev.data_ptr(), k, dist_dev.data_ptr(), ld, _stream_handle(stream)))
         return dist_dev
+
+    def sigma(self, sources_dev, sigma_dev, dist_dev=None, ld=None, stream=None):
+        """Shortest-path counts (uint64 rows, int64 tensor view) and optional distances."""
+        ld = self.n if ld is None else ld
+        check(lib().gu_sigma(self._h, sources_dev.data_ptr(), int(sources_dev.numel()),
+                             dist_dev.data_ptr() if dist_dev is not None else None, sigma_dev.data_ptr(), ld,
+                             _stream_handle(stream)))
+        return sigma_dev
+
+    def bc(self, sources_dev, bc_dev, delta_dev=None, batch=0, ld=None, stream=None):
+        """Betweenness (float64 tensor of n) from the given sources; optional delta rows."""
+        ld = self.n if ld is None else ld
+        check(lib().gu_bc(self._h, sources_dev.data_ptr(), int(sources_dev.numel()), batch, bc_dev.data_ptr(),
+                          delta_dev.data_ptr() if delta_dev is not None else None, ld, _stream_handle(stream)))
+        return bc_dev
+
+    def diameter(self, sources_dev, stream=None):
+        d = ctypes.c_int32()
+        check(lib().gu_diameter(self._h, sources_dev.data_ptr(), int(sources_dev.numel()), ctypes.byref(d),
+                                _stream_handle(stream)))
+        return d.value
 
     def bfs_host(self, sources_host, variant="auto", out=None, stream=None):
         """Host form: numpy sources in, numpy k x n int32 distances out."""

@@ -144,6 +144,30 @@ gu_status gu_bfs(gu_graph g, int variant, const int32_t *sources_dev, int32_t k,
 gu_status gu_bfs_host(gu_graph g, int variant, const int32_t *sources_host, int32_t k, int32_t *dist_host,
                       int64_t ld, void *stream);
 
+/* ---- shortest-path counts and betweenness ------------------------------------ */
+/* Row i of sigma_dev (uint64, stride ld) = number of shortest paths from
+ * sources[i] to every vertex (wrapping uint64 arithmetic, 0 where unreachable,
+ * 1 at the source); dist_dev (nullable, int32) receives the distances.  Replaces
+ * count_shortest_paths_setup (count_shortest_paths/count_shortest_paths.cuh:13),
+ * whose kernel the reference only designed (shuffle_based.cu:113-151). */
+gu_status gu_sigma(gu_graph g, const int32_t *sources_dev, int32_t k, int32_t *dist_dev, uint64_t *sigma_dev,
+                   int64_t ld, void *stream);
+
+/* Brandes betweenness from the given sources: bc_dev[v] = sum over sources s of
+ * delta_s(v), v != s (unnormalised, ordered pairs, as the reference's bc.cu:11-57
+ * and shuffle_based.cu:153-542), in FP64 with a fixed summation order
+ * (deterministic).  `batch` = sources per pass (64, 128, 256, 512 or 1024; 0 =
+ * default 256).  delta_dev (nullable, k x ld doubles) receives the per-source
+ * dependencies, 0 at the source and where unreachable.  Replaces
+ * betweenness_centrality_setup (betweenness_centrality.cuh:14), which returns
+ * float delta rows. */
+gu_status gu_bc(gu_graph g, const int32_t *sources_dev, int32_t k, int32_t batch, double *bc_dev, double *delta_dev,
+                int64_t ld, void *stream);
+
+/* Largest finite BFS distance from the given sources (0 if none).  Replaces
+ * diameter_sampling_setup (diameter_sampling/diameter_sampling.cuh:13). */
+gu_status gu_diameter(gu_graph g, const int32_t *sources_dev, int32_t k, int32_t *diameter, void *stream);
+
 /* Multi-source BFS that allocates no device memory.  No counterpart in the
  * reference: it exists for callers that may not call cudaMalloc while they
  * search -- code living in a process whose allocator owns every byte of the GPU
