@@ -450,6 +450,42 @@ gu_status gu_bc(gu_graph g, const int32_t *sources_dev, int32_t k, int32_t batch
     });
 }
 
+// ---- load-balanced search and race-and-resolve ------------------------------------
+// per-device scratch for calls without a graph handle (grown on demand)
+static Workspace &device_scratch(int dev)
+{
+    static std::mutex mu;
+    static Workspace ws[128];
+    if (dev < 0 || dev >= 128) throw gu_error(GU_ERR_UNSUPPORTED, "device ordinal out of range");
+    std::lock_guard<std::mutex> lk(mu);
+    return ws[dev];
+}
+static std::mutex g_scratch_call_mu;
+
+gu_status gu_lbs(const int32_t *counts_dev, int32_t N, int32_t *scanned_dev, int32_t *result_dev,
+                 int64_t result_capacity, int32_t *total_dev, int64_t *total_host, void *stream)
+{
+    return guarded([&] {
+        std::lock_guard<std::mutex> lk(g_scratch_call_mu);
+        int dev = 0;
+        GU_CUDA_CHECK(cudaGetDevice(&dev));
+        Workspace &ws = device_scratch(dev);
+        const size_t need = lbs_scratch_bytes(N);
+        void *p = ws.get(need);
+        launch_lbs(counts_dev, N, scanned_dev, result_dev, result_capacity, total_dev, total_host, p, ws.bytes,
+                   (cudaStream_t)stream);
+    });
+}
+
+gu_status gu_race_and_resolve(const int32_t *predicates_dev, int32_t nwarps, int32_t *winners_dev, void *stream)
+{
+    return guarded([&] {
+        if (nwarps < 0) throw gu_error(GU_ERR_INVALID_ARGUMENT, "nwarps must be >= 0");
+        if (nwarps > 0 && (!predicates_dev || !winners_dev)) throw gu_error(GU_ERR_INVALID_ARGUMENT, "null buffer");
+        launch_race_and_resolve(predicates_dev, nwarps, winners_dev, (cudaStream_t)stream);
+    });
+}
+
 gu_status gu_diameter(gu_graph g, const int32_t *sources_dev, int32_t k, int32_t *diameter, void *stream)
 {
     return guarded([&] {

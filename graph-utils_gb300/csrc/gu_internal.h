@@ -150,6 +150,10 @@ void launch_plain_bfs(DeviceGraph &g, const int32_t *sources, int32_t k, int32_t
 void launch_bc(DeviceGraph &g, const int32_t *sources, int32_t k, int batch, double *bc, int32_t *dist_rows,
                uint64_t *sigma_rows, double *delta_rows, int64_t ld, bool backward, cudaStream_t stream);
 void bc_read_status(DeviceGraph &g, int *dev_err, int *max_level);
+size_t lbs_scratch_bytes(int32_t N);
+void launch_lbs(const int32_t *counts, int32_t N, int32_t *scanned, int32_t *result, int64_t result_capacity,
+                int32_t *total_dev, int64_t *total_host, void *scratch_ptr, size_t scratch_bytes, cudaStream_t st);
+void launch_race_and_resolve(const int32_t *pred, int32_t nwarps, int32_t *winner, cudaStream_t st);
 void msbfs_read_status(DeviceGraph &g, int *dev_err, int *td_levels, int *bu_levels, int *max_level);
 void ensure_coo(DeviceGraph &g, cudaStream_t stream);
 int device_sm_count(int device);

@@ -1,0 +1,256 @@
+// lbs.cu -- load-balanced search and warp race-and-resolve on sm_103a.
+//
+// Load-balanced search (load_balanced_search.cu:123-192, example lbs.cu:18-31):
+// given per-item work counts, scanned = exclusive prefix sum (int32), total =
+// sum, and result[i] for every work slot i < total = the item owning it
+// (upper_bound(scanned, i) - 1).  The reference runs it in ONE CTA whose threads
+// each walk the scanned array from the start (quadratic in the item count);
+// here:
+//   1. scan: CTAs reduce tiles of 4096 counts (int64, warp shuffles), one CTA
+//      scans the tile sums, CTAs rescan their tiles with the tile offset;
+//   2. search: merge-path partition (the merge of slot keys 0..total-1 with the
+//      scanned offsets, ties to the offsets) into equal diagonals of 4096; a CTA
+//      finds its two path endpoints by binary search, stages its offsets in
+//      shared memory, every thread merges 8 steps from its own diagonal, and
+//      the CTA writes its run of owners contiguously.
+// race_and_resolve (race_and_resolve.cuh:13-25) is exposed as a warp-level
+// kernel over an array of predicates for testing the device primitive.
+#include "device_utils.cuh"
+#include "gu_internal.h"
+
+namespace gu {
+
+constexpr int LBS_THREADS = 512;
+constexpr int LBS_ITEMS = 8;
+constexpr int LBS_TILE = LBS_THREADS * LBS_ITEMS;  // counts per scan tile / diagonals per search tile
+
+__device__ __forceinline__ long long block_reduce_ll(long long x, long long *s_warp)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(FULL_MASK, x, o);
+    if (lane_id() == 0) s_warp[warp_in_block()] = x;
+    __syncthreads();
+    long long t = 0;
+    if (warp_in_block() == 0) {
+        t = lane_id() < (int)(blockDim.x >> 5) ? s_warp[lane_id()] : 0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(FULL_MASK, t, o);
+    }
+    __syncthreads();
+    return t;  // valid in warp 0
+}
+
+// exclusive scan of one value per thread across the CTA (warp shuffles)
+__device__ __forceinline__ long long block_exscan_ll(long long x, long long *s_warp, long long *total)
+{
+    const int lane = lane_id(), wid = warp_in_block(), nw = blockDim.x >> 5;
+    long long incl = x;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const long long y = __shfl_up_sync(FULL_MASK, incl, o);
+        if (lane >= o) incl += y;
+    }
+    if (lane == 31) s_warp[wid] = incl;
+    __syncthreads();
+    if (wid == 0) {
+        const long long t = lane < nw ? s_warp[lane] : 0;
+        long long ti = t;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const long long y = __shfl_up_sync(FULL_MASK, ti, o);
+            if (lane >= o) ti += y;
+        }
+        if (lane < nw) s_warp[lane] = ti - t;
+        if (lane == 31) s_warp[32] = ti;
+    }
+    __syncthreads();
+    const long long r = s_warp[wid] + incl - x;
+    *total = s_warp[32];
+    __syncthreads();
+    return r;
+}
+
+__global__ void __launch_bounds__(LBS_THREADS) lbs_tile_sums(const int32_t *__restrict__ counts, int32_t N,
+                                                             long long *__restrict__ tile_sum, int *negative)
+{
+    __shared__ long long s_warp[33];
+    const long long base = (long long)blockIdx.x * LBS_TILE;
+    long long s = 0;
+    bool neg = false;
+#pragma unroll
+    for (int t = 0; t < LBS_ITEMS; ++t) {
+        const long long i = base + (long long)t * LBS_THREADS + threadIdx.x;
+        if (i < N) {
+            const int32_t c = counts[i];
+            neg |= c < 0;
+            s += c;
+        }
+    }
+    if (__any_sync(FULL_MASK, neg) && lane_id() == 0) atomicOr(negative, 1);
+    const long long tot = block_reduce_ll(s, s_warp);
+    if (threadIdx.x == 0) tile_sum[blockIdx.x] = tot;
+}
+
+// one CTA: exclusive scan of the tile sums in chunks of blockDim; last entry = total
+__global__ void __launch_bounds__(LBS_THREADS) lbs_scan_tiles(long long *__restrict__ tile_sum, int32_t ntiles,
+                                                              long long *__restrict__ total)
+{
+    __shared__ long long s_warp[33];
+    long long carry = 0;
+    for (int base = 0; base < ntiles; base += blockDim.x) {
+        const int i = base + threadIdx.x;
+        const long long x = i < ntiles ? tile_sum[i] : 0;
+        long long tot;
+        const long long ex = block_exscan_ll(x, s_warp, &tot);
+        if (i < ntiles) tile_sum[i] = carry + ex;
+        carry += tot;
+    }
+    if (threadIdx.x == 0) *total = carry;
+}
+
+// rescan each tile with its offset; counts are read in blocked order (thread t
+// owns LBS_ITEMS consecutive counts) so the scan order is the array order
+__global__ void __launch_bounds__(LBS_THREADS) lbs_scan_write(const int32_t *__restrict__ counts, int32_t N,
+                                                              const long long *__restrict__ tile_off,
+                                                              int32_t *__restrict__ scanned)
+{
+    __shared__ long long s_warp[33];
+    const long long base = (long long)blockIdx.x * LBS_TILE + (long long)threadIdx.x * LBS_ITEMS;
+    int32_t v[LBS_ITEMS];
+    long long s = 0;
+#pragma unroll
+    for (int t = 0; t < LBS_ITEMS; ++t) {
+        v[t] = base + t < N ? counts[base + t] : 0;
+        s += v[t];
+    }
+    long long tot;
+    long long run = tile_off[blockIdx.x] + block_exscan_ll(s, s_warp, &tot);
+#pragma unroll
+    for (int t = 0; t < LBS_ITEMS; ++t) {
+        if (base + t < N) scanned[base + t] = (int32_t)run;
+        run += v[t];
+    }
+}
+
+// Merge-path split of diagonal d between slot keys A[i] = i (i < total) and
+// offsets B[k] = scanned[k] (k < N), ties to B: returns the number of offsets
+// among the first d merged elements.
+__device__ __forceinline__ int32_t merge_path(const int32_t *B, int32_t N, long long total, long long d)
+{
+    long long lo = d > total ? d - total : 0;
+    long long hi = d < N ? d : N;
+    while (lo < hi) {
+        const long long k = (lo + hi) >> 1;  // candidate: k offsets consumed
+        // B[k] belongs before A[d-k-1]  <=>  B[k] <= d-k-1
+        if ((long long)B[k] <= d - k - 1) lo = k + 1;
+        else hi = k;
+    }
+    return (int32_t)lo;
+}
+
+__global__ void __launch_bounds__(LBS_THREADS) lbs_search(const int32_t *__restrict__ scanned, int32_t N,
+                                                          long long total, int32_t *__restrict__ result)
+{
+    __shared__ int32_t s_b[LBS_TILE + 1];
+    __shared__ int32_t s_out[LBS_TILE];
+    __shared__ int32_t s_k[2];
+    const long long d0 = (long long)blockIdx.x * LBS_TILE;
+    const long long d1 = min(d0 + LBS_TILE, total + N);
+    if (threadIdx.x == 0) s_k[0] = merge_path(scanned, N, total, d0);
+    if (threadIdx.x == 32) s_k[1] = merge_path(scanned, N, total, d1);
+    __syncthreads();
+    const int32_t k0 = s_k[0], k1 = s_k[1];
+    const long long i0 = d0 - k0, i1 = d1 - k1;  // slots [i0, i1) of this tile
+    const int nb = k1 - k0;
+    for (int t = threadIdx.x; t < nb; t += blockDim.x) s_b[t] = scanned[k0 + t];
+    __syncthreads();
+    // this thread's diagonal, then LBS_ITEMS merge steps
+    const long long dt = min(d0 + (long long)threadIdx.x * LBS_ITEMS, d1) - d0;
+    long long lo = dt > (i1 - i0) ? dt - (i1 - i0) : 0, hi = dt < nb ? dt : nb;
+    while (lo < hi) {
+        const long long k = (lo + hi) >> 1;
+        if ((long long)s_b[k] <= i0 + (dt - k) - 1) lo = k + 1;
+        else hi = k;
+    }
+    int kk = (int)lo;
+    long long ii = i0 + (dt - lo);
+    for (int step = 0; step < LBS_ITEMS && (ii - i0) + kk < (i1 - i0) + nb; ++step) {
+        const bool take_slot = kk >= nb || ii < (long long)s_b[kk];
+        if (take_slot) {
+            if (ii >= i1) break;
+            s_out[ii - i0] = k0 + kk - 1;
+            ++ii;
+        } else {
+            ++kk;
+        }
+    }
+    __syncthreads();
+    for (long long i = threadIdx.x; i < i1 - i0; i += blockDim.x) result[i0 + i] = s_out[i];
+}
+
+// Winner lane per warp of 32 predicates (race_and_resolve_warp).
+__global__ void race_and_resolve_kernel(const int32_t *__restrict__ pred, int32_t nwarps, int32_t *__restrict__ winner)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if ((i >> 5) >= nwarps) return;  // whole warps only (blockDim is a multiple of 32)
+    winner[i] = race_and_resolve_warp(pred[i] != 0);
+}
+
+size_t lbs_scratch_bytes(int32_t N)
+{
+    const size_t ntiles = (size_t)(((long long)(N > 0 ? N : 0) + LBS_TILE - 1) / LBS_TILE);
+    return (ntiles + 2) * sizeof(long long) + 256;
+}
+
+void launch_lbs(const int32_t *counts, int32_t N, int32_t *scanned, int32_t *result, int64_t result_capacity,
+                int32_t *total_dev, int64_t *total_host, void *scratch_ptr, size_t scratch_bytes, cudaStream_t st)
+{
+    if (N < 0) throw gu_error(GU_ERR_INVALID_ARGUMENT, "N must be >= 0");
+    if (N > 0 && (!counts || !scanned)) throw gu_error(GU_ERR_INVALID_ARGUMENT, "null counts or scanned");
+    const int32_t ntiles = (int32_t)(((long long)N + LBS_TILE - 1) / LBS_TILE);
+    if (scratch_bytes < lbs_scratch_bytes(N)) throw gu_error(GU_ERR_INTERNAL, "lbs scratch too small");
+    long long *tile = reinterpret_cast<long long *>(scratch_ptr);
+    long long *tot_d = tile + ntiles;
+    int *neg_d = reinterpret_cast<int *>(tot_d + 1);
+    long long tot = 0;
+    int neg = 0;
+    if (N > 0) {
+        GU_CUDA_CHECK(cudaMemsetAsync(neg_d, 0, sizeof(int), st));
+        lbs_tile_sums<<<ntiles, LBS_THREADS, 0, st>>>(counts, N, tile, neg_d);
+        lbs_scan_tiles<<<1, LBS_THREADS, 0, st>>>(tile, ntiles, tot_d);
+        GU_CUDA_CHECK(cudaGetLastError());
+        GU_CUDA_CHECK(cudaMemcpyAsync(&tot, tot_d, sizeof(long long), cudaMemcpyDeviceToHost, st));
+        GU_CUDA_CHECK(cudaMemcpyAsync(&neg, neg_d, sizeof(int), cudaMemcpyDeviceToHost, st));
+        GU_CUDA_CHECK(cudaStreamSynchronize(st));
+    }
+    if (total_host) *total_host = tot;
+    if (neg) throw gu_error(GU_ERR_INVALID_ARGUMENT, "work counts must be >= 0");
+    if (tot > INT32_MAX) throw gu_error(GU_ERR_OVERFLOW, "total work exceeds INT32_MAX (int32 scanned offsets)");
+    if (tot > result_capacity)
+        throw gu_error(GU_ERR_CAPACITY, "result buffer holds " + std::to_string(result_capacity) + " slots, need " +
+                                            std::to_string(tot));
+    if (tot > 0 && !result) throw gu_error(GU_ERR_INVALID_ARGUMENT, "null result");
+    if (N > 0) {
+        lbs_scan_write<<<ntiles, LBS_THREADS, 0, st>>>(counts, N, tile, scanned);
+        const long long ndiag = tot + N;
+        const int32_t nsearch = (int32_t)((ndiag + LBS_TILE - 1) / LBS_TILE);
+        if (tot > 0) lbs_search<<<nsearch, LBS_THREADS, 0, st>>>(scanned, N, tot, result);
+        GU_CUDA_CHECK(cudaGetLastError());
+    }
+    if (total_dev) {
+        const int32_t t32 = (int32_t)tot;
+        GU_CUDA_CHECK(cudaMemcpyAsync(total_dev, &t32, sizeof(int32_t), cudaMemcpyHostToDevice, st));
+    }
+    GU_CUDA_CHECK(cudaStreamSynchronize(st));
+}
+
+void launch_race_and_resolve(const int32_t *pred, int32_t nwarps, int32_t *winner, cudaStream_t st)
+{
+    if (nwarps <= 0) return;
+    const long long threads = (long long)nwarps * 32;
+    race_and_resolve_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(pred, nwarps, winner);
+    GU_CUDA_CHECK(cudaGetLastError());
+    GU_CUDA_CHECK(cudaStreamSynchronize(st));
+}
+
+}  // namespace gu

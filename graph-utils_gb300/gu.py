@@ -81,6 +81,8 @@ def lib():
         "gu_sigma": ([_vp, _vp, ctypes.c_int32, _vp, _vp, ctypes.c_int64, _vp], ctypes.c_int),
         "gu_bc": ([_vp, _vp, ctypes.c_int32, ctypes.c_int32, _vp, _vp, ctypes.c_int64, _vp], ctypes.c_int),
         "gu_diameter": ([_vp, _vp, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32), _vp], ctypes.c_int),
+        "gu_lbs": ([_vp, ctypes.c_int32, _vp, _vp, ctypes.c_int64, _vp, _i64p, _vp], ctypes.c_int),
+        "gu_race_and_resolve": ([_vp, ctypes.c_int32, _vp, _vp], ctypes.c_int),
         "gu_bfs_noalloc": ([_vp, _vp, ctypes.c_int32, ctypes.c_int64, _vp, ctypes.c_int32, _vp, ctypes.c_int64, _vp],
                            ctypes.c_int),
     }
@@ -260,3 +262,20 @@ class Graph:
         check(lib().gu_bfs_host(self._h, VARIANTS[variant] if isinstance(variant, str) else variant, _ptr(s), k,
                                 out.ctypes.data_as(_i32p), out.shape[1], _stream_handle(stream)))
         return out
+
+
+def lbs(counts_dev, scanned_dev, result_dev, total_dev=None, stream=None):
+    """Load-balanced search on device tensors; returns the total (int)."""
+    tot = ctypes.c_int64()
+    check(lib().gu_lbs(counts_dev.data_ptr(), int(counts_dev.numel()), scanned_dev.data_ptr(),
+                       result_dev.data_ptr() if result_dev.numel() else None, int(result_dev.numel()),
+                       total_dev.data_ptr() if total_dev is not None else None, ctypes.byref(tot),
+                       _stream_handle(stream)))
+    return tot.value
+
+
+def race_and_resolve(pred_dev, winners_dev, stream=None):
+    """Winner lane per group of 32 predicates (device tensors, int32)."""
+    check(lib().gu_race_and_resolve(pred_dev.data_ptr(), int(pred_dev.numel()) // 32, winners_dev.data_ptr(),
+                                    _stream_handle(stream)))
+    return winners_dev

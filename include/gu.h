@@ -168,6 +168,24 @@ gu_status gu_bc(gu_graph g, const int32_t *sources_dev, int32_t k, int32_t batch
  * diameter_sampling_setup (diameter_sampling/diameter_sampling.cuh:13). */
 gu_status gu_diameter(gu_graph g, const int32_t *sources_dev, int32_t k, int32_t *diameter, void *stream);
 
+/* ---- load-balanced search and race-and-resolve ------------------------------- */
+/* Load-balanced search over N work counts (device pointers, counts >= 0):
+ * scanned_dev[i] = exclusive prefix sum of counts (int32), total = sum, and
+ * result_dev[j] for every work slot j < total = the item that owns it
+ * (upper_bound(scanned, j) - 1).  The total is returned in *total_host and/or
+ * *total_dev (either may be NULL).  GU_ERR_OVERFLOW if the total exceeds
+ * INT32_MAX, GU_ERR_CAPACITY if it exceeds result_capacity (nothing written to
+ * result then).  Replaces extract_edges_{warp,block} / load_balance_search_{warp,
+ * block} (load_balanced_search.cuh:10-13, load_balanced_search.cu:63-202). */
+gu_status gu_lbs(const int32_t *counts_dev, int32_t N, int32_t *scanned_dev, int32_t *result_dev,
+                 int64_t result_capacity, int32_t *total_dev, int64_t *total_host, void *stream);
+
+/* Warp leader election over nwarps groups of 32 predicates: winners_dev[32w+l] =
+ * the highest lane of group w whose predicate is non-zero, or l itself if none
+ * is.  Exposes race_and_resolve_warp (race_and_resolve.cuh:13-25), the device
+ * primitive the WARP and CTA_WARP gathers use. */
+gu_status gu_race_and_resolve(const int32_t *predicates_dev, int32_t nwarps, int32_t *winners_dev, void *stream);
+
 /* Multi-source BFS that allocates no device memory.  No counterpart in the
  * reference: it exists for callers that may not call cudaMalloc while they
  * search -- code living in a process whose allocator owns every byte of the GPU

@@ -1,0 +1,93 @@
+"""Load-balanced search and race-and-resolve on the GPU against the oracle.
+
+LBS must be bit-exact (int32 scan, owners, total) against the golden vectors of
+the reference's examples/load_balanced_search/lbs.cu and against
+oracle/gu_oracle.c on larger inputs, including the per-vertex degree array of
+the 2048 x 2048 grid (4,194,304 counts).
+"""
+import numpy as np
+import pytest
+
+import gu
+import oracle
+from conftest import golden_names, load_golden
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+
+def run_lbs(counts, capacity=None):
+    c = torch.as_tensor(np.asarray(counts, np.int32), device="cuda")
+    total = int(np.sum(np.asarray(counts, np.int64)))
+    cap = total if capacity is None else capacity
+    scanned = torch.empty(max(len(counts), 1), dtype=torch.int32, device="cuda")
+    result = torch.empty(max(cap, 0), dtype=torch.int32, device="cuda")
+    tdev = torch.full((1,), -1, dtype=torch.int32, device="cuda")
+    t = gu.lbs(c, scanned, result, total_dev=tdev)
+    torch.cuda.synchronize()
+    return scanned[: len(counts)].cpu().numpy(), result[:t].cpu().numpy(), t, int(tdev.item())
+
+
+@pytest.mark.parametrize("name", golden_names("lbs_"))
+def test_lbs_golden(name):
+    g = load_golden(name, "lbs_")
+    scanned, result, total, tdev = run_lbs(g["counts"])
+    assert total == tdev == int(g["counts"].sum())
+    np.testing.assert_array_equal(scanned, g["scanned"])
+    np.testing.assert_array_equal(result, g["result"])
+
+
+@pytest.mark.parametrize("seed,N,hi", [(1, 1_000_003, 8), (2, 50_000, 2000), (3, 4097, 1), (4, 123_457, 0)])
+def test_lbs_random_vs_oracle(seed, N, hi):
+    rng = np.random.default_rng(seed)
+    counts = rng.integers(0, hi + 1, N).astype(np.int32)
+    counts[rng.random(N) < 0.3] = 0
+    scanned, result, total, _ = run_lbs(counts)
+    rs, rr, rt = oracle.lbs(counts)
+    assert total == rt
+    np.testing.assert_array_equal(scanned, rs)
+    np.testing.assert_array_equal(result, rr)
+
+
+def test_lbs_grid_degree_array():
+    hg = gu.HostGraph.grid(2048, 2048, 0.05, seed=7)
+    counts = np.diff(hg.R).astype(np.int32)
+    scanned, result, total, _ = run_lbs(counts)
+    rs, rr, rt = oracle.lbs(counts)
+    assert total == rt == hg.m
+    np.testing.assert_array_equal(scanned, rs)
+    np.testing.assert_array_equal(result, rr)
+
+
+def test_lbs_errors():
+    L = gu.lib()
+    with pytest.raises(gu.GuError) as e:
+        run_lbs(np.full(4, 2 ** 30, np.int32), capacity=16)
+    assert e.value.status == 5  # overflow
+    with pytest.raises(gu.GuError) as e:
+        run_lbs(np.full(10, 5, np.int32), capacity=20)
+    assert e.value.status == 4 and b"50" in L.gu_last_error()
+    with pytest.raises(gu.GuError) as e:
+        run_lbs(np.array([3, -1, 4], np.int32), capacity=6)
+    assert e.value.status == 1
+    # no items
+    c = torch.zeros(0, dtype=torch.int32, device="cuda")
+    assert gu.lbs(c, torch.zeros(1, dtype=torch.int32, device="cuda"), torch.zeros(0, dtype=torch.int32,
+                                                                                      device="cuda")) == 0
+
+
+def test_race_and_resolve_vs_oracle():
+    rng = np.random.default_rng(5)
+    nw = 4096
+    pred = (rng.random(nw * 32) < rng.choice([0.0, 0.03, 0.5, 1.0], nw).repeat(32)).astype(np.int32)
+    p = torch.as_tensor(pred, device="cuda")
+    w = torch.empty_like(p)
+    gu.race_and_resolve(p, w)
+    got = w.cpu().numpy()
+    for g in range(nw):
+        vote = 0
+        for l in range(32):
+            if pred[32 * g + l]:
+                vote |= 1 << l
+        for l in range(32):
+            assert got[32 * g + l] == oracle.race_and_resolve(vote, l)
