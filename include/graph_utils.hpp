@@ -1,0 +1,293 @@
+// graph_utils.hpp -- C++ drop-in for graph-utils' multi-source search entry points.
+//
+// Header-only layer over the C ABI (gu.h), so it compiles against the caller's
+// own host_graph (the reference's parse.h:15-35) and adds no C++ symbols to the
+// library.  Include the reference's parse.h / util.h first, or define
+// GU_DEFINE_HOST_TYPES to get layout-compatible host_graph / program_options.
+//
+// Replaces: device_graph (device_graph.h:7-22); multi_search_*_setup
+// (linear_with_atomics.cuh:14, edge_parallel.cuh:13, warp_based.cuh:15,
+// CTA_warp.cuh:15, scan_based.cuh:15, shuffle_based.cuh:16);
+// betweenness_centrality_setup (betweenness_centrality.cuh:14);
+// count_shortest_paths_setup (count_shortest_paths.cuh:13);
+// diameter_sampling_setup (diameter_sampling.cuh:13); transitive_closure_setup
+// (transitive_closure.cuh:13); extract_edges_{block,warp}
+// (load_balanced_search.cuh:12-13, called as host functions here, without the
+// <<<1, BLOCK_SIZE>>> launch configuration).
+//
+// Semantics kept: every source in [start, end) is searched; the returned rows
+// are those of the last R = min(end - start, #SMs) sources, source s in row
+// (s - start) % R (the reference's one-CTA-per-source grid, common.cu:3-28, and
+// its checker multi_search_test.cu:43-63).  Timing lines are printed like the
+// reference's.  Errors throw std::runtime_error (the reference exits).
+#pragma once
+
+#include <algorithm>
+#include <cstdint>
+#include <cstdio>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime_api.h>
+
+#include "gu.h"
+
+#ifdef GU_DEFINE_HOST_TYPES
+class host_graph {
+public:
+    std::vector<int> C;  // neighbours
+    std::vector<int> R;  // offsets
+    std::vector<int> F;  // edge sources
+    int n = 0;
+    int m = 0;
+    bool directed = false;
+};
+class program_options {
+public:
+    int device = -1;
+    char *infile = nullptr;
+    char *outfile = nullptr;
+    bool verify = false;
+    int approx = 0;
+    char *format = nullptr;
+    bool isTesla = false;
+    bool nvml = false;
+};
+#endif
+
+namespace gu_shim {
+
+inline void check(gu_status s, const char *what)
+{
+    if (s != GU_OK) throw std::runtime_error(std::string(what) + ": " + gu_last_error());
+}
+
+inline int sm_count()
+{
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    return sms > 0 ? sms : 1;
+}
+
+// Device buffer owned by the shim for the duration of one call.
+template <class T>
+struct dbuf {
+    T *p = nullptr;
+    explicit dbuf(size_t count)
+    {
+        if (count && cudaMalloc((void **)&p, sizeof(T) * count) != cudaSuccess)
+            throw std::runtime_error("cudaMalloc failed");
+    }
+    ~dbuf() { if (p) cudaFree(p); }
+    dbuf(const dbuf &) = delete;
+    dbuf &operator=(const dbuf &) = delete;
+};
+
+inline double seconds_since(const cudaEvent_t &a)
+{
+    cudaEvent_t b;
+    cudaEventCreate(&b);
+    cudaEventRecord(b, 0);
+    cudaEventSynchronize(b);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, a, b);
+    cudaEventDestroy(b);
+    return ms / 1000.0;
+}
+
+struct timer {
+    cudaEvent_t a;
+    timer() { cudaEventCreate(&a); cudaEventRecord(a, 0); }
+    ~timer() { cudaEventDestroy(a); }
+    double stop() const { return seconds_since(a); }
+};
+
+// Rows of the last R sources of [start, end): returns R and the row of s.
+inline int rows_for(int start, int end) { return std::min(end - start, sm_count()); }
+
+}  // namespace gu_shim
+
+class device_graph {
+public:
+    explicit device_graph(const host_graph &g) : n(g.n), m(g.m), directed(g.directed)
+    {
+        gu_shim::check(gu_graph_create(g.R.data(), g.m ? g.C.data() : nullptr, g.n, g.m, g.directed ? 1 : 0, nullptr,
+                                       &handle),
+                       "device_graph");
+    }
+    ~device_graph() { if (handle) gu_graph_destroy(handle); }
+    device_graph(const device_graph &) = delete;
+    device_graph &operator=(const device_graph &) = delete;
+
+    int n;
+    int m;
+    bool directed;
+    gu_graph handle = nullptr;
+};
+
+namespace gu_shim {
+
+// Searches every source of [start, end) with `variant` in chunks and keeps the
+// rows of the last R sources (row (s - start) % R).
+inline std::vector<std::vector<int> > search_rows(const device_graph &g, int variant, int start, int end)
+{
+    std::vector<std::vector<int> > out;
+    if (end <= start) return out;
+    const int R = rows_for(start, end);
+    out.assign((size_t)R, std::vector<int>((size_t)g.n));
+    const int total = end - start;
+    const int chunk = std::max(R, std::min(total, 4096));
+    dbuf<int32_t> src((size_t)chunk), dist((size_t)chunk * g.n);
+    std::vector<int32_t> hs((size_t)chunk);
+    for (int c0 = start; c0 < end; c0 += chunk) {
+        const int k = std::min(chunk, end - c0);
+        for (int i = 0; i < k; ++i) hs[i] = c0 + i;
+        cudaMemcpy(src.p, hs.data(), sizeof(int32_t) * k, cudaMemcpyHostToDevice);
+        check(gu_bfs(g.handle, variant, src.p, k, dist.p, g.n, nullptr), "multi_search");
+        for (int i = 0; i < k; ++i) {
+            const int s = c0 + i;
+            if (s < end - R) continue;
+            cudaMemcpy(out[(size_t)((s - start) % R)].data(), dist.p + (size_t)i * g.n, sizeof(int) * g.n,
+                       cudaMemcpyDeviceToHost);
+        }
+    }
+    return out;
+}
+
+inline std::vector<int32_t> iota_sources(int start, int end)
+{
+    std::vector<int32_t> s((size_t)(end > start ? end - start : 0));
+    for (int i = start; i < end; ++i) s[(size_t)(i - start)] = i;
+    return s;
+}
+
+}  // namespace gu_shim
+
+inline std::vector<std::vector<int> > multi_search_linear_atomics_setup(const device_graph &g, int start, int end)
+{
+    gu_shim::timer t;
+    auto r = gu_shim::search_rows(g, GU_BFS_LINEAR, start, end);
+    std::printf("Time for baseline linear algorithm with atomics: %.9f s\n", t.stop());
+    return r;
+}
+
+inline std::vector<std::vector<int> > multi_search_edge_parallel_setup(const device_graph &g, int start, int end)
+{
+    gu_shim::timer t;
+    auto r = gu_shim::search_rows(g, GU_BFS_EDGE, start, end);
+    std::printf("Time for baseline edge-parallel algorithm: %.9f s\n", t.stop());
+    return r;
+}
+
+inline std::vector<std::vector<int> > multi_search_warp_based_setup(const device_graph &g, int start, int end)
+{
+    gu_shim::timer t;
+    auto r = gu_shim::search_rows(g, GU_BFS_WARP, start, end);
+    std::printf("Time for warp-based neighbor gathering: %.9f s\n", t.stop());
+    return r;
+}
+
+inline std::vector<std::vector<int> > multi_search_CTA_warp_based_setup(const device_graph &g, int start, int end)
+{
+    gu_shim::timer t;
+    auto r = gu_shim::search_rows(g, GU_BFS_CTA_WARP, start, end);
+    std::printf("Time for CTA+warp-based neighbor gathering: %.9f s\n", t.stop());
+    return r;
+}
+
+inline std::vector<std::vector<int> > multi_search_scan_based_setup(const device_graph &g, int start, int end)
+{
+    gu_shim::timer t;
+    auto r = gu_shim::search_rows(g, GU_BFS_SCAN, start, end);
+    std::printf("Time for scan-based neighbor gathering: %.9f s\n", t.stop());
+    return r;
+}
+
+inline std::vector<std::vector<int> > multi_search_shuffle_based_setup(const device_graph &g, const program_options &,
+                                                                       int start, int end)
+{
+    gu_shim::timer t;
+    auto r = gu_shim::search_rows(g, GU_BFS_SHUFFLE, start, end);
+    std::printf("Time for shuffle-based neighbor gathering: %.9f s\n", t.stop());
+    return r;
+}
+
+inline void transitive_closure_setup(const device_graph &g, int start, int end, std::vector<std::vector<int> > &d)
+{
+    gu_shim::timer t;
+    d = gu_shim::search_rows(g, GU_BFS_AUTO, start, end);
+    std::printf("Time for shuffle-based transitive closure: %.9f s\n", t.stop());
+}
+
+inline int diameter_sampling_setup(const device_graph &g, int start, int end)
+{
+    gu_shim::timer t;
+    std::vector<int32_t> hs = gu_shim::iota_sources(start, end);
+    gu_shim::dbuf<int32_t> src(hs.size());
+    if (!hs.empty()) cudaMemcpy(src.p, hs.data(), sizeof(int32_t) * hs.size(), cudaMemcpyHostToDevice);
+    int32_t diam = 0;
+    gu_shim::check(gu_diameter(g.handle, src.p, (int32_t)hs.size(), &diam, nullptr), "diameter_sampling");
+    std::printf("Time for shuffle-based diameter sampling: %.9f s\n", t.stop());
+    return diam;
+}
+
+// Rows of the last R sources (sigma), all sources searched.
+inline void count_shortest_paths_setup(const device_graph &g, int start, int end,
+                                       std::vector<std::vector<unsigned long long> > &sigma_h)
+{
+    gu_shim::timer t;
+    sigma_h.clear();
+    if (end > start) {
+        const int R = gu_shim::rows_for(start, end);
+        std::vector<int32_t> hs = gu_shim::iota_sources(start, end);
+        gu_shim::dbuf<int32_t> src(hs.size());
+        cudaMemcpy(src.p, hs.data(), sizeof(int32_t) * hs.size(), cudaMemcpyHostToDevice);
+        gu_shim::dbuf<uint64_t> sig(hs.size() * (size_t)g.n);
+        gu_shim::check(gu_sigma(g.handle, src.p, (int32_t)hs.size(), nullptr, sig.p, g.n, nullptr), "count_shortest_paths");
+        sigma_h.assign((size_t)R, std::vector<unsigned long long>((size_t)g.n));
+        for (int s = end - R; s < end; ++s)
+            cudaMemcpy(sigma_h[(size_t)((s - start) % R)].data(), sig.p + (size_t)(s - start) * g.n,
+                       sizeof(uint64_t) * g.n, cudaMemcpyDeviceToHost);
+    }
+    std::printf("Time for shuffle-based shortest-path counting: %.9f s\n", t.stop());
+}
+
+// Brandes over all sources of [start, end); the float dependency rows of the
+// last R sources are returned (the reference keeps bc on the device only).
+inline void betweenness_centrality_setup(const device_graph &g, int start, int end,
+                                         std::vector<std::vector<float> > &delta_h)
+{
+    gu_shim::timer t;
+    delta_h.clear();
+    if (end > start) {
+        const int R = gu_shim::rows_for(start, end);
+        std::vector<int32_t> hs = gu_shim::iota_sources(start, end);
+        gu_shim::dbuf<int32_t> src(hs.size());
+        cudaMemcpy(src.p, hs.data(), sizeof(int32_t) * hs.size(), cudaMemcpyHostToDevice);
+        gu_shim::dbuf<double> bc((size_t)g.n), delta(hs.size() * (size_t)g.n);
+        gu_shim::check(gu_bc(g.handle, src.p, (int32_t)hs.size(), 0, bc.p, delta.p, g.n, nullptr), "betweenness_centrality");
+        delta_h.assign((size_t)R, std::vector<float>((size_t)g.n));
+        std::vector<double> row((size_t)g.n);
+        for (int s = end - R; s < end; ++s) {
+            cudaMemcpy(row.data(), delta.p + (size_t)(s - start) * g.n, sizeof(double) * g.n, cudaMemcpyDeviceToHost);
+            std::vector<float> &dst = delta_h[(size_t)((s - start) % R)];
+            for (int v = 0; v < g.n; ++v) dst[(size_t)v] = (float)row[(size_t)v];
+        }
+    }
+    std::printf("Time for shuffle-based BC: %.9f s\n", t.stop());
+}
+
+// LBS over device arrays; *edges (device) receives the total.
+inline void extract_edges_block(int vertex_frontier_size, int *edge_counts, int *scanned_edges, int *result, int *edges)
+{
+    int64_t total = 0;
+    gu_shim::check(gu_lbs(edge_counts, vertex_frontier_size, scanned_edges, result, INT32_MAX, edges, &total, nullptr),
+                   "extract_edges_block");
+}
+
+inline void extract_edges_warp(int vertex_frontier_size, int *edge_counts, int *scanned_edges, int *result, int *edges)
+{
+    extract_edges_block(vertex_frontier_size, edge_counts, scanned_edges, result, edges);
+}
