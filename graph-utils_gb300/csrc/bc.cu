@@ -71,7 +71,9 @@ struct BcArgs {
     double *delta;
     double *beta;  // (1 + delta) / sigma
     double *part;
-    double *bc;           // n, accumulated
+    double *bc;           // nreq x n, accumulated
+    const int32_t *req_start;  // nreq+1 source offsets of the requests (null: one request)
+    int32_t nreq;
     int32_t *dist_rows;   // optional k x ld
     u64 *sigma_rows;      // optional k x ld
     double *delta_rows;   // optional k x ld
@@ -252,23 +254,51 @@ __device__ void bc_combine_item(const BcArgs &a, int l, int q, int i)
     if ((lm >> (lane + 32)) & 1ull) finish_delta(a, o + lane + 32, s1);
 }
 
-// bc[w] += sum of delta over the batch's sources whose level of w is >= 1, as a
-// fixed-shape tree: each lane sums its own sources word by word, then a
-// butterfly over the 32 lanes.
-__device__ void bc_accumulate_item(const BcArgs &a, int32_t w, int nb)
+// bc_r[w] += sum of delta over the batch's sources of request r whose level of
+// w is >= 1, as a fixed-shape tree: each lane sums its own sources word by
+// word, then a butterfly over the 32 lanes.  Requests own contiguous source
+// ranges (one request when req_start is null).
+__device__ __forceinline__ u64 range_bits(int q, int lo, int hi)
+{
+    // bits p of word q with lo <= 64q + p < hi
+    const int a = max(lo - 64 * q, 0), b = min(hi - 64 * q, 64);
+    if (b <= a) return 0ull;
+    const u64 upto = b >= 64 ? ~0ull : ((1ull << b) - 1ull);
+    return upto & ~((1ull << a) - 1ull);
+}
+
+__device__ void bc_accumulate_item(const BcArgs &a, int32_t w, int row0, int nb)
 {
     const int lane = lane_id();
     const int B = 64 * a.W;
-    double s = 0.0;
-    for (int q = 0; q < a.W && 64 * q < nb; ++q) {
-        const u64 counted = __ldcg(a.seen + (size_t)w * a.W + q) & ~__ldcg(a.lvl + (size_t)w * a.W + q);
-        const double *dw = a.delta + (size_t)w * B + 64 * q;
-        if ((counted >> lane) & 1ull) s += __ldcg(dw + lane);
-        if ((counted >> (lane + 32)) & 1ull) s += __ldcg(dw + lane + 32);
+    int r = 0;
+    if (a.req_start) {  // first request ending after row0
+        int lo = 0, hi = a.nreq - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (__ldg(a.req_start + mid + 1) > row0) hi = mid;
+            else lo = mid + 1;
+        }
+        r = lo;
     }
+    for (; r < a.nreq; ++r) {
+        const int rs = a.req_start ? __ldg(a.req_start + r) : 0;
+        const int re = a.req_start ? __ldg(a.req_start + r + 1) : a.k;
+        if (rs >= row0 + nb) break;
+        const int lo = max(rs, row0) - row0, hi = min(re, row0 + nb) - row0;
+        if (hi <= lo) continue;
+        double s = 0.0;
+        for (int q = 0; q < a.W && 64 * q < nb; ++q) {
+            const u64 counted = __ldcg(a.seen + (size_t)w * a.W + q) & ~__ldcg(a.lvl + (size_t)w * a.W + q) &
+                                range_bits(q, lo, hi);
+            const double *dw = a.delta + (size_t)w * B + 64 * q;
+            if ((counted >> lane) & 1ull) s += __ldcg(dw + lane);
+            if ((counted >> (lane + 32)) & 1ull) s += __ldcg(dw + lane + 32);
+        }
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(FULL_MASK, s, o);
-    if (lane == 0) a.bc[w] += s;
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(FULL_MASK, s, o);
+        if (lane == 0) a.bc[(size_t)r * a.n + w] += s;
+    }
 }
 
 // Optional per-source rows (dist, sigma, delta) of this batch: lane l writes
@@ -312,7 +342,7 @@ __global__ void __launch_bounds__(BC_THREADS, 2) bc_grid_kernel(BcArgs a, int do
     const int W = a.W, B = 64 * W;
     const size_t nW = (size_t)a.n * W;
     const int nbatch = (a.k + B - 1) / B;
-    for (long long i = rank; i < a.n; i += size) a.bc[i] = 0.0;
+    for (long long i = rank; i < (long long)a.nreq * a.n; i += size) a.bc[i] = 0.0;
     if (threadIdx.x < 16) s_act[threadIdx.x] = 0;
     for (int b = 0; b < nbatch; ++b) {
         const int row0 = b * B;
@@ -383,7 +413,7 @@ __global__ void __launch_bounds__(BC_THREADS, 2) bc_grid_kernel(BcArgs a, int do
                     if (!grid_barrier(&ctl->bar, &ctl->err, epoch)) return;
                 }
             }
-            for (long long w = gwarp(); w < a.n; w += nwarps()) bc_accumulate_item(a, (int32_t)w, nb);
+            for (long long w = gwarp(); w < a.n; w += nwarps()) bc_accumulate_item(a, (int32_t)w, row0, nb);
         }
         if (a.dist_rows || a.sigma_rows || a.delta_rows) {
             for (int q = 0; q < W; ++q)
@@ -471,27 +501,51 @@ static DevChunks dev_chunks(const ChunkMap &c)
     return d;
 }
 
-void launch_bc(DeviceGraph &g, const int32_t *sources, int32_t k, int batch, double *bc, int32_t *dist_rows,
-               uint64_t *sigma_rows, double *delta_rows, int64_t ld, bool backward, cudaStream_t stream)
+struct BcLayout {
+    int W;
+    size_t words, sig, del, prt, bcb, maxl, total;
+};
+
+// Level store: levels 0..maxl-1 (a BFS level is at most n - 1); 512 MiB of
+// level bitmaps by default, at least 64 levels (GU_BC_LEVEL_BUDGET_MB overrides).
+static BcLayout bc_layout(const DeviceGraph &g, int32_t k, int batch, bool backward, int nslots)
 {
     if (batch > 0 && batch % 64) throw gu_error(GU_ERR_INVALID_ARGUMENT, "batch must be a multiple of 64");
-    const int W = bc_words_for(k, batch > 0 ? batch / 64 : 0);
-    ensure_chunks(g);
-    const size_t n = (size_t)g.n, B = 64 * (size_t)W;
+    BcLayout L;
+    L.W = bc_words_for(k, batch > 0 ? batch / 64 : 0);
+    const size_t n = (size_t)g.n, B = 64 * (size_t)L.W;
     auto up = [](size_t x) { return ((x + 255) / 256) * 256; };
-    const size_t words = up(n * W * sizeof(u64));
-    const size_t sig = up(n * B * sizeof(u64));
-    const size_t del = backward ? 2 * up(n * B * sizeof(double)) : 0;  // delta and beta
-    const size_t prt = backward ? up((size_t)g.bc_out.nslots * W * 64 * sizeof(double)) : 0;
-    const size_t bcb = up(n * sizeof(double));
-    // level store: as many levels as fit a budget (a BFS level is at most n - 1)
-    size_t budget = (size_t)8 << 30;
+    L.words = up(n * L.W * sizeof(u64));
+    L.sig = up(n * B * sizeof(u64));
+    L.del = backward ? 2 * up(n * B * sizeof(double)) : 0;  // delta and beta
+    L.prt = backward ? up((size_t)nslots * L.W * 64 * sizeof(double)) : 0;
+    L.bcb = up(n * sizeof(double));
+    size_t budget = (size_t)512 << 20;
     if (const char *s = std::getenv("GU_BC_LEVEL_BUDGET_MB")) budget = (size_t)std::atoll(s) << 20;
-    size_t maxl = budget / (words ? words : 1);
-    if (maxl < 2) maxl = 2;
-    if (maxl > n + 1) maxl = n + 1;
-    const size_t need = WS_CONTROL_BYTES + words + maxl * words + sig + del + prt + bcb;
-    char *ws = (char *)g.ws.get(need);
+    L.maxl = budget / (L.words ? L.words : 1);
+    if (L.maxl < 64) L.maxl = 64;
+    if (L.maxl > n + 1) L.maxl = n + 1;
+    if (L.maxl < 2) L.maxl = 2;
+    L.total = WS_CONTROL_BYTES + L.words + L.maxl * L.words + L.sig + L.del + L.prt + L.bcb;
+    return L;
+}
+
+size_t bc_workspace_bytes(const DeviceGraph &g, int32_t k, int batch, bool backward)
+{
+    // the split-vertex slot count is known once the work items exist; bound it by m / 256 + n
+    const int nslots = g.bc_out.built ? g.bc_out.nslots : (int)(g.m / BC_CHUNK_EDGES + g.n);
+    return bc_layout(g, k, batch, backward, nslots).total;
+}
+
+void launch_bc(DeviceGraph &g, const int32_t *sources, int32_t k, const BcOptions &opt, double *bc, int32_t *dist_rows,
+               uint64_t *sigma_rows, double *delta_rows, int64_t ld, bool backward, cudaStream_t stream)
+{
+    ensure_chunks(g);
+    const BcLayout Lay = bc_layout(g, k, opt.batch, backward, g.bc_out.nslots);
+    const int W = Lay.W;
+    const size_t words = Lay.words, sig = Lay.sig, del = Lay.del, prt = Lay.prt, maxl = Lay.maxl;
+    Workspace &wsp = opt.ws ? *opt.ws : g.ws;
+    char *ws = (char *)wsp.get(Lay.total);
     BcArgs a;
     a.R = g.R;
     a.C = g.C;
@@ -519,6 +573,9 @@ void launch_bc(DeviceGraph &g, const int32_t *sources, int32_t k, int batch, dou
     a.part = backward ? reinterpret_cast<double *>(p) : nullptr;
     p += prt;
     a.bc = bc ? bc : reinterpret_cast<double *>(p);
+    a.req_start = opt.req_start;
+    a.nreq = opt.req_start ? opt.nreq : 1;
+    if (!bc && a.nreq != 1) throw gu_error(GU_ERR_INTERNAL, "per-request bc needs an output");
     a.dist_rows = dist_rows;
     a.sigma_rows = reinterpret_cast<u64 *>(sigma_rows);
     a.delta_rows = delta_rows;
@@ -529,12 +586,21 @@ void launch_bc(DeviceGraph &g, const int32_t *sources, int32_t k, int batch, dou
         GU_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, bc_grid_kernel, BC_THREADS, 0));
         if (blocks_per_sm < 1) throw gu_error(GU_ERR_INTERNAL, "bc kernel cannot be resident");
     }
-    dim3 grid(g.sm_count * blocks_per_sm), block(BC_THREADS);
+    int nblocks = g.sm_count * blocks_per_sm;
+    if (opt.max_blocks > 0 && nblocks > opt.max_blocks) nblocks = opt.max_blocks;
+    dim3 grid(nblocks), block(BC_THREADS);
     int do_backward = backward ? 1 : 0;
     void *params[] = {&a, &do_backward};
-    g.mark_start(stream);
+    if (opt.timed) g.mark_start(stream);
     GU_CUDA_CHECK(cudaLaunchCooperativeKernel((const void *)bc_grid_kernel, grid, block, params, 0, stream));
-    g.mark_stop(stream);
+    if (opt.timed) g.mark_stop(stream);
+}
+
+int bc_ws_error(const Workspace &ws)
+{
+    BcCtl c;
+    GU_CUDA_CHECK(cudaMemcpy(&c, ws.ptr, sizeof(BcCtl), cudaMemcpyDeviceToHost));
+    return c.err;
 }
 
 void bc_read_status(DeviceGraph &g, int *dev_err, int *max_level)

@@ -95,6 +95,7 @@ const char *gu_status_string(gu_status s)
     case GU_ERR_TIMEOUT: return "device wait timed out";
     case GU_ERR_UNSUPPORTED: return "unsupported";
     case GU_ERR_INTERNAL: return "internal error";
+    case GU_ERR_PENDING: return "request pending";
     }
     return "unknown status";
 }
@@ -423,7 +424,8 @@ gu_status gu_sigma(gu_graph g, const int32_t *sources_dev, int32_t k, int32_t *d
         cudaStream_t st = (cudaStream_t)stream;
         check_sources_device(dg, sources_dev, k, st);
         if (k == 0) return;
-        launch_bc(dg, sources_dev, k, 0, nullptr, dist_dev, sigma_dev, nullptr, ld, false, st);
+        BcOptions opt;
+        launch_bc(dg, sources_dev, k, opt, nullptr, dist_dev, sigma_dev, nullptr, ld, false, st);
         finish_bc(dg, st);
     });
 }
@@ -445,7 +447,9 @@ gu_status gu_bc(gu_graph g, const int32_t *sources_dev, int32_t k, int32_t batch
             GU_CUDA_CHECK(cudaStreamSynchronize(st));
             return;
         }
-        launch_bc(dg, sources_dev, k, batch, bc_dev, nullptr, nullptr, delta_dev, ld, true, st);
+        BcOptions opt;
+        opt.batch = batch;
+        launch_bc(dg, sources_dev, k, opt, bc_dev, nullptr, nullptr, delta_dev, ld, true, st);
         finish_bc(dg, st);
     });
 }
@@ -483,6 +487,66 @@ gu_status gu_race_and_resolve(const int32_t *predicates_dev, int32_t nwarps, int
         if (nwarps < 0) throw gu_error(GU_ERR_INVALID_ARGUMENT, "nwarps must be >= 0");
         if (nwarps > 0 && (!predicates_dev || !winners_dev)) throw gu_error(GU_ERR_INVALID_ARGUMENT, "null buffer");
         launch_race_and_resolve(predicates_dev, nwarps, winners_dev, (cudaStream_t)stream);
+    });
+}
+
+// ---- serving -----------------------------------------------------------------------
+struct gu_server_s {
+    Server *s = nullptr;
+};
+
+gu_status gu_server_create(size_t hbm_budget_bytes, int slots, int max_batch_sources, gu_server *out)
+{
+    return guarded([&] {
+        if (!out || slots < 1 || max_batch_sources < 1 || hbm_budget_bytes == 0)
+            throw gu_error(GU_ERR_INVALID_ARGUMENT, "bad server parameters");
+        std::unique_ptr<gu_server_s> h(new gu_server_s());
+        h->s = server_create(hbm_budget_bytes, slots, max_batch_sources);
+        *out = h.release();
+    });
+}
+
+gu_status gu_server_destroy(gu_server s)
+{
+    return guarded([&] {
+        if (!s) return;
+        server_destroy(s->s);
+        delete s;
+    });
+}
+
+gu_status gu_server_submit(gu_server s, gu_graph g, int query, const int32_t *sources_host, int32_t k, void *out_host,
+                           int64_t *request_id)
+{
+    return guarded([&] {
+        if (!s || !g || !request_id) throw gu_error(GU_ERR_INVALID_ARGUMENT, "null argument");
+        *request_id = server_submit(s->s, query, g->g.get(), sources_host, k, out_host);
+    });
+}
+
+gu_status gu_server_wait(gu_server s, int64_t request_id, double timeout_s, double *latency_s)
+{
+    try {
+        if (!s) throw gu_error(GU_ERR_INVALID_ARGUMENT, "null server");
+        std::string err;
+        const gu_status st = server_wait(s->s, request_id, timeout_s, latency_s, err);
+        if (st != GU_OK) set_last_error(st == GU_ERR_PENDING ? "request still running" : err);
+        return st;
+    } catch (const gu_error &e) {
+        set_last_error(e.what());
+        return e.code;
+    } catch (const std::exception &e) {
+        set_last_error(e.what());
+        return GU_ERR_INTERNAL;
+    }
+}
+
+gu_status gu_server_stats(gu_server s, int64_t *completed, int64_t *batches, double *p50_s, double *p99_s,
+                          double *mean_requests_per_batch)
+{
+    return guarded([&] {
+        if (!s) throw gu_error(GU_ERR_INVALID_ARGUMENT, "null server");
+        server_stats(s->s, completed, batches, p50_s, p99_s, mean_requests_per_batch);
     });
 }
 

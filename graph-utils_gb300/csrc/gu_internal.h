@@ -139,6 +139,19 @@ struct MsOptions {
     int batch_words = 1;  // 64-source words per batch
     float alpha = 2.f;    // top-down -> bottom-up when frontier out-edges > m / alpha
     float beta = 24.f;    // bottom-up -> top-down when frontier vertices < n / beta
+    Workspace *ws = nullptr;  // scratch to use (default: the graph's)
+    int max_blocks = 0;       // cap on the persistent grid (0: the whole GPU)
+    bool timed = true;        // record the graph's launch events
+};
+
+// Per-call options of the batched sigma / Brandes engine.
+struct BcOptions {
+    int batch = 0;                      // sources per pass (0: default)
+    Workspace *ws = nullptr;            // scratch to use (default: the graph's)
+    int max_blocks = 0;                 // cap on the persistent grid
+    bool timed = true;
+    const int32_t *req_start = nullptr; // device, nreq+1 source offsets of the requests (null: one request)
+    int32_t nreq = 1;                   // bc receives nreq x n values
 };
 
 // Kernel launchers (device pointers, stream ordered; return after enqueue).
@@ -147,13 +160,22 @@ void launch_msbfs(DeviceGraph &g, const int32_t *sources, int32_t k, int32_t *di
 void launch_plain_bfs(DeviceGraph &g, const int32_t *sources, int32_t k, int32_t *dist, int64_t ld,
                       cudaStream_t stream);
 // Batched sigma / Brandes: bc (n doubles, may be null), optional rows (k x ld).
-void launch_bc(DeviceGraph &g, const int32_t *sources, int32_t k, int batch, double *bc, int32_t *dist_rows,
+void launch_bc(DeviceGraph &g, const int32_t *sources, int32_t k, const BcOptions &opt, double *bc, int32_t *dist_rows,
                uint64_t *sigma_rows, double *delta_rows, int64_t ld, bool backward, cudaStream_t stream);
+size_t bc_workspace_bytes(const DeviceGraph &g, int32_t k, int batch, bool backward);
+size_t msbfs_workspace_bytes(const DeviceGraph &g, int32_t k);
 void bc_read_status(DeviceGraph &g, int *dev_err, int *max_level);
 size_t lbs_scratch_bytes(int32_t N);
 void launch_lbs(const int32_t *counts, int32_t N, int32_t *scanned, int32_t *result, int64_t result_capacity,
                 int32_t *total_dev, int64_t *total_host, void *scratch_ptr, size_t scratch_bytes, cudaStream_t st);
 void launch_race_and_resolve(const int32_t *pred, int32_t nwarps, int32_t *winner, cudaStream_t st);
+
+class Server;
+Server *server_create(size_t budget, int nslots, int max_batch);
+void server_destroy(Server *s);
+int64_t server_submit(Server *s, int kind, DeviceGraph *g, const int32_t *src, int32_t k, void *out);
+gu_status server_wait(Server *s, int64_t id, double timeout, double *latency, std::string &err);
+void server_stats(Server *s, int64_t *completed, int64_t *batches, double *p50, double *p99, double *mean_batch);
 void msbfs_read_status(DeviceGraph &g, int *dev_err, int *td_levels, int *bu_levels, int *max_level);
 void ensure_coo(DeviceGraph &g, cudaStream_t stream);
 int device_sm_count(int device);

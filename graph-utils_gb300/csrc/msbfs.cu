@@ -951,25 +951,27 @@ __global__ void __launch_bounds__(MS_THREADS, MS_MIN_BLOCKS) ms_grid_kernel(MsAr
 
 // ---- host side ---------------------------------------------------------------------
 template <int V, int W>
-static void launch_one(const MsArgs &a, int sms, cudaStream_t stream)
+static void launch_one(const MsArgs &a, int sms, cudaStream_t stream, int max_blocks = 0)
 {
     static int blocks_per_sm = -1;
     if (blocks_per_sm < 0) {
         GU_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, ms_grid_kernel<V, W>, MS_THREADS, 0));
         if (blocks_per_sm < 1) throw gu_error(GU_ERR_INTERNAL, "msbfs kernel cannot be resident");
     }
-    dim3 grid(sms * blocks_per_sm), block(MS_THREADS);
+    int nblocks = sms * blocks_per_sm;
+    if (max_blocks > 0 && nblocks > max_blocks) nblocks = max_blocks;
+    dim3 grid(nblocks), block(MS_THREADS);
     MsArgs args = a;
     void *params[] = {&args};
     GU_CUDA_CHECK(cudaLaunchCooperativeKernel((const void *)ms_grid_kernel<V, W>, grid, block, params, 0, stream));
 }
 
 template <int V>
-static void launch_words(const MsArgs &a, int W, int sms, cudaStream_t stream)
+static void launch_words(const MsArgs &a, int W, int sms, cudaStream_t stream, int max_blocks)
 {
-    if (W == 1) launch_one<V, 1>(a, sms, stream);
-    else if (W == 2) launch_one<V, 2>(a, sms, stream);
-    else launch_one<V, 4>(a, sms, stream);
+    if (W == 1) launch_one<V, 1>(a, sms, stream, max_blocks);
+    else if (W == 2) launch_one<V, 2>(a, sms, stream, max_blocks);
+    else launch_one<V, 4>(a, sms, stream, max_blocks);
 }
 
 static float env_float(const char *name, float dflt)
@@ -991,6 +993,22 @@ int msbfs_words_for(int32_t k)
     return 4;
 }
 
+static int msbfs_planes(size_t n)
+{
+    // every BFS level is at most n - 1: bit-length of n - 1 planes suffice
+    int nplanes = 1;
+    while (nplanes < MAX_PLANES && ((int64_t)(n > 0 ? n - 1 : 0) >> nplanes) != 0) ++nplanes;
+    return nplanes;
+}
+
+size_t msbfs_workspace_bytes(const DeviceGraph &g, int32_t k)
+{
+    const int W = msbfs_words_for(k);
+    const size_t n = (size_t)g.n;
+    auto up = [](size_t b) { return ((b + 255) / 256) * 256; };
+    return WS_CONTROL_BYTES + (4 + (size_t)msbfs_planes(n)) * up(n * W * sizeof(u64)) + 7 * up(n * sizeof(int32_t));
+}
+
 void launch_msbfs(DeviceGraph &g, const int32_t *sources, int32_t k, int32_t *dist, int64_t ld,
                   const MsOptions &opt, cudaStream_t stream, int *dev_err_out)
 {
@@ -998,15 +1016,14 @@ void launch_msbfs(DeviceGraph &g, const int32_t *sources, int32_t k, int32_t *di
     if (opt.variant == GU_BFS_EDGE) ensure_coo(g, stream);
     const int W = msbfs_words_for(k);
     const size_t n = (size_t)g.n;
-    // every BFS level is at most n - 1: bit-length of n - 1 planes suffice
-    int nplanes = 1;
-    while (nplanes < MAX_PLANES && ((int64_t)(n > 0 ? n - 1 : 0) >> nplanes) != 0) ++nplanes;
+    const int nplanes = msbfs_planes(n);
     auto up = [](size_t b) { return ((b + 255) / 256) * 256; };
     const size_t words_bytes = up(n * W * sizeof(u64));
     const size_t i32_bytes = up(n * sizeof(int32_t));
     static_assert(CTL_REGION <= WS_CONTROL_BYTES, "timeline must fit the control region");
     const size_t ctl_bytes = WS_CONTROL_BYTES;
-    char *ws = (char *)g.ws.get(ctl_bytes + (4 + (size_t)nplanes) * words_bytes + 7 * i32_bytes);
+    Workspace &wsp = opt.ws ? *opt.ws : g.ws;
+    char *ws = (char *)wsp.get(msbfs_workspace_bytes(g, k));
     MsArgs a;
     a.R = g.R;
     a.C = g.C;
@@ -1050,19 +1067,28 @@ void launch_msbfs(DeviceGraph &g, const int32_t *sources, int32_t k, int32_t *di
     a.degbits = degbits;
     GU_CUDA_CHECK(cudaMemsetAsync(a.ctl, 0, CTL_REGION, stream));
     const int sms = g.sm_count;
-    g.mark_start(stream);
+    const int mb = opt.max_blocks;
+    if (opt.timed) g.mark_start(stream);
     switch (opt.variant) {
-    case GU_BFS_AUTO: launch_words<GU_BFS_AUTO>(a, W, sms, stream); break;
-    case GU_BFS_LINEAR: launch_words<GU_BFS_LINEAR>(a, W, sms, stream); break;
-    case GU_BFS_EDGE: launch_words<GU_BFS_EDGE>(a, W, sms, stream); break;
-    case GU_BFS_WARP: launch_words<GU_BFS_WARP>(a, W, sms, stream); break;
-    case GU_BFS_CTA_WARP: launch_words<GU_BFS_CTA_WARP>(a, W, sms, stream); break;
-    case GU_BFS_SCAN: launch_words<GU_BFS_SCAN>(a, W, sms, stream); break;
-    case GU_BFS_SHUFFLE: launch_words<GU_BFS_SHUFFLE>(a, W, sms, stream); break;
-    case GU_BFS_BOTTOM_UP: launch_words<GU_BFS_BOTTOM_UP>(a, W, sms, stream); break;
+    case GU_BFS_AUTO: launch_words<GU_BFS_AUTO>(a, W, sms, stream, mb); break;
+    case GU_BFS_LINEAR: launch_words<GU_BFS_LINEAR>(a, W, sms, stream, mb); break;
+    case GU_BFS_EDGE: launch_words<GU_BFS_EDGE>(a, W, sms, stream, mb); break;
+    case GU_BFS_WARP: launch_words<GU_BFS_WARP>(a, W, sms, stream, mb); break;
+    case GU_BFS_CTA_WARP: launch_words<GU_BFS_CTA_WARP>(a, W, sms, stream, mb); break;
+    case GU_BFS_SCAN: launch_words<GU_BFS_SCAN>(a, W, sms, stream, mb); break;
+    case GU_BFS_SHUFFLE: launch_words<GU_BFS_SHUFFLE>(a, W, sms, stream, mb); break;
+    case GU_BFS_BOTTOM_UP: launch_words<GU_BFS_BOTTOM_UP>(a, W, sms, stream, mb); break;
     default: throw gu_error(GU_ERR_INVALID_ARGUMENT, "unknown BFS variant");
     }
-    g.mark_stop(stream);
+    if (opt.timed) g.mark_stop(stream);
+}
+
+// Device error word of a launch that used workspace `ws` (after its stream is synchronised).
+int msbfs_ws_error(const Workspace &ws)
+{
+    MsCtl c;
+    GU_CUDA_CHECK(cudaMemcpy(&c, ws.ptr, sizeof(MsCtl), cudaMemcpyDeviceToHost));
+    return c.err;
 }
 
 // Reads the control block of the last launch (after the stream is synchronised).

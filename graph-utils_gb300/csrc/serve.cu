@@ -1,0 +1,428 @@
+// serve.cu -- continuous-batching query server over device-resident graphs.
+//
+// Requests (BFS rows, BC over a source set, reachable-vertex counts) arrive from
+// any host thread.  A worker thread keeps a FIFO of pending requests and a fixed
+// set of slots (stream, workspace, pinned staging).  Whenever a slot is free it
+// forms a batch from the oldest pending request and every later pending request
+// of the same graph and kind (up to max_batch sources; a larger request runs
+// alone), admits it if the batch's device footprint (engine workspace + rows)
+// fits the HBM budget next to the batches already running, and launches it on
+// the slot's stream with a persistent grid of 1/slots of the GPU, so batches of
+// different slots overlap on the device.  Requests that arrive while batches
+// run are admitted as slots and memory free up.  Per-request state lives on the
+// device for the batch's lifetime: BFS requests own contiguous row ranges, BC
+// requests own contiguous source ranges with their own bc vector
+// (BcOptions::req_start), reachability requests own contiguous count ranges.
+// A request's result does not depend on its batch-mates: BFS rows and counts
+// are exact; BC sums its sources in batch order, within 1e-12 of running alone.
+#include "device_utils.cuh"
+#include "gu_internal.h"
+
+#include <algorithm>
+#include <chrono>
+#include <climits>
+#include <cmath>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <memory>
+#include <thread>
+#include <unordered_map>
+
+namespace gu {
+
+int msbfs_ws_error(const Workspace &ws);
+int bc_ws_error(const Workspace &ws);
+
+using Clock = std::chrono::steady_clock;
+
+__global__ void count_reached_kernel(const int32_t *__restrict__ dist, int32_t n, int32_t k, long long *__restrict__ counts)
+{
+    __shared__ long long s_warp[32];
+    for (int r = blockIdx.x; r < k; r += gridDim.x) {
+        long long c = 0;
+        for (int32_t v = threadIdx.x; v < n; v += blockDim.x) c += dist[(int64_t)r * n + v] != INT_MAX;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(FULL_MASK, c, o);
+        if (lane_id() == 0) s_warp[warp_in_block()] = c;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            long long t = 0;
+            for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += s_warp[w];
+            counts[r] = t;
+        }
+        __syncthreads();
+    }
+}
+
+struct SRequest {
+    int64_t id = 0;
+    int kind = 0;
+    DeviceGraph *g = nullptr;
+    std::vector<int32_t> src;
+    void *out = nullptr;
+    Clock::time_point t_submit, t_done;
+    gu_status status = GU_OK;
+    std::string err;
+    bool done = false;
+};
+
+struct PinnedBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+    void *get(size_t need)
+    {
+        if (need <= bytes && p) return p;
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        bytes = 0;
+        GU_CUDA_CHECK(cudaHostAlloc(&p, need, cudaHostAllocDefault));
+        bytes = need;
+        return p;
+    }
+    ~PinnedBuf()
+    {
+        if (p) cudaFreeHost(p);
+    }
+};
+
+struct Slot {
+    cudaStream_t st = nullptr;
+    cudaEvent_t ev = nullptr;
+    Workspace ws, io;
+    PinnedBuf stage;
+    bool busy = false;
+    int kind = 0;
+    DeviceGraph *g = nullptr;
+    std::vector<SRequest *> reqs;
+    size_t need = 0;
+    size_t out_off = 0;  // byte offset of the outputs in stage
+};
+
+class Server {
+public:
+    Server(size_t budget, int nslots, int max_batch) : budget_(budget), max_batch_(max_batch)
+    {
+        GU_CUDA_CHECK(cudaGetDevice(&device_));
+        const int sms = device_sm_count(device_);
+        nslots = std::max(1, std::min(nslots, 32));
+        blocks_per_slot_ = std::max(1, 2 * sms / nslots);
+        slots_.resize((size_t)nslots);
+        for (Slot &s : slots_) {
+            GU_CUDA_CHECK(cudaStreamCreateWithFlags(&s.st, cudaStreamNonBlocking));
+            GU_CUDA_CHECK(cudaEventCreateWithFlags(&s.ev, cudaEventDisableTiming));
+        }
+        worker_ = std::thread([this] { loop(); });
+    }
+
+    ~Server()
+    {
+        {
+            std::lock_guard<std::mutex> lk(mu_);
+            stop_ = true;
+        }
+        cv_work_.notify_all();
+        if (worker_.joinable()) worker_.join();
+        cudaSetDevice(device_);
+        for (Slot &s : slots_) {
+            if (s.st) cudaStreamSynchronize(s.st);
+            s.ws.release();
+            s.io.release();
+            if (s.ev) cudaEventDestroy(s.ev);
+            if (s.st) cudaStreamDestroy(s.st);
+        }
+    }
+
+    int64_t submit(int kind, DeviceGraph *g, const int32_t *src, int32_t k, void *out)
+    {
+        if (kind < GU_QUERY_BFS || kind > GU_QUERY_REACH) throw gu_error(GU_ERR_INVALID_ARGUMENT, "unknown query kind");
+        if (!g || k <= 0 || !src || !out) throw gu_error(GU_ERR_INVALID_ARGUMENT, "bad request");
+        if (g->device != device_) throw gu_error(GU_ERR_INVALID_ARGUMENT, "graph lives on another device");
+        for (int32_t i = 0; i < k; ++i)
+            if (src[i] < 0 || src[i] >= g->n) throw gu_error(GU_ERR_INVALID_ARGUMENT, "source vertex out of range");
+        std::unique_ptr<SRequest> r(new SRequest());
+        r->kind = kind;
+        r->g = g;
+        r->src.assign(src, src + k);
+        r->out = out;
+        r->t_submit = Clock::now();
+        int64_t id;
+        {
+            std::lock_guard<std::mutex> lk(mu_);
+            id = r->id = ++next_id_;
+            pending_.push_back(r.get());
+            all_[id] = std::move(r);
+        }
+        cv_work_.notify_all();
+        return id;
+    }
+
+    gu_status wait(int64_t id, double timeout_s, double *latency, std::string &err)
+    {
+        std::unique_lock<std::mutex> lk(mu_);
+        auto it = all_.find(id);
+        if (it == all_.end()) throw gu_error(GU_ERR_INVALID_ARGUMENT, "unknown request id");
+        SRequest *r = it->second.get();
+        const auto pred = [&] { return r->done; };
+        if (timeout_s < 0) cv_done_.wait(lk, pred);
+        else if (!cv_done_.wait_for(lk, std::chrono::duration<double>(timeout_s), pred)) return GU_ERR_PENDING;
+        if (latency) *latency = std::chrono::duration<double>(r->t_done - r->t_submit).count();
+        const gu_status st = r->status;
+        err = r->err;
+        all_.erase(it);
+        return st;
+    }
+
+    void stats(int64_t *completed, int64_t *batches, double *p50, double *p99, double *mean_batch)
+    {
+        std::lock_guard<std::mutex> lk(mu_);
+        if (completed) *completed = completed_;
+        if (batches) *batches = batches_;
+        std::vector<double> l = latencies_;
+        std::sort(l.begin(), l.end());
+        auto pct = [&](double p) {
+            if (l.empty()) return 0.0;
+            size_t i = (size_t)std::ceil(p * (double)l.size()) - 1;
+            return l[std::min(i, l.size() - 1)];
+        };
+        if (p50) *p50 = pct(0.50);
+        if (p99) *p99 = pct(0.99);
+        if (mean_batch) *mean_batch = batches_ ? (double)batched_reqs_ / (double)batches_ : 0.0;
+    }
+
+private:
+    size_t row_bytes(const SRequest *r) const
+    {
+        if (r->kind == GU_QUERY_BFS) return r->src.size() * (size_t)r->g->n * sizeof(int32_t);
+        if (r->kind == GU_QUERY_BC) return (size_t)r->g->n * sizeof(double);
+        return r->src.size() * sizeof(long long);
+    }
+
+    size_t batch_need(int kind, const DeviceGraph &g, int32_t k, int nreq, size_t out_bytes) const
+    {
+        size_t ws = kind == GU_QUERY_BC ? bc_workspace_bytes(g, k, 0, true) : msbfs_workspace_bytes(g, k);
+        size_t io = (size_t)k * 4 + (size_t)(nreq + 1) * 4 + 1024 + out_bytes;
+        if (kind == GU_QUERY_REACH) io += (size_t)k * (size_t)g.n * sizeof(int32_t);  // rows before counting
+        return ws + io;
+    }
+
+    size_t held_except(const Slot *self) const
+    {
+        size_t h = 0;
+        for (const Slot &s : slots_)
+            if (&s != self) h += s.ws.bytes + s.io.bytes;
+        return h;
+    }
+
+    void finish(SRequest *r, gu_status st, const std::string &err)
+    {
+        r->status = st;
+        r->err = err;
+        r->t_done = Clock::now();
+        r->done = true;
+        ++completed_;
+        latencies_.push_back(std::chrono::duration<double>(r->t_done - r->t_submit).count());
+    }
+
+    // Forms and launches a batch on slot s (mu_ held).  Returns true if launched.
+    bool try_launch(Slot &s)
+    {
+        if (pending_.empty()) return false;
+        SRequest *head = pending_.front();
+        std::vector<SRequest *> batch{head};
+        int32_t k = (int32_t)head->src.size();
+        size_t out_bytes = row_bytes(head);
+        for (size_t i = 1; i < pending_.size() && k < max_batch_; ++i) {
+            SRequest *r = pending_[i];
+            if (r->g != head->g || r->kind != head->kind) continue;
+            if (k + (int64_t)r->src.size() > max_batch_) continue;
+            batch.push_back(r);
+            k += (int32_t)r->src.size();
+            out_bytes += row_bytes(r);
+        }
+        DeviceGraph &g = *head->g;
+        const size_t need = batch_need(head->kind, g, k, (int)batch.size(), out_bytes);
+        if (held_except(&s) + std::max(need, s.ws.bytes + s.io.bytes) > budget_) {
+            for (Slot &o : slots_)  // give back memory idle slots hold
+                if (!o.busy && &o != &s) {
+                    o.ws.release();
+                    o.io.release();
+                }
+            s.ws.release();
+            s.io.release();
+            if (held_except(&s) + need > budget_) {
+                bool any_busy = false;
+                for (Slot &o : slots_) any_busy |= o.busy;
+                if (any_busy) return false;  // wait for memory
+                for (SRequest *r : batch) {  // can never fit
+                    pending_.erase(std::find(pending_.begin(), pending_.end(), r));
+                    finish(r, GU_ERR_CAPACITY, "request needs " + std::to_string(need) + " bytes of HBM, budget is " +
+                                                   std::to_string(budget_));
+                }
+                cv_done_.notify_all();
+                return false;
+            }
+        }
+        for (SRequest *r : batch) pending_.erase(std::find(pending_.begin(), pending_.end(), r));
+        try {
+            launch(s, head->kind, g, batch, k, out_bytes);
+        } catch (const gu_error &e) {
+            for (SRequest *r : batch) finish(r, e.code, e.what());
+            cv_done_.notify_all();
+            s.busy = false;
+            return false;
+        }
+        s.need = need;
+        ++batches_;
+        batched_reqs_ += (int64_t)batch.size();
+        return true;
+    }
+
+    void launch(Slot &s, int kind, DeviceGraph &g, const std::vector<SRequest *> &batch, int32_t k, size_t out_bytes)
+    {
+        GU_CUDA_CHECK(cudaSetDevice(device_));
+        const int nreq = (int)batch.size();
+        // pinned staging: sources | request offsets | outputs
+        const size_t src_b = ((size_t)k * 4 + 255) / 256 * 256;
+        const size_t off_b = ((size_t)(nreq + 1) * 4 + 255) / 256 * 256;
+        char *stage = (char *)s.stage.get(src_b + off_b + out_bytes + 256);
+        int32_t *hs = reinterpret_cast<int32_t *>(stage);
+        int32_t *hoff = reinterpret_cast<int32_t *>(stage + src_b);
+        int32_t pos = 0;
+        for (int i = 0; i < nreq; ++i) {
+            hoff[i] = pos;
+            std::memcpy(hs + pos, batch[i]->src.data(), batch[i]->src.size() * sizeof(int32_t));
+            pos += (int32_t)batch[i]->src.size();
+        }
+        hoff[nreq] = pos;
+        s.out_off = src_b + off_b;
+        // device io: sources | offsets | rows or bc | counts
+        const size_t rows_b = (kind == GU_QUERY_BC) ? (size_t)nreq * g.n * sizeof(double)
+                                                    : ((size_t)k * g.n * sizeof(int32_t) + 255) / 256 * 256;
+        const size_t cnt_b = kind == GU_QUERY_REACH ? (size_t)k * sizeof(long long) : 0;
+        char *io = (char *)s.io.get(src_b + off_b + rows_b + cnt_b + 256);
+        int32_t *dsrc = reinterpret_cast<int32_t *>(io);
+        int32_t *doff = reinterpret_cast<int32_t *>(io + src_b);
+        char *drows = io + src_b + off_b;
+        GU_CUDA_CHECK(cudaMemcpyAsync(dsrc, hs, src_b + off_b, cudaMemcpyHostToDevice, s.st));
+        {
+            std::lock_guard<std::mutex> glk(g.mu);  // lazily built graph-side structures
+            if (kind == GU_QUERY_BC) {
+                BcOptions o;
+                o.ws = &s.ws;
+                o.max_blocks = blocks_per_slot_;
+                o.timed = false;
+                o.req_start = doff;
+                o.nreq = nreq;
+                launch_bc(g, dsrc, k, o, reinterpret_cast<double *>(drows), nullptr, nullptr, nullptr, g.n, true, s.st);
+            } else {
+                MsOptions o;
+                o.variant = GU_BFS_AUTO;
+                o.ws = &s.ws;
+                o.max_blocks = blocks_per_slot_;
+                o.timed = false;
+                launch_msbfs(g, dsrc, k, reinterpret_cast<int32_t *>(drows), g.n, o, s.st, nullptr);
+            }
+        }
+        if (kind == GU_QUERY_REACH) {
+            long long *dcnt = reinterpret_cast<long long *>(drows + rows_b);
+            count_reached_kernel<<<std::min(k, 4096), 256, 0, s.st>>>(reinterpret_cast<int32_t *>(drows), g.n, k, dcnt);
+            GU_CUDA_CHECK(cudaGetLastError());
+            GU_CUDA_CHECK(cudaMemcpyAsync(stage + s.out_off, dcnt, (size_t)k * sizeof(long long), cudaMemcpyDeviceToHost, s.st));
+        } else {
+            GU_CUDA_CHECK(cudaMemcpyAsync(stage + s.out_off, drows, out_bytes, cudaMemcpyDeviceToHost, s.st));
+        }
+        GU_CUDA_CHECK(cudaEventRecord(s.ev, s.st));
+        s.busy = true;
+        s.kind = kind;
+        s.g = &g;
+        s.reqs = batch;
+    }
+
+    // Completes slot s's batch if its work is done (mu_ held).
+    bool poll(Slot &s)
+    {
+        if (!s.busy) return false;
+        const cudaError_t q = cudaEventQuery(s.ev);
+        if (q == cudaErrorNotReady) return false;
+        gu_status st = GU_OK;
+        std::string err;
+        if (q != cudaSuccess) {
+            st = GU_ERR_CUDA;
+            err = cudaGetErrorString(q);
+        } else {
+            const int e = s.kind == GU_QUERY_BC ? bc_ws_error(s.ws) : msbfs_ws_error(s.ws);
+            if (e == DEV_ERR_BARRIER_TIMEOUT) {
+                st = GU_ERR_TIMEOUT;
+                err = "a device-side wait exceeded its limit";
+            } else if (e != 0) {
+                st = e == 3 && s.kind == GU_QUERY_BC ? GU_ERR_CAPACITY : GU_ERR_INTERNAL;
+                err = "device reported error code " + std::to_string(e);
+            }
+        }
+        const char *out = (const char *)s.stage.p + s.out_off;
+        size_t off = 0;
+        for (SRequest *r : s.reqs) {
+            const size_t b = row_bytes(r);
+            if (st == GU_OK) std::memcpy(r->out, out + off, b);
+            off += b;
+            finish(r, st, err);
+        }
+        s.busy = false;
+        s.reqs.clear();
+        cv_done_.notify_all();
+        return true;
+    }
+
+    void loop()
+    {
+        cudaSetDevice(device_);
+        std::unique_lock<std::mutex> lk(mu_);
+        while (true) {
+            bool any_busy = false, progressed = false;
+            for (Slot &s : slots_) progressed |= poll(s);
+            for (Slot &s : slots_)
+                if (!s.busy) progressed |= try_launch(s);
+            for (Slot &s : slots_) any_busy |= s.busy;
+            if (stop_ && !any_busy && pending_.empty()) break;
+            if (!any_busy && !progressed) {
+                cv_work_.wait_for(lk, std::chrono::milliseconds(50));
+            } else if (!progressed) {
+                lk.unlock();
+                std::this_thread::sleep_for(std::chrono::microseconds(20));
+                lk.lock();
+            }
+        }
+    }
+
+    size_t budget_;
+    int max_batch_;
+    int device_ = 0;
+    int blocks_per_slot_ = 1;
+    std::vector<Slot> slots_;
+    std::mutex mu_;
+    std::condition_variable cv_work_, cv_done_;
+    std::deque<SRequest *> pending_;
+    std::unordered_map<int64_t, std::unique_ptr<SRequest> > all_;
+    int64_t next_id_ = 0, completed_ = 0, batches_ = 0, batched_reqs_ = 0;
+    std::vector<double> latencies_;
+    bool stop_ = false;
+    std::thread worker_;
+};
+
+Server *server_create(size_t budget, int nslots, int max_batch) { return new Server(budget, nslots, max_batch); }
+void server_destroy(Server *s) { delete s; }
+int64_t server_submit(Server *s, int kind, DeviceGraph *g, const int32_t *src, int32_t k, void *out)
+{
+    return s->submit(kind, g, src, k, out);
+}
+gu_status server_wait(Server *s, int64_t id, double timeout, double *latency, std::string &err)
+{
+    return s->wait(id, timeout, latency, err);
+}
+void server_stats(Server *s, int64_t *completed, int64_t *batches, double *p50, double *p99, double *mean_batch)
+{
+    s->stats(completed, batches, p50, p99, mean_batch);
+}
+
+}  // namespace gu

@@ -83,6 +83,12 @@ def lib():
         "gu_diameter": ([_vp, _vp, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32), _vp], ctypes.c_int),
         "gu_lbs": ([_vp, ctypes.c_int32, _vp, _vp, ctypes.c_int64, _vp, _i64p, _vp], ctypes.c_int),
         "gu_race_and_resolve": ([_vp, ctypes.c_int32, _vp, _vp], ctypes.c_int),
+        "gu_server_create": ([ctypes.c_size_t, ctypes.c_int, ctypes.c_int, ctypes.POINTER(_vp)], ctypes.c_int),
+        "gu_server_destroy": ([_vp], ctypes.c_int),
+        "gu_server_submit": ([_vp, _vp, ctypes.c_int, _i32p, ctypes.c_int32, _vp, _i64p], ctypes.c_int),
+        "gu_server_wait": ([_vp, ctypes.c_int64, ctypes.c_double, ctypes.POINTER(ctypes.c_double)], ctypes.c_int),
+        "gu_server_stats": ([_vp, _i64p, _i64p, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
+                             ctypes.POINTER(ctypes.c_double)], ctypes.c_int),
         "gu_bfs_noalloc": ([_vp, _vp, ctypes.c_int32, ctypes.c_int64, _vp, ctypes.c_int32, _vp, ctypes.c_int64, _vp],
                            ctypes.c_int),
     }
@@ -279,3 +285,53 @@ def race_and_resolve(pred_dev, winners_dev, stream=None):
     check(lib().gu_race_and_resolve(pred_dev.data_ptr(), int(pred_dev.numel()) // 32, winners_dev.data_ptr(),
                                     _stream_handle(stream)))
     return winners_dev
+
+
+QUERY_BFS, QUERY_BC, QUERY_REACH = 0, 1, 2
+PENDING = 9
+
+
+class Server:
+    """Continuous-batching query server (gu_server_*)."""
+
+    def __init__(self, hbm_budget_bytes=8 << 30, slots=4, max_batch=256):
+        self._h = _vp()
+        check(lib().gu_server_create(hbm_budget_bytes, slots, max_batch, ctypes.byref(self._h)))
+        self._keep = {}
+
+    def submit(self, graph, query, sources, out):
+        """Queue a request; `out` (numpy) receives the result when it is waited for."""
+        s = np.ascontiguousarray(sources, dtype=np.int32)
+        rid = ctypes.c_int64()
+        check(lib().gu_server_submit(self._h, graph._h, query, _ptr(s), len(s), out.ctypes.data_as(_vp),
+                                     ctypes.byref(rid)))
+        self._keep[rid.value] = (s, out)
+        return rid.value
+
+    def wait(self, rid, timeout=-1.0):
+        lat = ctypes.c_double()
+        st = lib().gu_server_wait(self._h, rid, timeout, ctypes.byref(lat))
+        if st == PENDING:
+            return None
+        self._keep.pop(rid, None)
+        check(st)
+        return lat.value
+
+    def stats(self):
+        c, b = ctypes.c_int64(), ctypes.c_int64()
+        p50, p99, mb = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        check(lib().gu_server_stats(self._h, ctypes.byref(c), ctypes.byref(b), ctypes.byref(p50), ctypes.byref(p99),
+                                    ctypes.byref(mb)))
+        return dict(completed=c.value, batches=b.value, p50_s=p50.value, p99_s=p99.value,
+                    mean_requests_per_batch=mb.value)
+
+    def close(self):
+        if self._h:
+            lib().gu_server_destroy(self._h)
+            self._h = _vp()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -34,7 +34,8 @@ typedef enum gu_status {
     GU_ERR_OVERFLOW = 5,
     GU_ERR_TIMEOUT = 6,
     GU_ERR_UNSUPPORTED = 7,
-    GU_ERR_INTERNAL = 8
+    GU_ERR_INTERNAL = 8,
+    GU_ERR_PENDING = 9 /* gu_server_wait: the request has not finished within the timeout */
 } gu_status;
 
 /* Breadth-first-search variants.  Each names the neighbour-gathering strategy
@@ -185,6 +186,37 @@ gu_status gu_lbs(const int32_t *counts_dev, int32_t N, int32_t *scanned_dev, int
  * is.  Exposes race_and_resolve_warp (race_and_resolve.cuh:13-25), the device
  * primitive the WARP and CTA_WARP gathers use. */
 gu_status gu_race_and_resolve(const int32_t *predicates_dev, int32_t nwarps, int32_t *winners_dev, void *stream);
+
+/* ---- serving ---------------------------------------------------------------------- */
+/* A query server with continuous batching over device-resident graphs (no
+ * reference counterpart: the reference runs one synchronous call at a time).
+ * Requests from any host thread join a FIFO; a worker merges the oldest
+ * request with later ones for the same graph and kind into a batch of at most
+ * max_batch_sources sources, admits it when one of `slots` streams is free and
+ * its device footprint fits hbm_budget_bytes next to the running batches, and
+ * runs it on 1/slots of the GPU, so batches overlap.  Results:
+ *   GU_QUERY_BFS    out_host = k x n int32 distance rows (as gu_bfs)
+ *   GU_QUERY_BC     out_host = n doubles, betweenness from the k sources (as gu_bc)
+ *   GU_QUERY_REACH  out_host = k int64, vertices reachable from each source
+ *                   (itself included; the reference's transitive closure rows
+ *                   reduced to counts, transitive_closure.cu:4-37)
+ * BFS rows and reach counts equal a lone call bit for bit; BC is within 1e-12
+ * relative of a lone call.  The graph must outlive its requests. */
+typedef enum gu_query { GU_QUERY_BFS = 0, GU_QUERY_BC = 1, GU_QUERY_REACH = 2 } gu_query;
+typedef struct gu_server_s *gu_server;
+gu_status gu_server_create(size_t hbm_budget_bytes, int slots, int max_batch_sources, gu_server *out);
+gu_status gu_server_destroy(gu_server s); /* finishes queued work first */
+/* sources_host is copied; out_host must stay valid until the request is waited for. */
+gu_status gu_server_submit(gu_server s, gu_graph g, int query, const int32_t *sources_host, int32_t k, void *out_host,
+                           int64_t *request_id);
+/* Blocks until the request finishes (timeout_s < 0: no limit; GU_ERR_PENDING on
+ * timeout) and returns its status; the latency from submit to completion goes
+ * to *latency_s.  A finished request can be waited for once. */
+gu_status gu_server_wait(gu_server s, int64_t request_id, double timeout_s, double *latency_s);
+/* Completed requests, batches launched, latency percentiles (s) and the mean
+ * number of requests per batch since creation. */
+gu_status gu_server_stats(gu_server s, int64_t *completed, int64_t *batches, double *p50_s, double *p99_s,
+                          double *mean_requests_per_batch);
 
 /* Multi-source BFS that allocates no device memory.  No counterpart in the
  * reference: it exists for callers that may not call cudaMalloc while they

@@ -1,0 +1,119 @@
+"""The continuous-batching server: every result in the mix equals the same request alone.
+
+Requests of three kinds (BFS rows, BC over a source set, reachable counts on a
+DAG) against three device-resident graphs are submitted from several host
+threads with random gaps, so batches form while others run.  BFS rows and
+reach counts must be bit-identical to a lone call; BC within 1e-12 relative.
+"""
+import threading
+import time
+
+import numpy as np
+import pytest
+
+import gu
+import oracle
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+
+def lone_bfs(g, srcs):
+    s = torch.as_tensor(np.asarray(srcs, np.int32), device="cuda")
+    d = torch.empty((len(srcs), g.n), dtype=torch.int32, device="cuda")
+    g.bfs(s, d)
+    return d.cpu().numpy()
+
+
+def lone_bc(g, srcs):
+    s = torch.as_tensor(np.asarray(srcs, np.int32), device="cuda")
+    bc = torch.empty(g.n, dtype=torch.float64, device="cuda")
+    g.bc(s, bc)
+    return bc.cpu().numpy()
+
+
+@pytest.fixture(scope="module")
+def graphs():
+    return {"rmat12": gu.Graph(gu.HostGraph.rmat(12, 16, seed=21)),
+            "rmat13": gu.Graph(gu.HostGraph.rmat(13, 8, seed=22)),
+            "dag": gu.Graph(gu.HostGraph.dag(20000, 160000, seed=23))}
+
+
+def test_results_alone_and_in_the_mix(graphs):
+    srv = gu.Server(hbm_budget_bytes=16 << 30, slots=4, max_batch=256)
+    rng = np.random.default_rng(7)
+    plan = []
+    for i in range(72):
+        kind = rng.choice(["bfs", "bc", "reach"], p=[0.5, 0.25, 0.25])
+        if kind == "reach":
+            gname = "dag"
+        else:
+            gname = rng.choice(["rmat12", "rmat13"])
+        g = graphs[gname]
+        k = int(rng.integers(1, 65 if kind != "bc" else 41))
+        srcs = rng.choice(g.n, size=k, replace=False).astype(np.int32)
+        plan.append((kind, gname, srcs, float(rng.exponential(0.002))))
+    results = [None] * len(plan)
+    errors = []
+
+    def client(idx):
+        try:
+            for i in idx:
+                kind, gname, srcs, gap = plan[i]
+                g = graphs[gname]
+                time.sleep(gap)
+                if kind == "bfs":
+                    out, q = np.empty((len(srcs), g.n), np.int32), gu.QUERY_BFS
+                elif kind == "bc":
+                    out, q = np.empty(g.n, np.float64), gu.QUERY_BC
+                else:
+                    out, q = np.empty(len(srcs), np.int64), gu.QUERY_REACH
+                rid = srv.submit(g, q, srcs, out)
+                results[i] = (rid, out)
+        except Exception as e:  # surfaced below
+            errors.append(e)
+
+    threads = [threading.Thread(target=client, args=(list(range(t, len(plan), 4)),)) for t in range(4)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    assert not errors, errors
+    lat = [srv.wait(rid) for rid, _ in results]
+    assert all(x is not None and x >= 0 for x in lat)
+    st = srv.stats()
+    assert st["completed"] == len(plan)
+    assert st["batches"] < len(plan), st  # requests were merged into shared batches
+    for i, (kind, gname, srcs, _) in enumerate(plan):
+        g = graphs[gname]
+        out = results[i][1]
+        if kind == "bfs":
+            np.testing.assert_array_equal(out, lone_bfs(g, srcs), err_msg=f"request {i}")
+        elif kind == "reach":
+            rows = lone_bfs(g, srcs)
+            np.testing.assert_array_equal(out, (rows != gu.UNREACHABLE).sum(1), err_msg=f"request {i}")
+            assert out[0] == oracle.reach_count(g.host.R, g.host.C, g.n, srcs[:1])
+        else:
+            ref = lone_bc(g, srcs)
+            rel = np.abs(out - ref) / np.maximum(np.abs(ref), 1e-300)
+            assert np.all((rel <= 1e-12) | (np.abs(out - ref) == 0)), f"request {i}: {rel.max()}"
+    srv.close()
+
+
+def test_admission_by_hbm_budget(graphs):
+    g = graphs["rmat13"]
+    srv = gu.Server(hbm_budget_bytes=1 << 20, slots=2, max_batch=64)  # 1 MiB: nothing fits
+    out = np.empty((4, g.n), np.int32)
+    rid = srv.submit(g, gu.QUERY_BFS, np.arange(4, dtype=np.int32), out)
+    with pytest.raises(gu.GuError) as e:
+        srv.wait(rid)
+    assert e.value.status == 4  # GU_ERR_CAPACITY
+    srv.close()
+
+
+def test_bad_request_rejected(graphs):
+    srv = gu.Server(slots=1)
+    g = graphs["rmat12"]
+    with pytest.raises(gu.GuError):
+        srv.submit(g, gu.QUERY_BFS, np.array([g.n], np.int32), np.empty((1, g.n), np.int32))
+    srv.close()
