@@ -242,6 +242,47 @@ __device__ __forceinline__ void td_visit(const MsArgs &a, const Lvl &L, const u6
     if (first) append_vertex(a, L.slot, L.qnxt, L.qnxt_off, w);
 }
 
+// Two visits with their state loads issued together (w2 < 0: none).
+template <int W>
+__device__ __forceinline__ void td_visit2(const MsArgs &a, const Lvl &L, const u64 (&f)[W], int32_t w,
+                                          const u64 (&f2)[W], int32_t w2)
+{
+    const size_t o = (size_t)w * W, o2 = (size_t)(w2 < 0 ? w : w2) * W;
+    u64 s[W], c[W], x[W], s2[W], c2[W], x2[W];
+    ldw<W>(a.seen + o, s);
+    ldw<W>(L.fcur + o, c);
+    ldw<W>(L.fnxt + o, x);
+    ldw<W>(a.seen + o2, s2);
+    ldw<W>(L.fcur + o2, c2);
+    ldw<W>(L.fnxt + o2, x2);
+    u64 nb[W], nb2[W];
+#pragma unroll
+    for (int q = 0; q < W; ++q) {
+        nb[q] = f[q] & ~(s[q] | c[q] | x[q]);
+        nb2[q] = w2 < 0 ? 0ull : (f2[q] & ~(s2[q] | c2[q] | x2[q]));
+    }
+    bool found = false, found2 = false, first = false, first2 = false;
+#pragma unroll
+    for (int q = 0; q < W; ++q) {
+        if (nb[q]) {
+            const u64 old = atomicOr(L.fnxt + o + q, nb[q]);
+            found = true;
+            if (W == 1 && old == 0) first = true;
+        }
+        if (nb2[q]) {
+            const u64 old = atomicOr(L.fnxt + o2 + q, nb2[q]);
+            found2 = true;
+            if (W == 1 && old == 0) first2 = true;
+        }
+    }
+    if (W > 1) {
+        if (found) first = atomicMax(a.stamp + w, L.tag) < L.tag;
+        if (found2) first2 = atomicMax(a.stamp + w2, L.tag) < L.tag;
+    }
+    if (first) append_vertex(a, L.slot, L.qnxt, L.qnxt_off, w);
+    if (first2) append_vertex(a, L.slot, L.qnxt, L.qnxt_off, w2);
+}
+
 // Finalise F_{j-1} bits of one vertex: seen and the level bit-planes.  Only the
 // thread that owns the vertex in this phase calls it.
 template <int W>
@@ -543,16 +584,28 @@ __device__ void gather_mp(const MsArgs &a, const Lvl &L)
                 s_r[i] = __ldg(a.R + v);
             }
             __syncthreads();
-            for (long long e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
+            // two edge slots per trip: both visits' loads are issued before either claims
+            for (long long e = e0 + threadIdx.x; e < e1; e += 2 * (long long)blockDim.x) {
+                const long long e2 = e + blockDim.x;
                 int lo = 0, hi = nk - 1;
                 while (lo < hi) {
                     const int mid = (lo + hi + 1) >> 1;
                     if ((long long)s_off[mid] <= e) lo = mid;
                     else hi = mid - 1;
                 }
-                u64 f[W];
+                int lo2 = lo, hi2 = nk - 1;
+                while (lo2 < hi2) {
+                    const int mid = (lo2 + hi2 + 1) >> 1;
+                    if ((long long)s_off[mid] <= e2) lo2 = mid;
+                    else hi2 = mid - 1;
+                }
+                const bool has2 = e2 < e1;
+                u64 f[W], f2[W];
                 load_front<W>(L, s_v[lo], f);
-                td_visit<W>(a, L, f, __ldg(a.C + s_r[lo] + (int32_t)(e - s_off[lo])));
+                if (has2) load_front<W>(L, s_v[lo2], f2);
+                const int32_t w = __ldg(a.C + s_r[lo] + (int32_t)(e - s_off[lo]));
+                const int32_t w2 = has2 ? __ldg(a.C + s_r[lo2] + (int32_t)(e2 - s_off[lo2])) : -1;
+                td_visit2<W>(a, L, f, w, f2, w2);
             }
         } else {
             for (int i = threadIdx.x; i < nk; i += blockDim.x) {
@@ -616,16 +669,13 @@ __device__ void bu_sweep(const MsArgs &a, const Lvl &L)
         const int32_t e0 = __ldg(a.RT + w), e1 = __ldg(a.RT + w + 1);
         if (e1 - e0 > BU_LIGHT_DEGREE || e1 == e0) continue;  // mid / heavy classes: bu_mid, bu_heavy
         u64 acc[W] = {};
-        for (int32_t e = e0; e < e1; e += 4) {
-            const int32_t c0 = __ldg(a.CT + e);
-            const int32_t c1 = e + 1 < e1 ? __ldg(a.CT + e + 1) : -1;
-            const int32_t c2 = e + 2 < e1 ? __ldg(a.CT + e + 2) : -1;
-            const int32_t c3 = e + 3 < e1 ? __ldg(a.CT + e + 3) : -1;
-            or_front<W>(L, c0, acc);
-            if (c1 >= 0) or_front<W>(L, c1, acc);
-            if (c2 >= 0) or_front<W>(L, c2, acc);
-            if (c3 >= 0) or_front<W>(L, c3, acc);
-            if (covers<W>(acc, need)) break;
+        {  // at most BU_LIGHT_DEGREE (8) in-neighbours: all loads in flight at once
+            int32_t c[BU_LIGHT_DEGREE];
+#pragma unroll
+            for (int t = 0; t < BU_LIGHT_DEGREE; ++t) c[t] = e0 + t < e1 ? __ldg(a.CT + e0 + t) : -1;
+#pragma unroll
+            for (int t = 0; t < BU_LIGHT_DEGREE; ++t)
+                if (c[t] >= 0) or_front<W>(L, c[t], acc);
         }
         u64 nb[W];
 #pragma unroll
@@ -639,8 +689,8 @@ __device__ void bu_sweep(const MsArgs &a, const Lvl &L)
 }
 
 // Mid-degree vertices (BU_LIGHT_DEGREE < in-degree <= BU_HEAVY_DEGREE): eight
-// lanes per vertex OR eight in-neighbours per step; the group stops once every
-// missing active source is found.
+// lanes per vertex OR 32 in-neighbours per step (four loads in flight per lane);
+// the group stops once every missing active source is found.
 template <int W, class G>
 __device__ void bu_mid(const MsArgs &a, const Lvl &L)
 {
@@ -659,10 +709,20 @@ __device__ void bu_mid(const MsArgs &a, const Lvl &L)
         if (!anyw<W>(need)) continue;
         const int32_t e0 = __ldg(a.RT + w), e1 = __ldg(a.RT + w + 1);
         u64 acc[W] = {};
-        for (int32_t eb = e0; eb < e1; eb += 8) {
+        {  // first step: the 8 highest-degree in-neighbours, which most often cover everything
             u64 x[W] = {};
-            const int32_t e = eb + sub;
-            if (e < e1) ldw<W>(L.fcur + (size_t)__ldg(a.CT + e) * W, x);
+            if (e0 + sub < e1) or_front<W>(L, __ldg(a.CT + e0 + sub), x);
+#pragma unroll
+            for (int q = 0; q < W; ++q) acc[q] |= warp_or_u64(gmask, x[q]);
+        }
+        for (int32_t eb = e0 + 8; eb < e1 && !covers<W>(acc, need); eb += 32) {  // then 32 per step, 4 per lane
+            u64 x[W] = {};
+            int32_t c[4];
+#pragma unroll
+            for (int t = 0; t < 4; ++t) c[t] = eb + 8 * t + sub < e1 ? __ldg(a.CT + eb + 8 * t + sub) : -1;
+#pragma unroll
+            for (int t = 0; t < 4; ++t)
+                if (c[t] >= 0) or_front<W>(L, c[t], x);
 #pragma unroll
             for (int q = 0; q < W; ++q) acc[q] |= warp_or_u64(gmask, x[q]);
             if (covers<W>(acc, need)) break;
@@ -677,8 +737,8 @@ __device__ void bu_mid(const MsArgs &a, const Lvl &L)
     }
 }
 
-// Heavy vertices (in-degree > BU_HEAVY_DEGREE): a warp per vertex ORs 64
-// in-neighbours per step (two loads in flight per lane) and stops once every
+// Heavy vertices (in-degree > BU_HEAVY_DEGREE): a warp per vertex ORs 128
+// in-neighbours per step (four loads in flight per lane) and stops once every
 // missing active source is found.
 template <int W, class G>
 __device__ void bu_heavy(const MsArgs &a, const Lvl &L)
@@ -696,13 +756,20 @@ __device__ void bu_heavy(const MsArgs &a, const Lvl &L)
         if (!anyw<W>(need)) continue;
         const int32_t e0 = __ldg(a.RT + w), e1 = __ldg(a.RT + w + 1);
         u64 acc[W] = {};
-        for (int32_t eb = e0; eb < e1; eb += 64) {
+        {  // first step: the 32 highest-degree in-neighbours
             u64 x[W] = {};
-            const int32_t ea = eb + lane, ebb = eb + 32 + lane;
-            const int32_t ca = ea < e1 ? __ldg(a.CT + ea) : -1;
-            const int32_t cb = ebb < e1 ? __ldg(a.CT + ebb) : -1;
-            if (ca >= 0) or_front<W>(L, ca, x);
-            if (cb >= 0) or_front<W>(L, cb, x);
+            if (e0 + lane < e1) or_front<W>(L, __ldg(a.CT + e0 + lane), x);
+#pragma unroll
+            for (int q = 0; q < W; ++q) acc[q] |= warp_or_u64(FULL_MASK, x[q]);
+        }
+        for (int32_t eb = e0 + 32; eb < e1 && !covers<W>(acc, need); eb += 128) {  // then 128 per step
+            u64 x[W] = {};
+            int32_t c[4];
+#pragma unroll
+            for (int t = 0; t < 4; ++t) c[t] = eb + 32 * t + lane < e1 ? __ldg(a.CT + eb + 32 * t + lane) : -1;
+#pragma unroll
+            for (int t = 0; t < 4; ++t)
+                if (c[t] >= 0) or_front<W>(L, c[t], x);
 #pragma unroll
             for (int q = 0; q < W; ++q) acc[q] |= warp_or_u64(FULL_MASK, x[q]);
             if (covers<W>(acc, need)) break;
@@ -725,6 +792,21 @@ __device__ void bu_heavy(const MsArgs &a, const Lvl &L)
 // CTA writes each row's segment (2 KiB for 512 vertices) with contiguous int4
 // stores.  Otherwise lanes hold consecutive vertices and store one int each.
 constexpr int WD_ROWS = 16;
+
+// Transpose of an 8x8 bit matrix held row-major in a u64 (bit 8r+c -> bit
+// 8c+r): three rounds of masked swaps of the off-diagonal blocks, the method of
+// Warren, "Hacker's Delight", section 7-3.
+__device__ __forceinline__ u64 transpose8x8(u64 x)
+{
+    u64 t;
+    t = (x ^ (x >> 7)) & 0x00AA00AA00AA00AAull;
+    x = x ^ t ^ (t << 7);
+    t = (x ^ (x >> 14)) & 0x0000CCCC0000CCCCull;
+    x = x ^ t ^ (t << 14);
+    t = (x ^ (x >> 28)) & 0x00000000F0F0F0F0ull;
+    x = x ^ t ^ (t << 28);
+    return x;
+}
 
 template <int W, class G>
 __device__ void write_distances(const MsArgs &a, int row0, int nb, int nplanes_used)
@@ -749,12 +831,18 @@ __device__ void write_distances(const MsArgs &a, int row0, int nb, int nplanes_u
             const int nv = min(BD, a.n - vbase);  // vertices in this tile
             for (int r0 = 0; r0 < rows; r0 += WD_ROWS) {
 #pragma unroll
-                for (int i = 0; i < WD_ROWS; ++i) {
-                    const int bit = r0 + i;
-                    int32_t lvl = 0;
+                for (int h = 0; h < WD_ROWS / 8; ++h) {
+                    // sources 8g..8g+7: byte b of M = byte g of plane b; after an
+                    // 8x8 bit-matrix transpose byte c of M is the level of source 8g+c
+                    const int g8 = (r0 >> 3) + h;
+                    u64 M = 0;
 #pragma unroll
-                    for (int b = 0; b < 8; ++b) lvl |= (int32_t)((pl[b] >> bit) & 1ull) << b;
-                    tile[i][threadIdx.x] = ((s >> bit) & 1ull) ? lvl : INT_MAX;
+                    for (int b = 0; b < 8; ++b) M |= ((pl[b] >> (8 * g8)) & 0xFFull) << (8 * b);
+                    M = transpose8x8(M);
+                    const unsigned sb = (unsigned)(s >> (8 * g8)) & 0xFFu;
+#pragma unroll
+                    for (int c = 0; c < 8; ++c)
+                        tile[8 * h + c][threadIdx.x] = ((sb >> c) & 1u) ? (int32_t)((M >> (8 * c)) & 0xFFull) : INT_MAX;
                 }
                 __syncthreads();
                 const int nr = min(WD_ROWS, rows - r0);
@@ -763,7 +851,8 @@ __device__ void write_distances(const MsArgs &a, int row0, int nb, int nplanes_u
                     const int r = k / (BD >> 2), c4 = k - r * (BD >> 2);
                     int32_t *drow = a.dist + (int64_t)(row0 + 64 * q + r0 + r) * a.ld + vbase;
                     if (c4 < nv4) {
-                        reinterpret_cast<int4 *>(drow)[c4] = reinterpret_cast<const int4 *>(&tile[r][0])[c4];
+                        // streaming store: the rows are not read again by this kernel
+                        __stcs(reinterpret_cast<int4 *>(drow) + c4, reinterpret_cast<const int4 *>(&tile[r][0])[c4]);
                     } else if (c4 == nv4) {
                         for (int x = 4 * c4; x < nv; ++x) drow[x] = tile[r][x];
                     }
