@@ -162,6 +162,25 @@ __device__ __forceinline__ void ldw(const u64 *p, u64 (&x)[W])
     }
 }
 
+// L1-allocating load of words that no thread changes in a way that matters
+// within the current phase (the frontier being expanded, seen | frontier):
+// hub vertices' words are re-read by many warps of an SM.  The grid barrier's
+// acquire fence invalidates L1, so no line survives from an earlier phase.
+template <int W>
+__device__ __forceinline__ void ldw_l1(const u64 *p, u64 (&x)[W])
+{
+    if constexpr (W == 1) {
+        x[0] = __ldca(p);
+    } else {
+#pragma unroll
+        for (int i = 0; i < W / 2; ++i) {
+            const ulonglong2 v = __ldca(reinterpret_cast<const ulonglong2 *>(p) + i);
+            x[2 * i] = v.x;
+            x[2 * i + 1] = v.y;
+        }
+    }
+}
+
 template <int W>
 __device__ __forceinline__ void stw(u64 *p, const u64 (&x)[W])
 {
@@ -225,8 +244,8 @@ __device__ __forceinline__ void td_visit(const MsArgs &a, const Lvl &L, const u6
 {
     const size_t o = (size_t)w * W;
     u64 s[W], c[W], x[W];
-    ldw<W>(a.seen + o, s);
-    ldw<W>(L.fcur + o, c);
+    ldw_l1<W>(a.seen + o, s);
+    ldw_l1<W>(L.fcur + o, c);
     ldw<W>(L.fnxt + o, x);
     bool found = false, first = false;
 #pragma unroll
@@ -249,11 +268,11 @@ __device__ __forceinline__ void td_visit2(const MsArgs &a, const Lvl &L, const u
 {
     const size_t o = (size_t)w * W, o2 = (size_t)(w2 < 0 ? w : w2) * W;
     u64 s[W], c[W], x[W], s2[W], c2[W], x2[W];
-    ldw<W>(a.seen + o, s);
-    ldw<W>(L.fcur + o, c);
+    ldw_l1<W>(a.seen + o, s);
+    ldw_l1<W>(L.fcur + o, c);
     ldw<W>(L.fnxt + o, x);
-    ldw<W>(a.seen + o2, s2);
-    ldw<W>(L.fcur + o2, c2);
+    ldw_l1<W>(a.seen + o2, s2);
+    ldw_l1<W>(L.fcur + o2, c2);
     ldw<W>(L.fnxt + o2, x2);
     u64 nb[W], nb2[W];
 #pragma unroll
@@ -340,7 +359,7 @@ __device__ void td_update(const MsArgs &a, const Lvl &L)
 template <int W>
 __device__ __forceinline__ void load_front(const Lvl &L, int32_t v, u64 (&f)[W])
 {
-    ldw<W>(L.fcur + (size_t)v * W, f);
+    ldw_l1<W>(L.fcur + (size_t)v * W, f);
 }
 
 // LINEAR: thread per frontier vertex, serial adjacency (linear_with_atomics.cu:122-135).
@@ -640,7 +659,7 @@ template <int W>
 __device__ __forceinline__ void or_front(const Lvl &L, int32_t v, u64 (&acc)[W])
 {
     u64 x[W];
-    ldw<W>(L.fcur + (size_t)v * W, x);
+    ldw_l1<W>(L.fcur + (size_t)v * W, x);
 #pragma unroll
     for (int q = 0; q < W; ++q) acc[q] |= x[q];
 }
