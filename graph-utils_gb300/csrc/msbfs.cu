@@ -147,11 +147,16 @@ struct GridG {
 };
 
 // ---- W-word helpers -----------------------------------------------------------
+// Four words (one 256-source group, 32-byte aligned) move as one 256-bit
+// access: one L1 wavefront per lane instead of two.
 template <int W>
 __device__ __forceinline__ void ldw(const u64 *p, u64 (&x)[W])
 {
     if constexpr (W == 1) {
         x[0] = __ldcg(p);
+    } else if constexpr (W == 4) {
+        asm volatile("ld.global.cg.v4.u64 {%0, %1, %2, %3}, [%4];"
+                     : "=l"(x[0]), "=l"(x[1]), "=l"(x[2]), "=l"(x[3]) : "l"(p) : "memory");
     } else {
 #pragma unroll
         for (int i = 0; i < W / 2; ++i) {
@@ -171,6 +176,9 @@ __device__ __forceinline__ void ldw_l1(const u64 *p, u64 (&x)[W])
 {
     if constexpr (W == 1) {
         x[0] = __ldca(p);
+    } else if constexpr (W == 4) {
+        asm volatile("ld.global.ca.v4.u64 {%0, %1, %2, %3}, [%4];"
+                     : "=l"(x[0]), "=l"(x[1]), "=l"(x[2]), "=l"(x[3]) : "l"(p) : "memory");
     } else {
 #pragma unroll
         for (int i = 0; i < W / 2; ++i) {
@@ -186,6 +194,9 @@ __device__ __forceinline__ void stw(u64 *p, const u64 (&x)[W])
 {
     if constexpr (W == 1) {
         p[0] = x[0];
+    } else if constexpr (W == 4) {
+        asm volatile("st.global.v4.u64 [%0], {%1, %2, %3, %4};"
+                     :: "l"(p), "l"(x[0]), "l"(x[1]), "l"(x[2]), "l"(x[3]) : "memory");
     } else {
 #pragma unroll
         for (int i = 0; i < W / 2; ++i)
