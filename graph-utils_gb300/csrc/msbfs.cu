@@ -146,6 +146,15 @@ struct GridG {
     __device__ static int nblk() { return gridDim.x; }
 };
 
+// One shared-memory buffer per CTA for the phases' staging (merge-path owners
+// and discovered vertices, distance-row tiles); phases never overlap in a CTA.
+constexpr int MS_SMEM_BYTES = 32768;
+__device__ __forceinline__ unsigned char *ms_smem()
+{
+    __shared__ __align__(16) unsigned char buf[MS_SMEM_BYTES];
+    return buf;
+}
+
 // ---- W-word helpers -----------------------------------------------------------
 // Four words (one 256-source group, 32-byte aligned) move as one 256-bit
 // access: one L1 wavefront per lane instead of two.
@@ -249,9 +258,96 @@ __device__ __forceinline__ void append_vertex(const MsArgs &a, int slot, int32_t
     qnxt_off[pos] = (int32_t)((old & QPACK_EDGES) + excl);
 }
 
+// ---- where a top-down visit puts the vertices it discovers first --------------------
+struct GlobalQ {  // straight into the level's queue, one 64-bit atomic per warp
+    __device__ __forceinline__ void push(const MsArgs &a, const Lvl &L, int32_t w) const
+    {
+        append_vertex(a, L.slot, L.qnxt, L.qnxt_off, w);
+    }
+};
+
+// Per-CTA collection in shared memory, appended to the level's queue by
+// cta_flush with one 64-bit atomic per flush: the queue counter is a single
+// address, and one atomic per warp from every warp of the GPU serialises there
+// when a level discovers 10^5..10^6 vertices.  Pushes beyond the capacity go to
+// the queue directly.
+constexpr int CQ_CAP = 2048;
+constexpr int CQ_PER_THREAD = CQ_CAP / MS_THREADS;
+struct CtaQ {
+    int32_t *v;  // [CQ_CAP] shared
+    int *n;      // shared: pushes since the last flush (the excess over CQ_CAP went direct)
+    __device__ __forceinline__ void push(const MsArgs &a, const Lvl &L, int32_t w) const
+    {
+        const unsigned mask = __activemask();
+        const int leader = __ffs(mask) - 1;
+        int base = 0;
+        if (lane_id() == leader) base = atomicAdd(n, __popc(mask));
+        base = __shfl_sync(mask, base, leader);
+        const int pos = base + __popc(mask & lanemask_lt());
+        if (pos < CQ_CAP) v[pos] = w;
+        else append_vertex(a, L.slot, L.qnxt, L.qnxt_off, w);
+    }
+};
+
+// Append the CTA's collected vertices to the level's queue: degrees scanned
+// across the CTA, one atomic reserves the slots and the edge range.  Every
+// thread of the CTA calls it after a __syncthreads (the count is then uniform).
+__device__ void cta_flush(const MsArgs &a, const Lvl &L, const CtaQ &cq, u64 *s_scan /* [33] */)
+{
+    const int cnt = min(*cq.n, CQ_CAP);
+    const int lane = lane_id(), warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int per_round = blockDim.x * CQ_PER_THREAD;
+    for (int r0 = 0; r0 < cnt; r0 += per_round) {
+        const int i0 = r0 + threadIdx.x * CQ_PER_THREAD;
+        int32_t v[CQ_PER_THREAD];
+        unsigned d[CQ_PER_THREAD];
+        u64 sum = 0;
+#pragma unroll
+        for (int t = 0; t < CQ_PER_THREAD; ++t) {
+            v[t] = i0 + t < cnt ? cq.v[i0 + t] : -1;
+            d[t] = v[t] >= 0 ? (unsigned)(__ldg(a.R + v[t] + 1) - __ldg(a.R + v[t])) : 0u;
+            sum += d[t];
+        }
+        u64 inc = sum;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const u64 y = __shfl_up_sync(FULL_MASK, inc, off);
+            if (lane >= off) inc += y;
+        }
+        if (lane == 31) s_scan[warp] = inc;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            u64 run = 0;
+            for (int k = 0; k < nw; ++k) {
+                const u64 t = s_scan[k];
+                s_scan[k] = run;
+                run += t;
+            }
+            const int rc = min(cnt - r0, per_round);
+            s_scan[32] = atomicAdd(&a.ctl->qpack[L.slot], ((u64)rc << QPACK_SHIFT) | run);
+        }
+        __syncthreads();
+        const u64 old = s_scan[32];
+        const long long slot0 = (long long)(old >> QPACK_SHIFT) + (i0 - r0);
+        u64 e = (old & QPACK_EDGES) + s_scan[warp] + (inc - sum);
+#pragma unroll
+        for (int t = 0; t < CQ_PER_THREAD; ++t) {
+            if (v[t] >= 0) {
+                L.qnxt[slot0 + t] = v[t];
+                L.qnxt_off[slot0 + t] = (int32_t)e;
+            }
+            e += d[t];
+        }
+        __syncthreads();  // s_scan is reused by the next round
+    }
+    if (threadIdx.x == 0) *cq.n = 0;
+    __syncthreads();
+}
+
 // ---- top-down visit: frontier bits f arrive at vertex w over one edge ----------------
-template <int W>
-__device__ __forceinline__ void td_visit(const MsArgs &a, const Lvl &L, const u64 (&f)[W], int32_t w)
+template <int W, class Q = GlobalQ>
+__device__ __forceinline__ void td_visit(const MsArgs &a, const Lvl &L, const u64 (&f)[W], int32_t w,
+                                         const Q &qu = Q())
 {
     const size_t o = (size_t)w * W;
     u64 s[W], c[W], x[W];
@@ -269,13 +365,13 @@ __device__ __forceinline__ void td_visit(const MsArgs &a, const Lvl &L, const u6
         }
     }
     if (W > 1 && found) first = atomicMax(a.stamp + w, L.tag) < L.tag;
-    if (first) append_vertex(a, L.slot, L.qnxt, L.qnxt_off, w);
+    if (first) qu.push(a, L, w);
 }
 
 // Two visits with their state loads issued together (w2 < 0: none).
-template <int W>
+template <int W, class Q = GlobalQ>
 __device__ __forceinline__ void td_visit2(const MsArgs &a, const Lvl &L, const u64 (&f)[W], int32_t w,
-                                          const u64 (&f2)[W], int32_t w2)
+                                          const u64 (&f2)[W], int32_t w2, const Q &qu = Q())
 {
     const size_t o = (size_t)w * W, o2 = (size_t)(w2 < 0 ? w : w2) * W;
     u64 s[W], c[W], x[W], s2[W], c2[W], x2[W];
@@ -309,8 +405,8 @@ __device__ __forceinline__ void td_visit2(const MsArgs &a, const Lvl &L, const u
         if (found) first = atomicMax(a.stamp + w, L.tag) < L.tag;
         if (found2) first2 = atomicMax(a.stamp + w2, L.tag) < L.tag;
     }
-    if (first) append_vertex(a, L.slot, L.qnxt, L.qnxt_off, w);
-    if (first2) append_vertex(a, L.slot, L.qnxt, L.qnxt_off, w2);
+    if (first) qu.push(a, L, w);
+    if (first2) qu.push(a, L, w2);
 }
 
 // Finalise F_{j-1} bits of one vertex: seen and the level bit-planes.  Only the
@@ -571,39 +667,62 @@ __device__ void gather_scan(const MsArgs &a, const Lvl &L)
 // offsets reserved at append time, are cut into equal tasks, and the owner of
 // every edge slot is found by binary search over those offsets (the
 // load-balanced search of load_balanced_search.cu:123-192, grid-wide).
-__device__ __forceinline__ int owner_search(const int32_t *off, int lo, int hi, long long e)
+// Warp-wide 32-ary search: the largest idx in [lo, hi] with off[idx] <= e
+// (off non-decreasing, off[lo] <= e).  Each round the lanes probe 32 evenly
+// spaced positions and the ballot of "off <= e" (a prefix of the lanes)
+// narrows the range 32-fold: three dependent loads for 10^4 owners instead of
+// fourteen.  Every lane of the warp calls it and gets the result.
+__device__ __forceinline__ int owner_search_warp(const int32_t *off, int lo, int hi, long long e)
 {
+    const int lane = lane_id();
     while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if ((long long)__ldcg(off + mid) <= e) lo = mid;
-        else hi = mid - 1;
+        const long long span = hi - lo;
+        const int p = lo + (int)((span * (lane + 1) + 31) / 32);  // lo < p <= hi, p(31) = hi
+        const unsigned le = __ballot_sync(FULL_MASK, (long long)__ldcg(off + p) <= e);
+        const int cnt = __popc(le);
+        const int plo = __shfl_sync(FULL_MASK, p, cnt > 0 ? cnt - 1 : 0);
+        const int phi = __shfl_sync(FULL_MASK, p, cnt < 32 ? cnt : 31);
+        if (cnt > 0) lo = plo;
+        hi = cnt < 32 ? phi - 1 : hi;
     }
     return lo;
 }
 
-// A CTA takes MP_TASK consecutive edge slots; two threads bracket the owners
-// [k0, k1] by binary search in global memory, the CTA stages the owners' ids,
+// A CTA takes a task of consecutive edge slots (MP_TASK, or fewer when the
+// frontier is small so that every CTA gets work); two warps bracket the owners
+// [k0, k1] by 32-ary search in global memory, the CTA stages the owners' ids,
 // offsets and CSR starts in shared memory, and every thread then resolves its
 // edge slots by binary search in shared memory.  Tasks whose bracket exceeds
 // the shared capacity (many tiny lists) are walked owner by owner.
 constexpr int MP_TASK = MS_THREADS * 8;
 constexpr int MP_STAGE = 1024;
+static_assert(3 * MP_STAGE * 4 + CQ_CAP * 4 <= MS_SMEM_BYTES, "merge-path staging exceeds the shared buffer");
 
 template <int W, class G>
 __device__ void gather_mp(const MsArgs &a, const Lvl &L)
 {
-    __shared__ int32_t s_off[MP_STAGE];
-    __shared__ int32_t s_v[MP_STAGE];
-    __shared__ int32_t s_r[MP_STAGE];
+    int32_t *s_off = reinterpret_cast<int32_t *>(ms_smem());
+    int32_t *s_v = s_off + MP_STAGE;
+    int32_t *s_r = s_v + MP_STAGE;
+    int32_t *s_cq = s_r + MP_STAGE;  // [CQ_CAP]
     __shared__ int s_k[2];
+    __shared__ int s_cqn;
+    __shared__ u64 s_scan[33];
     const long long E = L.qedges;
     if (E == 0) return;
-    const long long ntask = (E + MP_TASK - 1) / MP_TASK;
+    const CtaQ cq{s_cq, &s_cqn};
+    if (threadIdx.x == 0) s_cqn = 0;
+    const long long per_blk = (E + G::nblk() - 1) / G::nblk();
+    const long long task = min((long long)MP_TASK, max(32ll, (per_blk + 31) & ~31ll));
+    const long long ntask = (E + task - 1) / task;
     for (long long t = G::blk(); t < ntask; t += G::nblk()) {
-        const long long e0 = t * MP_TASK;
-        const long long e1 = min(E, e0 + MP_TASK);
-        if (threadIdx.x == 0) s_k[0] = owner_search(L.qcur_off, 0, L.qlen - 1, e0);
-        if (threadIdx.x == 32) s_k[1] = owner_search(L.qcur_off, 0, L.qlen - 1, e1 - 1);
+        const long long e0 = t * task;
+        const long long e1 = min(E, e0 + task);
+        const int warp = threadIdx.x >> 5;
+        if (warp < 2) {
+            const int k = owner_search_warp(L.qcur_off, 0, L.qlen - 1, warp == 0 ? e0 : e1 - 1);
+            if (lane_id() == 0) s_k[warp] = k;
+        }
         __syncthreads();
         const int k0 = s_k[0], nk = s_k[1] - k0 + 1;
         if (nk <= MP_STAGE) {
@@ -635,7 +754,7 @@ __device__ void gather_mp(const MsArgs &a, const Lvl &L)
                 if (has2) load_front<W>(L, s_v[lo2], f2);
                 const int32_t w = __ldg(a.C + s_r[lo] + (int32_t)(e - s_off[lo]));
                 const int32_t w2 = has2 ? __ldg(a.C + s_r[lo2] + (int32_t)(e2 - s_off[lo2])) : -1;
-                td_visit2<W>(a, L, f, w, f2, w2);
+                td_visit2<W>(a, L, f, w, f2, w2, cq);
             }
         } else {
             for (int i = threadIdx.x; i < nk; i += blockDim.x) {
@@ -646,11 +765,14 @@ __device__ void gather_mp(const MsArgs &a, const Lvl &L)
                 if (lo_e >= hi_e) continue;
                 u64 f[W];
                 load_front<W>(L, v, f);
-                for (long long e = lo_e; e < hi_e; ++e) td_visit<W>(a, L, f, __ldg(a.C + r + (int32_t)(e - off)));
+                for (long long e = lo_e; e < hi_e; ++e) td_visit<W>(a, L, f, __ldg(a.C + r + (int32_t)(e - off)), cq);
             }
         }
         __syncthreads();
+        if (s_cqn > CQ_CAP / 2) cta_flush(a, L, cq, s_scan);
     }
+    __syncthreads();
+    if (s_cqn > 0) cta_flush(a, L, cq, s_scan);
 }
 
 // Bottom-up level: every vertex (coalesced sweep) finalises its own F_{j-1}
@@ -822,6 +944,7 @@ __device__ void bu_heavy(const MsArgs &a, const Lvl &L)
 // CTA writes each row's segment (2 KiB for 512 vertices) with contiguous int4
 // stores.  Otherwise lanes hold consecutive vertices and store one int each.
 constexpr int WD_ROWS = 16;
+static_assert(WD_ROWS * MS_THREADS * 4 <= MS_SMEM_BYTES, "distance tile exceeds the shared buffer");
 
 // Transpose of an 8x8 bit matrix held row-major in a u64 (bit 8r+c -> bit
 // 8c+r): three rounds of masked swaps of the off-diagonal blocks, the method of
@@ -841,7 +964,7 @@ __device__ __forceinline__ u64 transpose8x8(u64 x)
 template <int W, class G>
 __device__ void write_distances(const MsArgs &a, int row0, int nb, int nplanes_used)
 {
-    __shared__ __align__(16) int32_t tile[WD_ROWS][MS_THREADS];
+    int32_t(*tile)[MS_THREADS] = reinterpret_cast<int32_t(*)[MS_THREADS]>(ms_smem());
     const int BD = blockDim.x;
     if (nplanes_used <= 8 && (a.ld & 3) == 0 && (((uintptr_t)a.dist) & 15) == 0 && BD == MS_THREADS) {
         const size_t pstride = (size_t)a.n * W;
