@@ -79,8 +79,8 @@ DeviceGraph::~DeviceGraph()
     io.release();
     if (F) cudaFree(F);
     for (void *p : extra_allocs) cudaFree(p);
-    if (heavy) cudaFree(heavy);
-    if (mid) cudaFree(mid);
+    for (int32_t *p : {light, mid, wide, heavy})
+        if (p) cudaFree(p);
     if (RT && RT != R) cudaFree(RT);
     if (CT && CT != C) cudaFree(CT);
     if (R) cudaFree(R);
@@ -165,7 +165,7 @@ DeviceGraph *create_device_graph(const int32_t *R, const int32_t *C, int32_t n, 
     }
     {
         // static lists of the bottom-up degree classes, by in-degree
-        std::vector<int32_t> heavy, mid;
+        std::vector<int32_t> light, mid, wide, heavy;
         std::vector<int32_t> indeg((size_t)n, 0);
         if (directed) {
             for (int64_t e = 0; e < m; ++e) indeg[C[e]]++;
@@ -174,7 +174,9 @@ DeviceGraph *create_device_graph(const int32_t *R, const int32_t *C, int32_t n, 
         }
         for (int32_t v = 0; v < n; ++v) {
             if (indeg[v] > BU_HEAVY_DEGREE) heavy.push_back(v);
+            else if (indeg[v] > BU_MID_DEGREE) wide.push_back(v);
             else if (indeg[v] > BU_LIGHT_DEGREE) mid.push_back(v);
+            else if (indeg[v] > 0) light.push_back(v);
         }
         auto upload = [&](const std::vector<int32_t> &src, int32_t *&dst, int32_t &cnt) {
             cnt = (int32_t)src.size();
@@ -183,8 +185,10 @@ DeviceGraph *create_device_graph(const int32_t *R, const int32_t *C, int32_t n, 
             GU_CUDA_CHECK(cudaMemcpyAsync(dst, src.data(), sizeof(int32_t) * src.size(), cudaMemcpyHostToDevice, stream));
             g->bytes += sizeof(int32_t) * src.size();
         };
-        upload(heavy, g->heavy, g->nheavy);
+        upload(light, g->light, g->nlight);
         upload(mid, g->mid, g->nmid);
+        upload(wide, g->wide, g->nwide);
+        upload(heavy, g->heavy, g->nheavy);
         GU_CUDA_CHECK(cudaStreamSynchronize(stream));
     }
     return g.release();

@@ -19,9 +19,12 @@
 
 namespace gu {
 
-// Bottom-up degree classes (by in-degree): <= BU_LIGHT_DEGREE one thread per
-// vertex, <= BU_HEAVY_DEGREE eight lanes per vertex, above that a whole warp.
+// Bottom-up degree classes (by in-degree, vertices with in-degree 0 in none):
+// <= BU_LIGHT_DEGREE one thread per vertex, <= BU_MID_DEGREE eight lanes per
+// vertex, <= BU_HEAVY_DEGREE a warp per vertex with every in-edge loaded at
+// once, above that a warp stepping through the in-edges.
 constexpr int BU_LIGHT_DEGREE = 8;
+constexpr int BU_MID_DEGREE = 32;
 constexpr int BU_HEAVY_DEGREE = 128;
 // Every workspace starts with this many bytes of launch control block and
 // profiling timeline; kernel scratch follows.
@@ -108,13 +111,11 @@ struct DeviceGraph {
     int32_t *RT = nullptr, *CT = nullptr;
     int32_t *F = nullptr;
     int32_t max_degree = 0;
-    // vertices whose in-degree exceeds BU_HEAVY_DEGREE, ascending (bottom-up
-    // levels scan their in-edges with a whole warp instead of one thread)
-    int32_t *heavy = nullptr;
-    int32_t nheavy = 0;
-    // vertices with BU_LIGHT_DEGREE < in-degree <= BU_HEAVY_DEGREE, ascending
-    int32_t *mid = nullptr;
-    int32_t nmid = 0;
+    // bottom-up degree classes by in-degree, each ascending: light (1 ..
+    // BU_LIGHT_DEGREE), mid (.. BU_MID_DEGREE), wide (.. BU_HEAVY_DEGREE),
+    // heavy (above)
+    int32_t *light = nullptr, *mid = nullptr, *wide = nullptr, *heavy = nullptr;
+    int32_t nlight = 0, nmid = 0, nwide = 0, nheavy = 0;
     size_t bytes = 0;
     std::mutex mu;  // serialises calls on one handle (workspace reuse)
     Workspace ws;  // kernel scratch
@@ -139,6 +140,7 @@ struct MsOptions {
     int batch_words = 1;  // 64-source words per batch
     float alpha = 2.f;    // top-down -> bottom-up when frontier out-edges > m / alpha
     float beta = 24.f;    // bottom-up -> top-down when frontier vertices < n / beta
+    float gamma = 4.f;    // ... or when frontier out-edges < n / gamma
     Workspace *ws = nullptr;  // scratch to use (default: the graph's)
     int max_blocks = 0;       // cap on the persistent grid (0: the whole GPU)
     bool timed = true;        // record the graph's launch events

@@ -30,7 +30,9 @@
 // A source is active while its frontier is non-empty; the active mask of F_j is
 // OR-reduced per CTA in shared memory during phase j.  Direction: top-down ->
 // bottom-up when the frontier's out-edges exceed m / alpha, back when it holds
-// fewer than n / beta vertices (after Beamer, Asanovic, Patterson, SC'12).
+// fewer than n / beta vertices (after Beamer, Asanovic, Patterson, SC'12) or
+// its out-edges are fewer than n / gamma (a wide frontier of low-degree
+// vertices: expanding it costs less than one sweep over all vertices).
 //
 // Top-down gather strategies restate the reference kernels' neighbour gathering
 // (file:line in include/gu.h); AUTO uses the edge-balanced merge-path gather.
@@ -99,11 +101,12 @@ struct MsArgs {
     const int32_t *__restrict__ RT;
     const int32_t *__restrict__ CT;
     const int32_t *__restrict__ F;
-    const int32_t *__restrict__ heavy;
+    const int32_t *__restrict__ light;  // bottom-up degree classes (ascending vertex lists)
     const int32_t *__restrict__ mid;
+    const int32_t *__restrict__ wide;
+    const int32_t *__restrict__ heavy;
     int32_t n;
-    int32_t nheavy;
-    int32_t nmid;
+    int32_t nlight, nmid, nwide, nheavy;
     int64_t m;
     const int32_t *sources;
     int32_t k;
@@ -117,7 +120,7 @@ struct MsArgs {
     int32_t *q[3];
     int32_t *qoff[3];
     MsCtl *ctl;
-    float alpha, beta;
+    float alpha, beta, gamma;
     int degbits;
 };
 
@@ -267,15 +270,15 @@ struct GlobalQ {  // straight into the level's queue, one 64-bit atomic per warp
 };
 
 // Per-CTA collection in shared memory, appended to the level's queue by
-// cta_flush with one 64-bit atomic per flush: the queue counter is a single
-// address, and one atomic per warp from every warp of the GPU serialises there
-// when a level discovers 10^5..10^6 vertices.  Pushes beyond the capacity go to
-// the queue directly.
-constexpr int CQ_CAP = 2048;
-constexpr int CQ_PER_THREAD = CQ_CAP / MS_THREADS;
+// cta_flush with one 64-bit atomic per 2048 vertices: the queue counter is a
+// single address, and one atomic per warp from every warp of the GPU
+// serialises there when a level discovers 10^5..10^6 vertices.  Pushes beyond
+// the capacity go to the queue directly.
+constexpr int CQ_PER_THREAD = 4;
 struct CtaQ {
-    int32_t *v;  // [CQ_CAP] shared
-    int *n;      // shared: pushes since the last flush (the excess over CQ_CAP went direct)
+    int32_t *v;  // [cap] shared
+    int *n;      // shared: pushes since the last flush (the excess over cap went direct)
+    int cap;
     __device__ __forceinline__ void push(const MsArgs &a, const Lvl &L, int32_t w) const
     {
         const unsigned mask = __activemask();
@@ -284,17 +287,31 @@ struct CtaQ {
         if (lane_id() == leader) base = atomicAdd(n, __popc(mask));
         base = __shfl_sync(mask, base, leader);
         const int pos = base + __popc(mask & lanemask_lt());
-        if (pos < CQ_CAP) v[pos] = w;
+        if (pos < cap) v[pos] = w;
         else append_vertex(a, L.slot, L.qnxt, L.qnxt_off, w);
     }
 };
 
+// The CTA's queue counter and flush scratch (zeroed at kernel start; every
+// flush leaves the counter at zero).
+__device__ __forceinline__ int *cq_count()
+{
+    __shared__ int n;
+    return &n;
+}
+__device__ __forceinline__ u64 *cq_scan()
+{
+    __shared__ u64 scan[33];
+    return scan;
+}
+
 // Append the CTA's collected vertices to the level's queue: degrees scanned
 // across the CTA, one atomic reserves the slots and the edge range.  Every
 // thread of the CTA calls it after a __syncthreads (the count is then uniform).
-__device__ void cta_flush(const MsArgs &a, const Lvl &L, const CtaQ &cq, u64 *s_scan /* [33] */)
+__device__ void cta_flush(const MsArgs &a, const Lvl &L, const CtaQ &cq)
 {
-    const int cnt = min(*cq.n, CQ_CAP);
+    u64 *s_scan = cq_scan();
+    const int cnt = min(*cq.n, cq.cap);
     const int lane = lane_id(), warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const int per_round = blockDim.x * CQ_PER_THREAD;
     for (int r0 = 0; r0 < cnt; r0 += per_round) {
@@ -696,7 +713,8 @@ __device__ __forceinline__ int owner_search_warp(const int32_t *off, int lo, int
 // the shared capacity (many tiny lists) are walked owner by owner.
 constexpr int MP_TASK = MS_THREADS * 8;
 constexpr int MP_STAGE = 1024;
-static_assert(3 * MP_STAGE * 4 + CQ_CAP * 4 <= MS_SMEM_BYTES, "merge-path staging exceeds the shared buffer");
+constexpr int MP_QUEUE = 2048;  // discovered-vertex queue after the staging
+static_assert(3 * MP_STAGE * 4 + MP_QUEUE * 4 <= MS_SMEM_BYTES, "merge-path staging exceeds the shared buffer");
 
 template <int W, class G>
 __device__ void gather_mp(const MsArgs &a, const Lvl &L)
@@ -704,14 +722,10 @@ __device__ void gather_mp(const MsArgs &a, const Lvl &L)
     int32_t *s_off = reinterpret_cast<int32_t *>(ms_smem());
     int32_t *s_v = s_off + MP_STAGE;
     int32_t *s_r = s_v + MP_STAGE;
-    int32_t *s_cq = s_r + MP_STAGE;  // [CQ_CAP]
     __shared__ int s_k[2];
-    __shared__ int s_cqn;
-    __shared__ u64 s_scan[33];
     const long long E = L.qedges;
     if (E == 0) return;
-    const CtaQ cq{s_cq, &s_cqn};
-    if (threadIdx.x == 0) s_cqn = 0;
+    const CtaQ cq{s_r + MP_STAGE, cq_count(), MP_QUEUE};
     const long long per_blk = (E + G::nblk() - 1) / G::nblk();
     const long long task = min((long long)MP_TASK, max(32ll, (per_blk + 31) & ~31ll));
     const long long ntask = (E + task - 1) / task;
@@ -749,12 +763,20 @@ __device__ void gather_mp(const MsArgs &a, const Lvl &L)
                     else hi2 = mid - 1;
                 }
                 const bool has2 = e2 < e1;
-                u64 f[W], f2[W];
+                u64 f[W];
                 load_front<W>(L, s_v[lo], f);
-                if (has2) load_front<W>(L, s_v[lo2], f2);
                 const int32_t w = __ldg(a.C + s_r[lo] + (int32_t)(e - s_off[lo]));
                 const int32_t w2 = has2 ? __ldg(a.C + s_r[lo2] + (int32_t)(e2 - s_off[lo2])) : -1;
-                td_visit2<W>(a, L, f, w, f2, w2, cq);
+                if (!has2 || lo2 == lo) {
+                    // both slots in one adjacency list (the common case: frontier
+                    // hubs): one frontier word group, both visits' loads together
+                    td_visit2<W>(a, L, f, w, f, w2, cq);
+                } else {
+                    td_visit<W>(a, L, f, w, cq);
+                    u64 f2[W];
+                    load_front<W>(L, s_v[lo2], f2);
+                    td_visit<W>(a, L, f2, w2, cq);
+                }
             }
         } else {
             for (int i = threadIdx.x; i < nk; i += blockDim.x) {
@@ -769,16 +791,21 @@ __device__ void gather_mp(const MsArgs &a, const Lvl &L)
             }
         }
         __syncthreads();
-        if (s_cqn > CQ_CAP / 2) cta_flush(a, L, cq, s_scan);
+        if (*cq.n > cq.cap / 2) cta_flush(a, L, cq);
     }
     __syncthreads();
-    if (s_cqn > 0) cta_flush(a, L, cq, s_scan);
+    if (*cq.n > 0) cta_flush(a, L, cq);
 }
 
-// Bottom-up level: every vertex (coalesced sweep) finalises its own F_{j-1}
-// bits and clears F_{j-2}; a light vertex still missing an active source ORs
-// its in-neighbours' F_{j-1} words itself (four independent loads in flight),
-// stopping once every missing active source is found.
+// Bottom-up level.  Each vertex with in-edges belongs to one degree class
+// (light, mid, wide, heavy; vertices without in-edges are never discovered
+// after level 0 and are in none).  The pass of its class finalises its
+// F_{j-1} bits, clears its F_{j-2} words and, while it still misses an active
+// source, ORs its in-neighbours' F_{j-1} words.  The light, mid and wide
+// passes take a vertex's in-neighbours in at most two rounds of loads issued
+// together (no loop: lanes of a warp never diverge over trip counts); the
+// heavy pass steps through the in-edges.  The mid, wide and heavy passes stop
+// once every missing active source is found.
 template <int W>
 __device__ __forceinline__ bool covers(const u64 (&acc)[W], const u64 (&need)[W])
 {
@@ -797,143 +824,236 @@ __device__ __forceinline__ void or_front(const Lvl &L, int32_t v, u64 (&acc)[W])
     for (int q = 0; q < W; ++q) acc[q] |= x[q];
 }
 
-template <int W, class G>
-__device__ void bu_sweep(const MsArgs &a, const Lvl &L)
+// The class pass's own-vertex step: returns the sources still missing.
+template <int W>
+__device__ __forceinline__ void bu_own(const MsArgs &a, const Lvl &L, size_t o, u64 (&act)[W], u64 (&need)[W])
 {
-    const long long size = G::size();
+    u64 s[W], f[W];
+    ldw<W>(a.seen + o, s);
+    ldw<W>(L.fcur + o, f);
+#pragma unroll
+    for (int q = 0; q < W; ++q) need[q] = L.active[q] & ~(s[q] | f[q]);
+    if (anyw<W>(f)) {
+        finalise<W>(a, L.lev, o, f, s);
+#pragma unroll
+        for (int q = 0; q < W; ++q) act[q] |= f[q];
+    }
+    zerow<W>(L.fprv + o);
+}
+
+template <int W>
+__device__ __forceinline__ void bu_found(const MsArgs &a, const Lvl &L, const CtaQ &cq, int32_t w,
+                                         const u64 (&acc)[W], const u64 (&need)[W])
+{
+    u64 nb[W];
+#pragma unroll
+    for (int q = 0; q < W; ++q) nb[q] = acc[q] & need[q];
+    if (anyw<W>(nb)) {
+        stw<W>(L.fnxt + (size_t)w * W, nb);
+        cq.push(a, L, w);
+    }
+}
+
+// Vertices of a class per warp step: the class spread over every warp, at most
+// one per lane.  Each lane runs the own-vertex step of one vertex; the warp
+// then scans only the vertices that still miss a source.
+__device__ __forceinline__ long long class_chunk(long long count, long long nwarps)
+{
+    return max(1ll, min(32ll, (count + nwarps - 1) / nwarps));
+}
+
+// Light: one thread per vertex, up to BU_LIGHT_DEGREE loads in flight.
+template <int W, class G>
+__device__ void bu_light(const MsArgs &a, const Lvl &L, const CtaQ &cq)
+{
     u64 act[W] = {};
-    for (long long wl = G::rank(); wl < a.n; wl += size) {
-        const int32_t w = (int32_t)wl;
-        const size_t o = (size_t)w * W;
-        u64 s[W], f[W];
-        ldw<W>(a.seen + o, s);
-        ldw<W>(L.fcur + o, f);
-        if (anyw<W>(f)) {
-            finalise<W>(a, L.lev, o, f, s);
-#pragma unroll
-            for (int q = 0; q < W; ++q) act[q] |= f[q];
-        }
-        zerow<W>(L.fprv + o);
+    const long long size = G::size();
+    for (long long i = G::rank(); i < a.nlight; i += size) {
+        const int32_t w = __ldg(a.light + i);
         u64 need[W];
-#pragma unroll
-        for (int q = 0; q < W; ++q) need[q] = L.active[q] & ~s[q];
+        bu_own<W>(a, L, (size_t)w * W, act, need);
         if (!anyw<W>(need)) continue;
         const int32_t e0 = __ldg(a.RT + w), e1 = __ldg(a.RT + w + 1);
-        if (e1 - e0 > BU_LIGHT_DEGREE || e1 == e0) continue;  // mid / heavy classes: bu_mid, bu_heavy
+        int32_t c[BU_LIGHT_DEGREE];
+#pragma unroll
+        for (int t = 0; t < BU_LIGHT_DEGREE; ++t) c[t] = e0 + t < e1 ? __ldg(a.CT + e0 + t) : -1;
         u64 acc[W] = {};
-        {  // at most BU_LIGHT_DEGREE (8) in-neighbours: all loads in flight at once
-            int32_t c[BU_LIGHT_DEGREE];
 #pragma unroll
-            for (int t = 0; t < BU_LIGHT_DEGREE; ++t) c[t] = e0 + t < e1 ? __ldg(a.CT + e0 + t) : -1;
+        for (int t = 0; t < BU_LIGHT_DEGREE; ++t)
+            if (c[t] >= 0) or_front<W>(L, c[t], acc);
+        bu_found<W>(a, L, cq, w, acc, need);
+    }
+    flush_active<W>(L, act);
+}
+
+template <int W>
+__device__ __forceinline__ void shfl_words(const u64 (&x)[W], u64 (&y)[W], int src)
+{
 #pragma unroll
-            for (int t = 0; t < BU_LIGHT_DEGREE; ++t)
-                if (c[t] >= 0) or_front<W>(L, c[t], acc);
-        }
-        u64 nb[W];
+    for (int q = 0; q < W; ++q) y[q] = __shfl_sync(FULL_MASK, x[q], src);
+}
+
+// Mid: after the own-vertex steps, eight lanes per needy vertex (four at a
+// time).  First the eight highest-degree in-neighbours (one load per lane),
+// which at the later levels usually cover every missing source; then, only
+// where they do not, the rest (up to three more loads per lane, in flight
+// together).  The group's words are OR-ed with xor shuffles inside the group;
+// no loop per vertex, so the four groups of a warp never diverge.
+template <int W>
+__device__ __forceinline__ void group8_or(u64 (&x)[W])
+{
 #pragma unroll
-        for (int q = 0; q < W; ++q) nb[q] = acc[q] & need[q];
-        if (anyw<W>(nb)) {
-            stw<W>(L.fnxt + o, nb);
-            append_vertex(a, L.slot, L.qnxt, L.qnxt_off, w);
+    for (int q = 0; q < W; ++q) {
+#pragma unroll
+        for (int off = 1; off < 8; off <<= 1) x[q] |= __shfl_xor_sync(FULL_MASK, x[q], off);
+    }
+}
+
+template <int W, class G>
+__device__ void bu_mid(const MsArgs &a, const Lvl &L, const CtaQ &cq)
+{
+    static_assert(BU_LIGHT_DEGREE >= 7, "mid class: the first round gives every lane an in-edge");
+    static_assert(BU_MID_DEGREE <= 8 * 4, "mid class: at most four in-edges per lane");
+    u64 act[W] = {};
+    const int lane = lane_id(), sub = lane & 7, grp = lane >> 3;
+    const long long nw = G::size() >> 5, chunk = class_chunk(a.nmid, nw);
+    for (long long base = (G::rank() >> 5) * chunk; base < a.nmid; base += nw * chunk) {  // warp-uniform
+        const bool valid = lane < chunk && base + lane < a.nmid;
+        const int32_t mine = valid ? __ldg(a.mid + base + lane) : 0;
+        u64 need_l[W] = {};
+        if (valid) bu_own<W>(a, L, (size_t)mine * W, act, need_l);
+        unsigned todo = __ballot_sync(FULL_MASK, anyw<W>(need_l));
+        while (todo) {  // warp-uniform
+            unsigned t = todo;
+            for (int k = 0; k < grp && t; ++k) t &= t - 1;  // this group's needy lane: the grp-th set bit
+            const int src = t ? __ffs(t) - 1 : 0;
+            const bool has = t != 0;
+            for (int k = 0; k < 4 && todo; ++k) todo &= todo - 1;
+            const int32_t w = __shfl_sync(FULL_MASK, mine, src);
+            u64 need[W];
+            shfl_words<W>(need_l, need, src);
+            u64 acc[W] = {};
+            int32_t e0 = 0, e1 = 0;
+            if (has) {
+                e0 = __ldg(a.RT + w);
+                e1 = __ldg(a.RT + w + 1);
+                or_front<W>(L, __ldg(a.CT + e0 + sub), acc);  // in-degree > 8: every lane has one
+            }
+            group8_or<W>(acc);
+            const bool more = has && !covers<W>(acc, need);
+            if (__any_sync(FULL_MASK, more)) {
+                u64 x[W] = {};
+                if (more) {
+                    int32_t c[3];
+#pragma unroll
+                    for (int r = 0; r < 3; ++r)
+                        c[r] = e0 + 8 * (r + 1) + sub < e1 ? __ldg(a.CT + e0 + 8 * (r + 1) + sub) : -1;
+#pragma unroll
+                    for (int r = 0; r < 3; ++r)
+                        if (c[r] >= 0) or_front<W>(L, c[r], x);
+                }
+                group8_or<W>(x);
+#pragma unroll
+                for (int q = 0; q < W; ++q) acc[q] |= x[q];
+            }
+            if (has && sub == 0) bu_found<W>(a, L, cq, w, acc, need);
         }
     }
     flush_active<W>(L, act);
 }
 
-// Mid-degree vertices (BU_LIGHT_DEGREE < in-degree <= BU_HEAVY_DEGREE): eight
-// lanes per vertex OR 32 in-neighbours per step (four loads in flight per lane);
-// the group stops once every missing active source is found.
+// Wide: after the own-vertex steps, a warp per needy vertex: the 32
+// highest-degree in-neighbours first, then, only if they leave a missing
+// source uncovered, the rest (up to three more loads per lane, in flight
+// together).
 template <int W, class G>
-__device__ void bu_mid(const MsArgs &a, const Lvl &L)
+__device__ void bu_wide(const MsArgs &a, const Lvl &L, const CtaQ &cq)
 {
+    static_assert(BU_MID_DEGREE >= 31, "wide class: the first round gives every lane an in-edge");
+    static_assert(BU_HEAVY_DEGREE <= 32 * 4, "wide class: at most four in-edges per lane");
+    u64 act[W] = {};
     const int lane = lane_id();
-    const int sub = lane & 7;
-    const unsigned gmask = 0xFFu << (lane & ~7);
-    const long long ngroups = G::size() >> 3;
-    for (long long i = G::rank() >> 3; i < a.nmid; i += ngroups) {
-        const int32_t w = __ldg(a.mid + i);
-        const size_t o = (size_t)w * W;
-        u64 s[W], f[W], need[W];
-        ldw<W>(a.seen + o, s);
-        ldw<W>(L.fcur + o, f);
+    const long long nw = G::size() >> 5, chunk = class_chunk(a.nwide, nw);
+    for (long long base = (G::rank() >> 5) * chunk; base < a.nwide; base += nw * chunk) {  // warp-uniform
+        const bool valid = lane < chunk && base + lane < a.nwide;
+        const int32_t mine = valid ? __ldg(a.wide + base + lane) : 0;
+        u64 need_l[W] = {};
+        if (valid) bu_own<W>(a, L, (size_t)mine * W, act, need_l);
+        unsigned todo = __ballot_sync(FULL_MASK, anyw<W>(need_l));
+        while (todo) {  // warp-uniform
+            const int src = __ffs(todo) - 1;
+            todo &= todo - 1;
+            const int32_t w = __shfl_sync(FULL_MASK, mine, src);
+            u64 need[W];
+            shfl_words<W>(need_l, need, src);
+            const int32_t e0 = __ldg(a.RT + w), e1 = __ldg(a.RT + w + 1);
+            u64 acc[W] = {};
+            or_front<W>(L, __ldg(a.CT + e0 + lane), acc);  // in-degree > 32: every lane has one
 #pragma unroll
-        for (int q = 0; q < W; ++q) need[q] = L.active[q] & ~(s[q] | f[q]);
-        if (!anyw<W>(need)) continue;
-        const int32_t e0 = __ldg(a.RT + w), e1 = __ldg(a.RT + w + 1);
-        u64 acc[W] = {};
-        {  // first step: the 8 highest-degree in-neighbours, which most often cover everything
-            u64 x[W] = {};
-            if (e0 + sub < e1) or_front<W>(L, __ldg(a.CT + e0 + sub), x);
+            for (int q = 0; q < W; ++q) acc[q] = warp_or_u64(FULL_MASK, acc[q]);
+            if (!covers<W>(acc, need)) {
+                int32_t c[3];
 #pragma unroll
-            for (int q = 0; q < W; ++q) acc[q] |= warp_or_u64(gmask, x[q]);
-        }
-        for (int32_t eb = e0 + 8; eb < e1 && !covers<W>(acc, need); eb += 32) {  // then 32 per step, 4 per lane
-            u64 x[W] = {};
-            int32_t c[4];
+                for (int r = 0; r < 3; ++r)
+                    c[r] = e0 + 32 * (r + 1) + lane < e1 ? __ldg(a.CT + e0 + 32 * (r + 1) + lane) : -1;
+                u64 x[W] = {};
 #pragma unroll
-            for (int t = 0; t < 4; ++t) c[t] = eb + 8 * t + sub < e1 ? __ldg(a.CT + eb + 8 * t + sub) : -1;
+                for (int r = 0; r < 3; ++r)
+                    if (c[r] >= 0) or_front<W>(L, c[r], x);
 #pragma unroll
-            for (int t = 0; t < 4; ++t)
-                if (c[t] >= 0) or_front<W>(L, c[t], x);
-#pragma unroll
-            for (int q = 0; q < W; ++q) acc[q] |= warp_or_u64(gmask, x[q]);
-            if (covers<W>(acc, need)) break;
-        }
-        u64 nb[W];
-#pragma unroll
-        for (int q = 0; q < W; ++q) nb[q] = acc[q] & need[q];
-        if (sub == 0 && anyw<W>(nb)) {
-            stw<W>(L.fnxt + o, nb);
-            append_vertex(a, L.slot, L.qnxt, L.qnxt_off, w);
+                for (int q = 0; q < W; ++q) acc[q] |= warp_or_u64(FULL_MASK, x[q]);
+            }
+            if (lane == 0) bu_found<W>(a, L, cq, w, acc, need);
         }
     }
+    flush_active<W>(L, act);
 }
 
-// Heavy vertices (in-degree > BU_HEAVY_DEGREE): a warp per vertex ORs 128
-// in-neighbours per step (four loads in flight per lane) and stops once every
-// missing active source is found.
+// Heavy (in-degree > BU_HEAVY_DEGREE): after the own-vertex steps, a warp per
+// needy vertex ORs 128 in-neighbours per step (four loads in flight per lane),
+// the 32 highest-degree ones first, and stops once every missing active source
+// is found.
 template <int W, class G>
-__device__ void bu_heavy(const MsArgs &a, const Lvl &L)
+__device__ void bu_heavy(const MsArgs &a, const Lvl &L, const CtaQ &cq)
 {
+    u64 act[W] = {};
     const int lane = lane_id();
-    const long long nw = G::size() >> 5;
-    for (long long i = G::rank() >> 5; i < a.nheavy; i += nw) {
-        const int32_t w = __ldg(a.heavy + i);
-        const size_t o = (size_t)w * W;
-        u64 s[W], f[W], need[W];
-        ldw<W>(a.seen + o, s);
-        ldw<W>(L.fcur + o, f);
+    const long long nw = G::size() >> 5, chunk = class_chunk(a.nheavy, nw);
+    for (long long base = (G::rank() >> 5) * chunk; base < a.nheavy; base += nw * chunk) {  // warp-uniform
+        const bool valid = lane < chunk && base + lane < a.nheavy;
+        const int32_t mine = valid ? __ldg(a.heavy + base + lane) : 0;
+        u64 need_l[W] = {};
+        if (valid) bu_own<W>(a, L, (size_t)mine * W, act, need_l);
+        unsigned todo = __ballot_sync(FULL_MASK, anyw<W>(need_l));
+        while (todo) {  // warp-uniform
+            const int src = __ffs(todo) - 1;
+            todo &= todo - 1;
+            const int32_t w = __shfl_sync(FULL_MASK, mine, src);
+            u64 need[W];
+            shfl_words<W>(need_l, need, src);
+            const int32_t e0 = __ldg(a.RT + w), e1 = __ldg(a.RT + w + 1);
+            u64 acc[W] = {};
+            {  // first step: the 32 highest-degree in-neighbours
+                u64 x[W] = {};
+                or_front<W>(L, __ldg(a.CT + e0 + lane), x);  // in-degree > 128
 #pragma unroll
-        for (int q = 0; q < W; ++q) need[q] = L.active[q] & ~(s[q] | f[q]);
-        if (!anyw<W>(need)) continue;
-        const int32_t e0 = __ldg(a.RT + w), e1 = __ldg(a.RT + w + 1);
-        u64 acc[W] = {};
-        {  // first step: the 32 highest-degree in-neighbours
-            u64 x[W] = {};
-            if (e0 + lane < e1) or_front<W>(L, __ldg(a.CT + e0 + lane), x);
+                for (int q = 0; q < W; ++q) acc[q] |= warp_or_u64(FULL_MASK, x[q]);
+            }
+            for (int32_t eb = e0 + 32; eb < e1 && !covers<W>(acc, need); eb += 128) {  // then 128 per step
+                u64 x[W] = {};
+                int32_t c[4];
 #pragma unroll
-            for (int q = 0; q < W; ++q) acc[q] |= warp_or_u64(FULL_MASK, x[q]);
-        }
-        for (int32_t eb = e0 + 32; eb < e1 && !covers<W>(acc, need); eb += 128) {  // then 128 per step
-            u64 x[W] = {};
-            int32_t c[4];
+                for (int r = 0; r < 4; ++r) c[r] = eb + 32 * r + lane < e1 ? __ldg(a.CT + eb + 32 * r + lane) : -1;
 #pragma unroll
-            for (int t = 0; t < 4; ++t) c[t] = eb + 32 * t + lane < e1 ? __ldg(a.CT + eb + 32 * t + lane) : -1;
+                for (int r = 0; r < 4; ++r)
+                    if (c[r] >= 0) or_front<W>(L, c[r], x);
 #pragma unroll
-            for (int t = 0; t < 4; ++t)
-                if (c[t] >= 0) or_front<W>(L, c[t], x);
-#pragma unroll
-            for (int q = 0; q < W; ++q) acc[q] |= warp_or_u64(FULL_MASK, x[q]);
-            if (covers<W>(acc, need)) break;
-        }
-        u64 nb[W];
-#pragma unroll
-        for (int q = 0; q < W; ++q) nb[q] = acc[q] & need[q];
-        if (lane == 0 && anyw<W>(nb)) {
-            stw<W>(L.fnxt + o, nb);
-            append_vertex(a, L.slot, L.qnxt, L.qnxt_off, w);
+                for (int q = 0; q < W; ++q) acc[q] |= warp_or_u64(FULL_MASK, x[q]);
+            }
+            if (lane == 0) bu_found<W>(a, L, cq, w, acc, need);
         }
     }
+    flush_active<W>(L, act);
 }
 
 // Distance rows of one batch from seen and the level bit-planes.
@@ -1065,6 +1185,7 @@ __global__ void __launch_bounds__(MS_THREADS, MS_MIN_BLOCKS) ms_grid_kernel(MsAr
     const long long rank = GridG::rank(), size = GridG::size();
     const size_t pstride = (size_t)a.n * W;
     if (threadIdx.x < MAXW) s_act[threadIdx.x] = 0;
+    if (threadIdx.x == 0) *cq_count() = 0;
     const int bsz = 64 * W;
     const int nbatch = (a.k + bsz - 1) / bsz;
     for (int b = 0; b < nbatch; ++b) {
@@ -1149,12 +1270,27 @@ __global__ void __launch_bounds__(MS_THREADS, MS_MIN_BLOCKS) ms_grid_kernel(MsAr
                 bu = j > 1;
             } else if (VARIANT == GU_BFS_AUTO) {
                 if (!prev_bu) bu = j > 1 && (double)L.qedges * (double)a.alpha > (double)a.m;
-                else bu = (double)L.qlen * (double)a.beta > (double)a.n;
+                else bu = (double)L.qlen * (double)a.beta > (double)a.n &&
+                          (double)L.qedges * (double)a.gamma > (double)a.n;
             }
             if (bu) {
-                bu_sweep<W, GridG>(a, L);
-                if (a.nmid) bu_mid<W, GridG>(a, L);
-                if (a.nheavy) bu_heavy<W, GridG>(a, L);
+                // F_0 may hold sources without in-edges, which no class pass visits
+                if (j == 2 && rank < nb) zerow<W>(L.fprv + (size_t)__ldg(a.sources + row0 + rank) * W);
+                // sub-stage stamps (kinds 5, 6): when warp 0 of the slowest CTA finished
+                // the light class and the mid + wide classes
+                // discovered vertices collect in the CTA's shared queue (the whole
+                // staging buffer), flushed to the level's queue at the end
+                const CtaQ cq{reinterpret_cast<int32_t *>(ms_smem()), cq_count(), MS_SMEM_BYTES / 4};
+                bu_light<W, GridG>(a, L, cq);
+                if (threadIdx.x == 0) record_event(ctl, ev_idx, rank == 0, b, j, 5, L.qlen, L.qedges);
+                ++ev_idx;
+                bu_mid<W, GridG>(a, L, cq);
+                bu_wide<W, GridG>(a, L, cq);
+                if (threadIdx.x == 0) record_event(ctl, ev_idx, rank == 0, b, j, 6, L.qlen, L.qedges);
+                ++ev_idx;
+                bu_heavy<W, GridG>(a, L, cq);
+                __syncthreads();
+                if (*cq.n > 0) cta_flush(a, L, cq);
             } else {
                 td_update<W, GridG>(a, L);
                 if (VARIANT == GU_BFS_EDGE) gather_edge<W, GridG>(a, L);
@@ -1272,11 +1408,15 @@ void launch_msbfs(DeviceGraph &g, const int32_t *sources, int32_t k, int32_t *di
     a.RT = g.RT;
     a.CT = g.CT;
     a.F = g.F;
+    a.light = g.light;
+    a.mid = g.mid;
+    a.wide = g.wide;
     a.heavy = g.heavy;
     a.n = g.n;
-    a.nheavy = g.nheavy;
-    a.mid = g.mid;
+    a.nlight = g.nlight;
     a.nmid = g.nmid;
+    a.nwide = g.nwide;
+    a.nheavy = g.nheavy;
     a.m = g.m;
     a.sources = sources;
     a.k = k;
@@ -1304,6 +1444,7 @@ void launch_msbfs(DeviceGraph &g, const int32_t *sources, int32_t k, int32_t *di
     }
     a.alpha = env_float("GU_MS_ALPHA", opt.alpha);
     a.beta = env_float("GU_MS_BETA", opt.beta);
+    a.gamma = env_float("GU_MS_GAMMA", opt.gamma);
     int degbits = 1;
     while (degbits < 31 && (1ll << degbits) <= (long long)g.max_degree) ++degbits;
     a.degbits = degbits;
@@ -1473,11 +1614,9 @@ static void bfs_noalloc(const int32_t *R, const int32_t *C, int32_t n, int64_t m
     a.RT = R;  // never read: top-down levels only
     a.CT = C;
     a.F = nullptr;
-    a.heavy = nullptr;
-    a.mid = nullptr;
+    a.light = a.mid = a.wide = a.heavy = nullptr;  // top-down levels only
     a.n = n;
-    a.nheavy = 0;
-    a.nmid = 0;
+    a.nlight = a.nmid = a.nwide = a.nheavy = 0;
     a.m = m;
     a.sources = sources;
     a.k = k;
@@ -1505,6 +1644,7 @@ static void bfs_noalloc(const int32_t *R, const int32_t *C, int32_t n, int64_t m
     }
     a.alpha = 0.f;  // never switch to bottom-up
     a.beta = 24.f;
+    a.gamma = 4.f;
     int degbits = 1;
     while (degbits < 31 && (1ll << degbits) <= (long long)m) ++degbits;
     a.degbits = degbits;

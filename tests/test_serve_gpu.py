@@ -83,7 +83,7 @@ def test_results_alone_and_in_the_mix(graphs):
     assert all(x is not None and x >= 0 for x in lat)
     st = srv.stats()
     assert st["completed"] == len(plan)
-    assert st["batches"] < len(plan), st  # requests were merged into shared batches
+    assert st["batches"] <= len(plan), st
     for i, (kind, gname, srcs, _) in enumerate(plan):
         g = graphs[gname]
         out = results[i][1]
@@ -97,6 +97,26 @@ def test_results_alone_and_in_the_mix(graphs):
             ref = lone_bc(g, srcs)
             rel = np.abs(out - ref) / np.maximum(np.abs(ref), 1e-300)
             assert np.all((rel <= 1e-12) | (np.abs(out - ref) == 0)), f"request {i}: {rel.max()}"
+    srv.close()
+
+
+def test_queued_requests_share_a_batch(graphs):
+    """With one slot, requests submitted while a batch runs are merged into the next one."""
+    g = graphs["rmat13"]
+    srv = gu.Server(hbm_budget_bytes=16 << 30, slots=1, max_batch=256)
+    rng = np.random.default_rng(11)
+    reqs = []
+    for i in range(48):
+        srcs = rng.choice(g.n, size=4, replace=False).astype(np.int32)
+        out = np.empty((4, g.n), np.int32)
+        reqs.append((srv.submit(g, gu.QUERY_BFS, srcs, out), srcs, out))
+    for rid, _, _ in reqs:
+        srv.wait(rid)
+    st = srv.stats()
+    assert st["completed"] == len(reqs)
+    assert st["batches"] < len(reqs), st  # the burst did not run one request per batch
+    for _, srcs, out in reqs:
+        np.testing.assert_array_equal(out, lone_bfs(g, srcs))
     srv.close()
 
 
