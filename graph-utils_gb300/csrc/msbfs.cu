@@ -1059,10 +1059,14 @@ __device__ void bu_heavy(const MsArgs &a, const Lvl &L, const CtaQ &cq)
 // Distance rows of one batch from seen and the level bit-planes.
 //
 // Fast path (levels < 256, 16-byte aligned rows): a CTA takes a tile of
-// blockDim consecutive vertices and one 64-source word; each thread decodes its
-// vertex's levels 16 rows at a time into a shared [16][blockDim] tile, and the
-// CTA writes each row's segment (2 KiB for 512 vertices) with contiguous int4
-// stores.  Otherwise lanes hold consecutive vertices and store one int each.
+// blockDim / W consecutive vertices and all W words of each, thread (vertex,
+// word) reading its seen and plane words coalesced (consecutive threads,
+// consecutive words); the next tile's words are loaded while this one is
+// written.  Each thread decodes 16 rows of its word per round into a shared
+// [16 W][blockDim / W] tile (columns rotated by word so a warp's stores hit 32
+// distinct banks), and the CTA writes each row's segment (512 bytes for W = 4)
+// with contiguous int4 stores.  Otherwise lanes hold consecutive vertices and
+// store one int each.
 constexpr int WD_ROWS = 16;
 static_assert(WD_ROWS * MS_THREADS * 4 <= MS_SMEM_BYTES, "distance tile exceeds the shared buffer");
 
@@ -1081,32 +1085,164 @@ __device__ __forceinline__ u64 transpose8x8(u64 x)
     return x;
 }
 
+// 8x8 bit-matrix transpose on two 32-bit words: rows 0-3 are the bytes of x,
+// rows 4-7 those of y; afterwards byte c (of x for c < 4, of y for c >= 4)
+// holds column c.  The three stages of transpose8x8, the first two inside
+// each word and the third exchanging nibbles between the words.
+__device__ __forceinline__ void transpose8x8_32(uint32_t &x, uint32_t &y)
+{
+    uint32_t t;
+    t = (x ^ (x >> 7)) & 0x00AA00AAu;
+    x ^= t ^ (t << 7);
+    t = (y ^ (y >> 7)) & 0x00AA00AAu;
+    y ^= t ^ (t << 7);
+    t = (x ^ (x >> 14)) & 0x0000CCCCu;
+    x ^= t ^ (t << 14);
+    t = (y ^ (y >> 14)) & 0x0000CCCCu;
+    y ^= t ^ (t << 14);
+    t = (x ^ (y << 4)) & 0xF0F0F0F0u;
+    x ^= t;
+    y ^= t >> 4;
+}
+
+// Distance rows of a batch whose levels fit in four planes (levels < 16, the
+// common case).  Tiles of 256 / W consecutive vertices (all W words each) go
+// through a double-buffered shared byte tile: while the upper half of the CTA
+// writes tile i-1 to the rows, the lower half decodes tile i, so the row
+// stores stream without waiting for the decode.  A decoding thread (vertex,
+// word q) reads its seen and plane words coalesced (the next tile's words are
+// loaded while this one is decoded); for each group of eight sources it
+// gathers byte g of the four planes into x and byte g of ~seen, four times,
+// into y, and after the bit transpose byte c holds the source's level in the
+// low nibble and 0xF in the high nibble if the source never reached the
+// vertex.  The bytes fill a [64 W rows][256 / W] tile (columns rotated by word
+// so a warp's stores hit distinct banks); the writing half widens four bytes
+// at a time (unreached -> INT_MAX) into int4 streaming stores.
+template <int W, class G>
+__device__ void write_distances_nibble(const MsArgs &a, int row0, int nb)
+{
+    constexpr int HALF = MS_THREADS / 2;
+    constexpr int TV = HALF / W;  // vertices per tile
+    constexpr int ROWS = 64 * W;
+    constexpr int TILE = ROWS * TV;
+    constexpr int SWZ = 32 / W;   // byte rotation per word
+    static_assert(2 * TILE <= MS_SMEM_BYTES, "byte tiles exceed the shared buffer");
+    unsigned char *tiles = ms_smem();
+    const size_t pstride = (size_t)a.n * W;
+    const bool decoder = threadIdx.x < HALF;
+    const int tid = decoder ? threadIdx.x : threadIdx.x - HALF;
+    const int q = tid % W, vl = tid / W;
+    const int nq = (nb + 63) / 64;
+    const long long ntile = ((long long)a.n + TV - 1) / TV;
+    const int col = (vl + SWZ * q) % TV;
+    auto load = [&](long long t, u64 &s, u64 (&pl)[4]) {
+        const int32_t v = (int32_t)(t * TV) + vl;
+        const bool valid = decoder && t < ntile && v < a.n && q < nq;
+        const size_t o = (size_t)v * W + q;
+        s = valid ? __ldcs(a.seen + o) : 0ull;
+#pragma unroll
+        for (int b = 0; b < 4; ++b) pl[b] = (b < a.nplanes && valid) ? __ldcs(a.plane + b * pstride + o) : 0ull;
+    };
+    u64 s, pl[4];
+    load(G::blk(), s, pl);
+    for (long long i = 0;; ++i) {  // block-uniform
+        const long long td = G::blk() + i * G::nblk(), ts = td - G::nblk();
+        if (ts >= ntile) break;
+        if (decoder) {
+            if (td < ntile) {
+                u64 s_n, pl_n[4];
+                load(td + G::nblk(), s_n, pl_n);
+                unsigned char *tile = tiles + (i & 1) * TILE;
+#pragma unroll
+                for (int g = 0; g < 8; ++g) {
+                    const int bi = g & 3;
+                    const uint32_t h0 = (uint32_t)(pl[0] >> (g < 4 ? 0 : 32)), h1 = (uint32_t)(pl[1] >> (g < 4 ? 0 : 32));
+                    const uint32_t h2 = (uint32_t)(pl[2] >> (g < 4 ? 0 : 32)), h3 = (uint32_t)(pl[3] >> (g < 4 ? 0 : 32));
+                    const uint32_t ns = ~(uint32_t)(s >> (g < 4 ? 0 : 32));
+                    const uint32_t t01 = __byte_perm(h0, h1, bi | ((4 + bi) << 4));
+                    const uint32_t t23 = __byte_perm(h2, h3, bi | ((4 + bi) << 4));
+                    uint32_t x = __byte_perm(t01, t23, 0x5410);
+                    uint32_t y = __byte_perm(ns, 0u, bi * 0x1111);
+                    transpose8x8_32(x, y);
+                    unsigned char *dst = tile + (64 * q + 8 * g) * TV + col;
+#pragma unroll
+                    for (int c = 0; c < 4; ++c) {
+                        dst[c * TV] = (unsigned char)(x >> (8 * c));
+                        dst[(c + 4) * TV] = (unsigned char)(y >> (8 * c));
+                    }
+                }
+                s = s_n;
+#pragma unroll
+                for (int b = 0; b < 4; ++b) pl[b] = pl_n[b];
+            }
+        } else if (i > 0) {
+            const unsigned char *tile = tiles + ((i - 1) & 1) * TILE;
+            const int32_t vbase = (int32_t)(ts * TV);
+            const int nv = min(TV, a.n - vbase), nv4 = nv >> 2;
+            for (int k = tid; k < ROWS * (TV / 4); k += HALF) {
+                const int row = k / (TV / 4), c4 = k - row * (TV / 4);
+                if (row >= nb) continue;
+                const int sh = SWZ * (row >> 6);
+                const unsigned char *trow = tile + row * TV;
+                int32_t *drow = a.dist + (int64_t)(row0 + row) * a.ld + vbase;
+                if (c4 < nv4) {
+                    uint32_t w4 = *reinterpret_cast<const uint32_t *>(trow + (4 * c4 + sh) % TV);
+                    w4 |= (w4 >> 4) & 0x0F0F0F0Fu;  // unreached bytes 0xF0 -> 0xFF
+                    int4 o;
+                    o.x = (int32_t)(int8_t)(w4) & INT_MAX;
+                    o.y = (int32_t)(int8_t)(w4 >> 8) & INT_MAX;
+                    o.z = (int32_t)(int8_t)(w4 >> 16) & INT_MAX;
+                    o.w = (int32_t)(int8_t)(w4 >> 24) & INT_MAX;
+                    // streaming store: the rows are not read again by this kernel
+                    __stcs(reinterpret_cast<int4 *>(drow) + c4, o);
+                } else if (c4 == nv4) {
+                    for (int x = 4 * c4; x < nv; ++x) {
+                        const unsigned b = trow[(x + sh) % TV];
+                        drow[x] = (b & 0xF0u) ? INT_MAX : (int32_t)b;
+                    }
+                }
+            }
+        }
+        __syncthreads();
+    }
+}
+
 template <int W, class G>
 __device__ void write_distances(const MsArgs &a, int row0, int nb, int nplanes_used)
 {
-    int32_t(*tile)[MS_THREADS] = reinterpret_cast<int32_t(*)[MS_THREADS]>(ms_smem());
-    const int BD = blockDim.x;
-    if (nplanes_used <= 8 && (a.ld & 3) == 0 && (((uintptr_t)a.dist) & 15) == 0 && BD == MS_THREADS) {
+    if (nplanes_used <= 4 && (a.ld & 3) == 0 && (((uintptr_t)a.dist) & 15) == 0 && blockDim.x == MS_THREADS) {
+        write_distances_nibble<W, G>(a, row0, nb);
+        return;
+    }
+    if (nplanes_used <= 8 && (a.ld & 3) == 0 && (((uintptr_t)a.dist) & 15) == 0 && blockDim.x == MS_THREADS) {
+        constexpr int TV = MS_THREADS / W;  // vertices per tile
+        constexpr int SWZ = 32 / W;         // column rotation per word
+        int32_t *tile = reinterpret_cast<int32_t *>(ms_smem());  // [WD_ROWS * W][TV]
         const size_t pstride = (size_t)a.n * W;
-        const long long ntile = ((long long)a.n + BD - 1) / BD;
+        const int q = threadIdx.x % W, vl = threadIdx.x / W;
         const int nq = (nb + 63) / 64;
-        for (long long t = G::blk(); t < ntile * nq; t += G::nblk()) {
-            const int q = (int)(t % nq);
-            const int32_t vbase = (int32_t)((t / nq) * BD);
-            const int32_t v = vbase + threadIdx.x;
-            const bool valid = v < a.n;
+        const long long ntile = ((long long)a.n + TV - 1) / TV;
+        const int col = (vl + SWZ * q) % TV;
+        auto load = [&](long long t, u64 &s, u64 (&pl)[8]) {
+            const int32_t v = (int32_t)(t * TV) + vl;
+            const bool valid = t < ntile && v < a.n && q < nq;
             const size_t o = (size_t)v * W + q;
-            const u64 s = valid ? __ldcg(a.seen + o) : 0ull;
-            u64 pl[8];
+            s = valid ? __ldcs(a.seen + o) : 0ull;
 #pragma unroll
-            for (int b = 0; b < 8; ++b) pl[b] = (b < nplanes_used && valid) ? __ldcg(a.plane + b * pstride + o) : 0ull;
-            const int rows = min(64, nb - 64 * q);
-            const int nv = min(BD, a.n - vbase);  // vertices in this tile
-            for (int r0 = 0; r0 < rows; r0 += WD_ROWS) {
+            for (int b = 0; b < 8; ++b) pl[b] = (b < nplanes_used && valid) ? __ldcs(a.plane + b * pstride + o) : 0ull;
+        };
+        u64 s, pl[8];
+        load(G::blk(), s, pl);
+        for (long long t = G::blk(); t < ntile; t += G::nblk()) {
+            u64 s_n, pl_n[8];
+            load(t + G::nblk(), s_n, pl_n);  // next tile's words in flight during this one
+            const int32_t vbase = (int32_t)(t * TV);
+            const int nv = min(TV, a.n - vbase);
+            for (int r0 = 0; r0 < 64; r0 += WD_ROWS) {
 #pragma unroll
                 for (int h = 0; h < WD_ROWS / 8; ++h) {
-                    // sources 8g..8g+7: byte b of M = byte g of plane b; after an
-                    // 8x8 bit-matrix transpose byte c of M is the level of source 8g+c
+                    // sources 8g..8g+7 of word q: byte b of M = byte g of plane b; after
+                    // an 8x8 bit-matrix transpose byte c of M is the level of source 8g+c
                     const int g8 = (r0 >> 3) + h;
                     u64 M = 0;
 #pragma unroll
@@ -1115,23 +1251,31 @@ __device__ void write_distances(const MsArgs &a, int row0, int nb, int nplanes_u
                     const unsigned sb = (unsigned)(s >> (8 * g8)) & 0xFFu;
 #pragma unroll
                     for (int c = 0; c < 8; ++c)
-                        tile[8 * h + c][threadIdx.x] = ((sb >> c) & 1u) ? (int32_t)((M >> (8 * c)) & 0xFFull) : INT_MAX;
+                        tile[(WD_ROWS * q + 8 * h + c) * TV + col] =
+                            ((sb >> c) & 1u) ? (int32_t)((M >> (8 * c)) & 0xFFull) : INT_MAX;
                 }
                 __syncthreads();
-                const int nr = min(WD_ROWS, rows - r0);
                 const int nv4 = nv >> 2;
-                for (int k = threadIdx.x; k < nr * (BD >> 2); k += BD) {
-                    const int r = k / (BD >> 2), c4 = k - r * (BD >> 2);
-                    int32_t *drow = a.dist + (int64_t)(row0 + 64 * q + r0 + r) * a.ld + vbase;
+                for (int k = threadIdx.x; k < WD_ROWS * W * (TV / 4); k += MS_THREADS) {
+                    const int rr = k / (TV / 4), c4 = k - rr * (TV / 4);
+                    const int wq = rr / WD_ROWS, row = 64 * wq + r0 + (rr - wq * WD_ROWS);
+                    if (row >= nb) continue;
+                    int32_t *drow = a.dist + (int64_t)(row0 + row) * a.ld + vbase;
+                    const int32_t *trow = tile + rr * TV;
+                    const int sh = SWZ * wq;
                     if (c4 < nv4) {
                         // streaming store: the rows are not read again by this kernel
-                        __stcs(reinterpret_cast<int4 *>(drow) + c4, reinterpret_cast<const int4 *>(&tile[r][0])[c4]);
+                        __stcs(reinterpret_cast<int4 *>(drow) + c4,
+                               *reinterpret_cast<const int4 *>(trow + (4 * c4 + sh) % TV));
                     } else if (c4 == nv4) {
-                        for (int x = 4 * c4; x < nv; ++x) drow[x] = tile[r][x];
+                        for (int x = 4 * c4; x < nv; ++x) drow[x] = trow[(x + sh) % TV];
                     }
                 }
                 __syncthreads();
             }
+            s = s_n;
+#pragma unroll
+            for (int b = 0; b < 8; ++b) pl[b] = pl_n[b];
         }
         return;
     }
