@@ -336,8 +336,13 @@ __device__ void bc_rows_item(const BcArgs &a, int32_t w, int q, int row0, int nb
 __global__ void __launch_bounds__(BC_THREADS, 2) bc_grid_kernel(BcArgs a, int do_backward)
 {
     __shared__ u64 s_act[16];
+    __shared__ BcCtl s_ctl;  // control block as read by thread 0 after each barrier
     unsigned epoch = 0;
     BcCtl *ctl = a.ctl;
+    auto barrier = [&]() {
+        return grid_barrier(&ctl->bar, &ctl->err, epoch, reinterpret_cast<const u64 *>(ctl), reinterpret_cast<u64 *>(&s_ctl),
+                            (int)(sizeof(BcCtl) / sizeof(u64)));
+    };
     const long long rank = (long long)blockIdx.x * blockDim.x + threadIdx.x, size = (long long)gridDim.x * blockDim.x;
     const int W = a.W, B = 64 * W;
     const size_t nW = (size_t)a.n * W;
@@ -358,7 +363,7 @@ __global__ void __launch_bounds__(BC_THREADS, 2) bc_grid_kernel(BcArgs a, int do
             ctl->found[0] = ctl->found[1] = 0;
             for (int q = 0; q < 16; ++q) ctl->active[0][q] = ctl->active[1][q] = 0;
         }
-        if (!grid_barrier(&ctl->bar, &ctl->err, epoch)) return;
+        if (!barrier()) return;
         if (rank < nb) {
             const int32_t s = __ldg(a.sources + row0 + rank);
             const int q = (int)rank >> 6;
@@ -367,13 +372,13 @@ __global__ void __launch_bounds__(BC_THREADS, 2) bc_grid_kernel(BcArgs a, int do
             a.sigma[(size_t)s * B + rank] = 1ull;
             atomicOr(&ctl->active[0][q], bit);
         }
-        if (!grid_barrier(&ctl->bar, &ctl->err, epoch)) return;
+        if (!barrier()) return;
         // forward levels
         int L = 0;
         for (int j = 1;; ++j) {
             if (j > a.max_lvl) {
                 if (rank == 0) atomicCAS(&ctl->err, 0, (int)DEV_ERR_LEVELS);
-                grid_barrier(&ctl->bar, &ctl->err, epoch);
+                barrier();
                 return;
             }
             for (size_t i = (size_t)rank; i < nW; i += (size_t)size) a.lvl[(size_t)j * nW + i] = 0;
@@ -381,9 +386,9 @@ __global__ void __launch_bounds__(BC_THREADS, 2) bc_grid_kernel(BcArgs a, int do
                 ctl->found[j & 1] = 0;
                 for (int q = 0; q < 16; ++q) ctl->active[j & 1][q] = 0;
             }
-            if (!grid_barrier(&ctl->bar, &ctl->err, epoch)) return;
+            if (!barrier()) return;
             for (int q = 0; q < W; ++q) {
-                const u64 act = ld_volatile_u64(&ctl->active[(j - 1) & 1][q]);
+                const u64 act = s_ctl.active[(j - 1) & 1][q];
                 u64 found = 0;
                 for (long long c = gwarp(); c < a.cin.nchunks; c += nwarps())
                     bc_forward_item(a, j, q, (int)c, act, found);
@@ -395,8 +400,8 @@ __global__ void __launch_bounds__(BC_THREADS, 2) bc_grid_kernel(BcArgs a, int do
                 atomicOr(&ctl->found[j & 1], 1);
                 s_act[threadIdx.x] = 0;
             }
-            if (!grid_barrier(&ctl->bar, &ctl->err, epoch)) return;
-            if (ld_volatile_i32(&ctl->found[j & 1]) == 0) {
+            if (!barrier()) return;
+            if (s_ctl.found[j & 1] == 0) {
                 L = j - 1;  // this pass also folded lvl[L] into seen
                 break;
             }
@@ -406,11 +411,11 @@ __global__ void __launch_bounds__(BC_THREADS, 2) bc_grid_kernel(BcArgs a, int do
             for (int l = L; l >= 1; --l) {
                 for (int q = 0; q < W; ++q)
                     for (long long c = gwarp(); c < a.cout.nchunks; c += nwarps()) bc_backward_item(a, l, L, q, (int)c);
-                if (!grid_barrier(&ctl->bar, &ctl->err, epoch)) return;
+                if (!barrier()) return;
                 if (a.cout.nmulti) {
                     for (int q = 0; q < W; ++q)
                         for (long long i = gwarp(); i < a.cout.nmulti; i += nwarps()) bc_combine_item(a, l, q, (int)i);
-                    if (!grid_barrier(&ctl->bar, &ctl->err, epoch)) return;
+                    if (!barrier()) return;
                 }
             }
             for (long long w = gwarp(); w < a.n; w += nwarps()) bc_accumulate_item(a, (int32_t)w, row0, nb);
@@ -419,7 +424,7 @@ __global__ void __launch_bounds__(BC_THREADS, 2) bc_grid_kernel(BcArgs a, int do
             for (int q = 0; q < W; ++q)
                 for (long long w = gwarp(); w < a.n; w += nwarps()) bc_rows_item(a, (int32_t)w, q, row0, nb, L);
         }
-        if (!grid_barrier(&ctl->bar, &ctl->err, epoch)) return;
+        if (!barrier()) return;
     }
 }
 

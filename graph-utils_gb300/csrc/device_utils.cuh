@@ -68,8 +68,13 @@ constexpr u64 WAIT_LIMIT_NS = 4ull * 1000ull * 1000ull * 1000ull;
 // Grid-wide barrier for a cooperative launch (all CTAs co-resident).  `bar` is a
 // monotonically increasing arrival counter zeroed before the launch; `epoch`
 // counts this CTA's barriers.  Returns false if any CTA reported an error.
-__device__ __forceinline__ bool grid_barrier(unsigned *bar, int *err, unsigned &epoch)
+// Thread 0 alone reads the global words every thread needs after the barrier
+// (the error flag, and n 64-bit words from src into the shared dst): one
+// request per CTA instead of one per warp, all at the same address.
+__device__ __forceinline__ bool grid_barrier(unsigned *bar, int *err, unsigned &epoch, const u64 *src = nullptr,
+                                             u64 *dst = nullptr, int n = 0)
 {
+    __shared__ int s_ok;
     __syncthreads();
     if (threadIdx.x == 0) {
         epoch += 1;
@@ -93,9 +98,11 @@ __device__ __forceinline__ bool grid_barrier(unsigned *bar, int *err, unsigned &
             __nanosleep(32);
         }
         __threadfence();
+        s_ok = ld_volatile_i32(err) == 0;
+        for (int i = 0; i < n; ++i) dst[i] = ld_volatile_u64(src + i);
     }
     __syncthreads();
-    return ld_volatile_i32(err) == 0;
+    return s_ok != 0;
 }
 
 // Lanes of `mask` append one value each to q at a reserved, contiguous range.

@@ -141,6 +141,9 @@ struct MsOptions {
     float alpha = 2.f;    // top-down -> bottom-up when frontier out-edges > m / alpha
     float beta = 24.f;    // bottom-up -> top-down when frontier vertices < n / beta
     float gamma = 4.f;    // ... or when frontier out-edges < n / gamma
+    // bottom-up levels expand top-down the sources that fewer than this fraction
+    // of the CTAs discovered in the previous level (0: none)
+    float rare_frac = 1.f / 3.f;
     Workspace *ws = nullptr;  // scratch to use (default: the graph's)
     int max_blocks = 0;       // cap on the persistent grid (0: the whole GPU)
     bool timed = true;        // record the graph's launch events

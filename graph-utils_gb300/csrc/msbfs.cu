@@ -62,7 +62,8 @@ struct __align__(128) MsCtl {
     int pad0[3];
     u64 qpack[4];
     int work[4];
-    int pad1[4];
+    u64 rpack;  // bottom-up level: rare-source frontier list, (count << 38) | edges
+    int pad1[2];
     u64 active[4][MAXW];
 };
 static_assert(sizeof(MsCtl) <= 256, "control block must fit its reserved space");
@@ -77,7 +78,12 @@ struct MsEvent {
     int32_t bottom_up, qlen;
     long long qedges;
 };
-constexpr size_t CTL_REGION = 256 + sizeof(MsEvent) * TIMELINE_MAX + sizeof(int) * 4;
+// Per-source coverage of each level's discoveries: cover[j & 3][s] counts the
+// CTAs that discovered source s in F_j (a source with a frontier of a few dozen
+// vertices is seen by a few dozen CTAs, an empty frontier by none).
+constexpr size_t COVER_OFF = (256 + sizeof(MsEvent) * TIMELINE_MAX + sizeof(int) * 4 + 15) & ~size_t(15);
+constexpr int COVER_SLOT = 64 * MAXW;
+constexpr size_t CTL_REGION = COVER_OFF + sizeof(int) * 4 * COVER_SLOT;
 
 __device__ __forceinline__ void record_event(MsCtl *ctl, int i, bool describe, int batch, int level, int bu,
                                              int qlen, long long qedges)
@@ -120,7 +126,9 @@ struct MsArgs {
     int32_t *q[3];
     int32_t *qoff[3];
     MsCtl *ctl;
+    int *cover;  // [4][COVER_SLOT]
     float alpha, beta, gamma;
+    float rare_frac;  // bottom-up levels leave a source covered by fewer CTAs to top-down
     int degbits;
 };
 
@@ -139,7 +147,8 @@ struct Lvl {
     u64 *sact;    // shared-memory active-source accumulator of this CTA
     int32_t lev;  // BFS level of F_{j-1}
     int32_t tag;  // stamp of level j (j + 1)
-    u64 active[MAXW];
+    u64 active[MAXW];  // bottom-up levels: without the rare sources
+    bool rare_td;      // bottom-up level with rare sources expanded top-down
 };
 
 struct GridG {
@@ -239,8 +248,7 @@ __device__ __forceinline__ unsigned lanemask_lt() { return (1u << lane_id()) - 1
 // 64-bit atomicAdd reserves both the queue slots and the range of their
 // out-edges.  The exclusive prefix of the degrees over the active lanes is a
 // bit-sliced ballot sum (works for any active mask).
-__device__ __forceinline__ void append_vertex(const MsArgs &a, int slot, int32_t *qnxt, int32_t *qnxt_off,
-                                              int32_t w)
+__device__ __forceinline__ void append_to(const MsArgs &a, u64 *pack, int32_t *qnxt, int32_t *qnxt_off, int32_t w)
 {
     const unsigned deg = (unsigned)(__ldg(a.R + w + 1) - __ldg(a.R + w));
     const unsigned mask = __activemask();
@@ -254,11 +262,17 @@ __device__ __forceinline__ void append_vertex(const MsArgs &a, int slot, int32_t
         tot += (u64)__popc(v) << b;
     }
     u64 old = 0;
-    if (lane == leader) old = atomicAdd(&a.ctl->qpack[slot], ((u64)__popc(mask) << QPACK_SHIFT) | tot);
+    if (lane == leader) old = atomicAdd(pack, ((u64)__popc(mask) << QPACK_SHIFT) | tot);
     old = __shfl_sync(mask, old, leader);
     const int pos = (int)(old >> QPACK_SHIFT) + __popc(mask & lt);
     qnxt[pos] = w;
     qnxt_off[pos] = (int32_t)((old & QPACK_EDGES) + excl);
+}
+
+__device__ __forceinline__ void append_vertex(const MsArgs &a, int slot, int32_t *qnxt, int32_t *qnxt_off,
+                                              int32_t w)
+{
+    append_to(a, &a.ctl->qpack[slot], qnxt, qnxt_off, w);
 }
 
 // ---- where a top-down visit puts the vertices it discovers first --------------------
@@ -367,16 +381,16 @@ __device__ __forceinline__ void td_visit(const MsArgs &a, const Lvl &L, const u6
                                          const Q &qu = Q())
 {
     const size_t o = (size_t)w * W;
-    u64 s[W], c[W], x[W];
+    u64 s[W], c[W], x[W], nb[W];
     ldw_l1<W>(a.seen + o, s);
     ldw_l1<W>(L.fcur + o, c);
     ldw<W>(L.fnxt + o, x);
     bool found = false, first = false;
 #pragma unroll
     for (int q = 0; q < W; ++q) {
-        const u64 nb = f[q] & ~(s[q] | c[q] | x[q]);
-        if (nb) {
-            const u64 old = atomicOr(L.fnxt + o + q, nb);
+        nb[q] = f[q] & ~(s[q] | c[q] | x[q]);
+        if (nb[q]) {
+            const u64 old = atomicOr(L.fnxt + o + q, nb[q]);
             found = true;
             if (W == 1 && old == 0) first = true;
         }
@@ -484,6 +498,17 @@ template <int W>
 __device__ __forceinline__ void load_front(const Lvl &L, int32_t v, u64 (&f)[W])
 {
     ldw_l1<W>(L.fcur + (size_t)v * W, f);
+}
+
+// Frontier words of v restricted to the sources in fmask (shared) when MASKED.
+template <int W, bool MASKED>
+__device__ __forceinline__ void load_front_m(const Lvl &L, int32_t v, u64 (&f)[W], const u64 *fmask)
+{
+    ldw_l1<W>(L.fcur + (size_t)v * W, f);
+    if (MASKED) {
+#pragma unroll
+        for (int q = 0; q < W; ++q) f[q] &= fmask[q];
+    }
 }
 
 // LINEAR: thread per frontier vertex, serial adjacency (linear_with_atomics.cu:122-135).
@@ -716,8 +741,8 @@ constexpr int MP_STAGE = 1024;
 constexpr int MP_QUEUE = 2048;  // discovered-vertex queue after the staging
 static_assert(3 * MP_STAGE * 4 + MP_QUEUE * 4 <= MS_SMEM_BYTES, "merge-path staging exceeds the shared buffer");
 
-template <int W, class G>
-__device__ void gather_mp(const MsArgs &a, const Lvl &L)
+template <int W, class G, bool MASKED = false>
+__device__ void gather_mp(const MsArgs &a, const Lvl &L, const u64 *fmask = nullptr)
 {
     int32_t *s_off = reinterpret_cast<int32_t *>(ms_smem());
     int32_t *s_v = s_off + MP_STAGE;
@@ -764,7 +789,7 @@ __device__ void gather_mp(const MsArgs &a, const Lvl &L)
                 }
                 const bool has2 = e2 < e1;
                 u64 f[W];
-                load_front<W>(L, s_v[lo], f);
+                load_front_m<W, MASKED>(L, s_v[lo], f, fmask);
                 const int32_t w = __ldg(a.C + s_r[lo] + (int32_t)(e - s_off[lo]));
                 const int32_t w2 = has2 ? __ldg(a.C + s_r[lo2] + (int32_t)(e2 - s_off[lo2])) : -1;
                 if (!has2 || lo2 == lo) {
@@ -774,7 +799,7 @@ __device__ void gather_mp(const MsArgs &a, const Lvl &L)
                 } else {
                     td_visit<W>(a, L, f, w, cq);
                     u64 f2[W];
-                    load_front<W>(L, s_v[lo2], f2);
+                    load_front_m<W, MASKED>(L, s_v[lo2], f2, fmask);
                     td_visit<W>(a, L, f2, w2, cq);
                 }
             }
@@ -786,7 +811,7 @@ __device__ void gather_mp(const MsArgs &a, const Lvl &L)
                 const long long lo_e = max(off, e0), hi_e = min(off + deg, e1);
                 if (lo_e >= hi_e) continue;
                 u64 f[W];
-                load_front<W>(L, v, f);
+                load_front_m<W, MASKED>(L, v, f, fmask);
                 for (long long e = lo_e; e < hi_e; ++e) td_visit<W>(a, L, f, __ldg(a.C + r + (int32_t)(e - off)), cq);
             }
         }
@@ -797,15 +822,24 @@ __device__ void gather_mp(const MsArgs &a, const Lvl &L)
     if (*cq.n > 0) cta_flush(a, L, cq);
 }
 
-// Bottom-up level.  Each vertex with in-edges belongs to one degree class
-// (light, mid, wide, heavy; vertices without in-edges are never discovered
-// after level 0 and are in none).  The pass of its class finalises its
-// F_{j-1} bits, clears its F_{j-2} words and, while it still misses an active
-// source, ORs its in-neighbours' F_{j-1} words.  The light, mid and wide
-// passes take a vertex's in-neighbours in at most two rounds of loads issued
-// together (no loop: lanes of a warp never diverge over trip counts); the
-// heavy pass steps through the in-edges.  The mid, wide and heavy passes stop
-// once every missing active source is found.
+// Bottom-up level, in up to three grid-synchronised parts.
+//  A  Every vertex with in-edges (the light, mid, wide and heavy class lists;
+//     vertices without in-edges are never discovered after level 0) finalises
+//     its F_{j-1} bits and clears its F_{j-2} words.  The OR of the F_{j-1}
+//     words a CTA finalised marks the sources it saw; the count of CTAs that saw
+//     a source is its coverage (a source with a frontier of a few dozen vertices
+//     is seen by a few dozen CTAs, a source whose search ended by none).
+//  B  Sources seen by at least rare_frac of the CTAs are searched bottom-up:
+//     each vertex still missing one ORs its in-neighbours' F_{j-1} words, the
+//     light, mid and wide passes in at most two rounds of loads issued together
+//     (no loop: lanes of a warp never diverge over trip counts), the heavy pass
+//     stepping through the in-edges; mid, wide and heavy stop once every
+//     missing source is found.  Frontier vertices holding a rare source (seen,
+//     but by fewer CTAs) are listed.
+//  C  Only with rare sources: the listed vertices are expanded top-down, with
+//     their rare bits only, by the merge-path gather.  Searched bottom-up, a
+//     rare source would keep every vertex it has not reached scanning all its
+//     in-edges, since the early exit waits for every missing source.
 template <int W>
 __device__ __forceinline__ bool covers(const u64 (&acc)[W], const u64 (&need)[W])
 {
@@ -824,21 +858,43 @@ __device__ __forceinline__ void or_front(const Lvl &L, int32_t v, u64 (&acc)[W])
     for (int q = 0; q < W; ++q) acc[q] |= x[q];
 }
 
-// The class pass's own-vertex step: returns the sources still missing.
+// Part A for one vertex.
 template <int W>
-__device__ __forceinline__ void bu_own(const MsArgs &a, const Lvl &L, size_t o, u64 (&act)[W], u64 (&need)[W])
+__device__ __forceinline__ void bu_finalise(const MsArgs &a, const Lvl &L, int32_t w, u64 (&act)[W])
 {
-    u64 s[W], f[W];
-    ldw<W>(a.seen + o, s);
+    const size_t o = (size_t)w * W;
+    u64 f[W];
     ldw<W>(L.fcur + o, f);
-#pragma unroll
-    for (int q = 0; q < W; ++q) need[q] = L.active[q] & ~(s[q] | f[q]);
     if (anyw<W>(f)) {
+        u64 s[W];
+        ldw<W>(a.seen + o, s);
         finalise<W>(a, L.lev, o, f, s);
 #pragma unroll
         for (int q = 0; q < W; ++q) act[q] |= f[q];
     }
     zerow<W>(L.fprv + o);
+}
+
+template <int W, class G>
+__device__ void bu_finalise_all(const MsArgs &a, const Lvl &L)
+{
+    u64 act[W] = {};
+    const long long rank = G::rank(), size = G::size();
+    for (long long i = rank; i < a.nlight; i += size) bu_finalise<W>(a, L, __ldg(a.light + i), act);
+    for (long long i = rank; i < a.nmid; i += size) bu_finalise<W>(a, L, __ldg(a.mid + i), act);
+    for (long long i = rank; i < a.nwide; i += size) bu_finalise<W>(a, L, __ldg(a.wide + i), act);
+    for (long long i = rank; i < a.nheavy; i += size) bu_finalise<W>(a, L, __ldg(a.heavy + i), act);
+    flush_active<W>(L, act);
+}
+
+// Sources of part B a vertex still misses (seen holds F_{j-1} after part A).
+template <int W>
+__device__ __forceinline__ void bu_need(const MsArgs &a, const Lvl &L, int32_t w, u64 (&need)[W])
+{
+    u64 s[W];
+    ldw<W>(a.seen + (size_t)w * W, s);
+#pragma unroll
+    for (int q = 0; q < W; ++q) need[q] = L.active[q] & ~s[q];
 }
 
 template <int W>
@@ -848,30 +904,36 @@ __device__ __forceinline__ void bu_found(const MsArgs &a, const Lvl &L, const Ct
     u64 nb[W];
 #pragma unroll
     for (int q = 0; q < W; ++q) nb[q] = acc[q] & need[q];
-    if (anyw<W>(nb)) {
-        stw<W>(L.fnxt + (size_t)w * W, nb);
-        cq.push(a, L, w);
-    }
+    if (!anyw<W>(nb)) return;
+    stw<W>(L.fnxt + (size_t)w * W, nb);  // the vertex's only writer in part B
+    if (W > 1 && L.rare_td) a.stamp[w] = L.tag;  // part C's visits must not append w again
+    cq.push(a, L, w);
 }
 
 // Vertices of a class per warp step: the class spread over every warp, at most
-// one per lane.  Each lane runs the own-vertex step of one vertex; the warp
-// then scans only the vertices that still miss a source.
+// one per lane.  Each lane reads the missing set of one vertex; the warp then
+// scans only the vertices that still miss a source.
 __device__ __forceinline__ long long class_chunk(long long count, long long nwarps)
 {
     return max(1ll, min(32ll, (count + nwarps - 1) / nwarps));
+}
+
+template <int W>
+__device__ __forceinline__ void shfl_words(const u64 (&x)[W], u64 (&y)[W], int src)
+{
+#pragma unroll
+    for (int q = 0; q < W; ++q) y[q] = __shfl_sync(FULL_MASK, x[q], src);
 }
 
 // Light: one thread per vertex, up to BU_LIGHT_DEGREE loads in flight.
 template <int W, class G>
 __device__ void bu_light(const MsArgs &a, const Lvl &L, const CtaQ &cq)
 {
-    u64 act[W] = {};
     const long long size = G::size();
     for (long long i = G::rank(); i < a.nlight; i += size) {
         const int32_t w = __ldg(a.light + i);
         u64 need[W];
-        bu_own<W>(a, L, (size_t)w * W, act, need);
+        bu_need<W>(a, L, w, need);
         if (!anyw<W>(need)) continue;
         const int32_t e0 = __ldg(a.RT + w), e1 = __ldg(a.RT + w + 1);
         int32_t c[BU_LIGHT_DEGREE];
@@ -883,22 +945,13 @@ __device__ void bu_light(const MsArgs &a, const Lvl &L, const CtaQ &cq)
             if (c[t] >= 0) or_front<W>(L, c[t], acc);
         bu_found<W>(a, L, cq, w, acc, need);
     }
-    flush_active<W>(L, act);
 }
 
-template <int W>
-__device__ __forceinline__ void shfl_words(const u64 (&x)[W], u64 (&y)[W], int src)
-{
-#pragma unroll
-    for (int q = 0; q < W; ++q) y[q] = __shfl_sync(FULL_MASK, x[q], src);
-}
-
-// Mid: after the own-vertex steps, eight lanes per needy vertex (four at a
-// time).  First the eight highest-degree in-neighbours (one load per lane),
-// which at the later levels usually cover every missing source; then, only
-// where they do not, the rest (up to three more loads per lane, in flight
-// together).  The group's words are OR-ed with xor shuffles inside the group;
-// no loop per vertex, so the four groups of a warp never diverge.
+// Mid: eight lanes per needy vertex (four at a time).  First the eight
+// highest-degree in-neighbours (one load per lane), which at the later levels
+// usually cover every missing source; then, only where they do not, the rest
+// (up to three more loads per lane, in flight together).  The group's words
+// are OR-ed with xor shuffles inside the group.
 template <int W>
 __device__ __forceinline__ void group8_or(u64 (&x)[W])
 {
@@ -914,14 +967,13 @@ __device__ void bu_mid(const MsArgs &a, const Lvl &L, const CtaQ &cq)
 {
     static_assert(BU_LIGHT_DEGREE >= 7, "mid class: the first round gives every lane an in-edge");
     static_assert(BU_MID_DEGREE <= 8 * 4, "mid class: at most four in-edges per lane");
-    u64 act[W] = {};
     const int lane = lane_id(), sub = lane & 7, grp = lane >> 3;
     const long long nw = G::size() >> 5, chunk = class_chunk(a.nmid, nw);
     for (long long base = (G::rank() >> 5) * chunk; base < a.nmid; base += nw * chunk) {  // warp-uniform
         const bool valid = lane < chunk && base + lane < a.nmid;
         const int32_t mine = valid ? __ldg(a.mid + base + lane) : 0;
         u64 need_l[W] = {};
-        if (valid) bu_own<W>(a, L, (size_t)mine * W, act, need_l);
+        if (valid) bu_need<W>(a, L, mine, need_l);
         unsigned todo = __ballot_sync(FULL_MASK, anyw<W>(need_l));
         while (todo) {  // warp-uniform
             unsigned t = todo;
@@ -959,26 +1011,23 @@ __device__ void bu_mid(const MsArgs &a, const Lvl &L, const CtaQ &cq)
             if (has && sub == 0) bu_found<W>(a, L, cq, w, acc, need);
         }
     }
-    flush_active<W>(L, act);
 }
 
-// Wide: after the own-vertex steps, a warp per needy vertex: the 32
-// highest-degree in-neighbours first, then, only if they leave a missing
-// source uncovered, the rest (up to three more loads per lane, in flight
-// together).
+// Wide: a warp per needy vertex: the 32 highest-degree in-neighbours first,
+// then, only if they leave a missing source uncovered, the rest (up to three
+// more loads per lane, in flight together).
 template <int W, class G>
 __device__ void bu_wide(const MsArgs &a, const Lvl &L, const CtaQ &cq)
 {
     static_assert(BU_MID_DEGREE >= 31, "wide class: the first round gives every lane an in-edge");
     static_assert(BU_HEAVY_DEGREE <= 32 * 4, "wide class: at most four in-edges per lane");
-    u64 act[W] = {};
     const int lane = lane_id();
     const long long nw = G::size() >> 5, chunk = class_chunk(a.nwide, nw);
     for (long long base = (G::rank() >> 5) * chunk; base < a.nwide; base += nw * chunk) {  // warp-uniform
         const bool valid = lane < chunk && base + lane < a.nwide;
         const int32_t mine = valid ? __ldg(a.wide + base + lane) : 0;
         u64 need_l[W] = {};
-        if (valid) bu_own<W>(a, L, (size_t)mine * W, act, need_l);
+        if (valid) bu_need<W>(a, L, mine, need_l);
         unsigned todo = __ballot_sync(FULL_MASK, anyw<W>(need_l));
         while (todo) {  // warp-uniform
             const int src = __ffs(todo) - 1;
@@ -1006,24 +1055,21 @@ __device__ void bu_wide(const MsArgs &a, const Lvl &L, const CtaQ &cq)
             if (lane == 0) bu_found<W>(a, L, cq, w, acc, need);
         }
     }
-    flush_active<W>(L, act);
 }
 
-// Heavy (in-degree > BU_HEAVY_DEGREE): after the own-vertex steps, a warp per
-// needy vertex ORs 128 in-neighbours per step (four loads in flight per lane),
-// the 32 highest-degree ones first, and stops once every missing active source
-// is found.
+// Heavy (in-degree > BU_HEAVY_DEGREE): a warp per needy vertex ORs 128
+// in-neighbours per step (four loads in flight per lane), the 32
+// highest-degree ones first, and stops once every missing source is found.
 template <int W, class G>
 __device__ void bu_heavy(const MsArgs &a, const Lvl &L, const CtaQ &cq)
 {
-    u64 act[W] = {};
     const int lane = lane_id();
     const long long nw = G::size() >> 5, chunk = class_chunk(a.nheavy, nw);
     for (long long base = (G::rank() >> 5) * chunk; base < a.nheavy; base += nw * chunk) {  // warp-uniform
         const bool valid = lane < chunk && base + lane < a.nheavy;
         const int32_t mine = valid ? __ldg(a.heavy + base + lane) : 0;
         u64 need_l[W] = {};
-        if (valid) bu_own<W>(a, L, (size_t)mine * W, act, need_l);
+        if (valid) bu_need<W>(a, L, mine, need_l);
         unsigned todo = __ballot_sync(FULL_MASK, anyw<W>(need_l));
         while (todo) {  // warp-uniform
             const int src = __ffs(todo) - 1;
@@ -1053,7 +1099,25 @@ __device__ void bu_heavy(const MsArgs &a, const Lvl &L, const CtaQ &cq)
             if (lane == 0) bu_found<W>(a, L, cq, w, acc, need);
         }
     }
-    flush_active<W>(L, act);
+}
+
+// Part B's list of the frontier vertices that hold a rare source, with their
+// out-edge offsets, in F_{j-2}'s queue arrays (free during a bottom-up level).
+template <int W, class G>
+__device__ void bu_rare_list(const MsArgs &a, const Lvl &L, const u64 *s_rare)
+{
+    u64 r[W];
+#pragma unroll
+    for (int q = 0; q < W; ++q) r[q] = s_rare[q];
+    for (long long i = G::rank(); i < L.qlen; i += G::size()) {
+        const int32_t u = __ldcg(L.qcur + i);
+        u64 f[W];
+        ldw<W>(L.fcur + (size_t)u * W, f);
+        bool any = false;
+#pragma unroll
+        for (int q = 0; q < W; ++q) any |= (f[q] & r[q]) != 0;
+        if (any) append_to(a, &a.ctl->rpack, a.q[L.prv], a.qoff[L.prv], u);
+    }
 }
 
 // Distance rows of one batch from seen and the level bit-planes.
@@ -1323,9 +1387,17 @@ template <int VARIANT, int W>
 __global__ void __launch_bounds__(MS_THREADS, MS_MIN_BLOCKS) ms_grid_kernel(MsArgs a)
 {
     __shared__ u64 s_act[MAXW];
+    // copy of the control block taken by each CTA's thread 0 after every barrier
+    __shared__ MsCtl s_ctl;
+    __shared__ u64 s_rare[MAXW];  // bottom-up level: rare sources expanded top-down
+    __shared__ u64 s_excl[MAXW];  // ... and the sources it searches bottom-up
     unsigned epoch = 0;
     int ev_idx = 0;
     MsCtl *ctl = a.ctl;
+    auto barrier = [&]() {
+        return grid_barrier(&ctl->bar, &ctl->err, epoch, reinterpret_cast<const u64 *>(ctl), reinterpret_cast<u64 *>(&s_ctl),
+                            (int)(sizeof(MsCtl) / sizeof(u64)));
+    };
     const long long rank = GridG::rank(), size = GridG::size();
     const size_t pstride = (size_t)a.n * W;
     if (threadIdx.x < MAXW) s_act[threadIdx.x] = 0;
@@ -1353,7 +1425,8 @@ __global__ void __launch_bounds__(MS_THREADS, MS_MIN_BLOCKS) ms_grid_kernel(MsAr
 #pragma unroll
             for (int q = 0; q < MAXW; ++q) ctl->active[rank][q] = 0;
         }
-        if (!grid_barrier(&ctl->bar, &ctl->err, epoch)) return;
+        if (rank < 4 * COVER_SLOT) a.cover[rank] = 0;
+        if (!barrier()) return;
         if (rank < nb) {
             const int32_t s = __ldg(a.sources + row0 + rank);
             const int q = (int)rank >> 6;
@@ -1367,20 +1440,20 @@ __global__ void __launch_bounds__(MS_THREADS, MS_MIN_BLOCKS) ms_grid_kernel(MsAr
         }
         if (threadIdx.x == 0) record_event(ctl, ev_idx, rank == 0, b, 0, 4, nb, 0);  // batch initialised, seeded
         ++ev_idx;
-        if (!grid_barrier(&ctl->bar, &ctl->err, epoch)) return;
+        if (!barrier()) return;
 
         bool prev_bu = false;
         int j = 1;
         for (;; ++j) {
             Lvl L;
             const int sc = (j - 1) & 3, sp = (j - 2) & 3;
-            const u64 pk = ld_volatile_u64(&ctl->qpack[sc]);
+            const u64 pk = s_ctl.qpack[sc];
             L.qlen = (int)(pk >> QPACK_SHIFT);
             if (L.qlen == 0) break;
             L.qedges = (long long)(pk & QPACK_EDGES);
-            L.qlen_prev = j >= 2 ? (int)(ld_volatile_u64(&ctl->qpack[sp]) >> QPACK_SHIFT) : 0;
+            L.qlen_prev = j >= 2 ? (int)(s_ctl.qpack[sp] >> QPACK_SHIFT) : 0;
 #pragma unroll
-            for (int q = 0; q < MAXW; ++q) L.active[q] = q < W ? ld_volatile_u64(&ctl->active[sc][q]) : 0ull;
+            for (int q = 0; q < MAXW; ++q) L.active[q] = q < W ? s_ctl.active[sc][q] : 0ull;
             L.slot = j & 3;
             L.cur = (j - 1) % 3;
             L.nxt = j % 3;
@@ -1403,6 +1476,8 @@ __global__ void __launch_bounds__(MS_THREADS, MS_MIN_BLOCKS) ms_grid_kernel(MsAr
 #pragma unroll
                 for (int q = 0; q < MAXW; ++q) ctl->active[z][q] = 0;
             }
+            if (rank < COVER_SLOT) a.cover[((j + 1) & 3) * COVER_SLOT + rank] = 0;
+            L.rare_td = false;
             // plane b is first written in phase 2^b + 1; clear it one phase earlier
             if ((j & (j - 1)) == 0) {
                 const int pb = __ffs(j) - 1;
@@ -1418,23 +1493,60 @@ __global__ void __launch_bounds__(MS_THREADS, MS_MIN_BLOCKS) ms_grid_kernel(MsAr
                           (double)L.qedges * (double)a.gamma > (double)a.n;
             }
             if (bu) {
-                // F_0 may hold sources without in-edges, which no class pass visits
+                // part A; F_0 may hold sources without in-edges, which no class list has
                 if (j == 2 && rank < nb) zerow<W>(L.fprv + (size_t)__ldg(a.sources + row0 + rank) * W);
-                // sub-stage stamps (kinds 5, 6): when warp 0 of the slowest CTA finished
-                // the light class and the mid + wide classes
+                if (rank == 0) ctl->rpack = 0;
+                bu_finalise_all<W, GridG>(a, L);
+                __syncthreads();
+                if (threadIdx.x < 64 * W && ((s_act[threadIdx.x >> 6] >> (threadIdx.x & 63)) & 1ull))
+                    atomicAdd(&a.cover[L.slot * COVER_SLOT + threadIdx.x], 1);
+                // timeline kinds 5-7: parts A and B, and the light class within B
+                if (threadIdx.x == 0) record_event(ctl, ev_idx, rank == 0, b, j, 5, L.qlen, L.qedges);
+                ++ev_idx;
+                if (!barrier()) return;
+                // part B: sources searched bottom-up and rare ones, from the coverage
+                if (threadIdx.x < 64 * W) {
+                    const float c = (float)ld_volatile_i32(&a.cover[L.slot * COVER_SLOT + threadIdx.x]);
+                    const float thr = fmaxf(1.f, a.rare_frac * (float)gridDim.x);
+                    const unsigned cb = __ballot_sync(FULL_MASK, c >= thr);
+                    const unsigned rb = __ballot_sync(FULL_MASK, c >= 1.f && c < thr);
+                    if ((threadIdx.x & 31) == 0) {  // 32-bit halves of the 64-bit words
+                        reinterpret_cast<unsigned *>(s_excl)[threadIdx.x >> 5] = cb;
+                        reinterpret_cast<unsigned *>(s_rare)[threadIdx.x >> 5] = rb;
+                    }
+                }
+                __syncthreads();
+                u64 any_rare = 0;
+#pragma unroll
+                for (int q = 0; q < W; ++q) {
+                    L.active[q] = s_excl[q];
+                    any_rare |= s_rare[q];
+                }
+                L.rare_td = any_rare != 0;
                 // discovered vertices collect in the CTA's shared queue (the whole
-                // staging buffer), flushed to the level's queue at the end
+                // staging buffer), flushed to the level's queue at the end of part B
                 const CtaQ cq{reinterpret_cast<int32_t *>(ms_smem()), cq_count(), MS_SMEM_BYTES / 4};
                 bu_light<W, GridG>(a, L, cq);
-                if (threadIdx.x == 0) record_event(ctl, ev_idx, rank == 0, b, j, 5, L.qlen, L.qedges);
+                if (threadIdx.x == 0) record_event(ctl, ev_idx, rank == 0, b, j, 6, L.qlen, L.qedges);
                 ++ev_idx;
                 bu_mid<W, GridG>(a, L, cq);
                 bu_wide<W, GridG>(a, L, cq);
-                if (threadIdx.x == 0) record_event(ctl, ev_idx, rank == 0, b, j, 6, L.qlen, L.qedges);
-                ++ev_idx;
                 bu_heavy<W, GridG>(a, L, cq);
+                if (L.rare_td) bu_rare_list<W, GridG>(a, L, s_rare);
                 __syncthreads();
                 if (*cq.n > 0) cta_flush(a, L, cq);
+                if (L.rare_td) {  // part C
+                    if (threadIdx.x == 0) record_event(ctl, ev_idx, rank == 0, b, j, 7, L.qlen, L.qedges);
+                    ++ev_idx;
+                    if (!barrier()) return;
+                    const u64 rp = s_ctl.rpack;
+                    Lvl LC = L;
+                    LC.qcur = a.q[L.prv];
+                    LC.qcur_off = a.qoff[L.prv];
+                    LC.qlen = (int)(rp >> QPACK_SHIFT);
+                    LC.qedges = (long long)(rp & QPACK_EDGES);
+                    gather_mp<W, GridG, true>(a, LC, s_rare);
+                }
             } else {
                 td_update<W, GridG>(a, L);
                 if (VARIANT == GU_BFS_EDGE) gather_edge<W, GridG>(a, L);
@@ -1459,7 +1571,7 @@ __global__ void __launch_bounds__(MS_THREADS, MS_MIN_BLOCKS) ms_grid_kernel(MsAr
             if (threadIdx.x == 0) record_event(ctl, ev_idx, rank == 0, b, j, bu ? 1 : 0, L.qlen, L.qedges);
             ++ev_idx;
             prev_bu = bu;
-            if (!grid_barrier(&ctl->bar, &ctl->err, epoch)) return;
+            if (!barrier()) return;
         }
         // F_{j-1} is empty: levels of this batch are 0..j-2
         int used = 0;
@@ -1467,7 +1579,7 @@ __global__ void __launch_bounds__(MS_THREADS, MS_MIN_BLOCKS) ms_grid_kernel(MsAr
         if (a.dist) write_distances<W, GridG>(a, row0, nb, used);  // no rows: diameter queries
         if (threadIdx.x == 0) record_event(ctl, ev_idx, rank == 0, b, j, 2, 0, 0);  // distance rows written
         ++ev_idx;
-        if (!grid_barrier(&ctl->bar, &ctl->err, epoch)) return;
+        if (!barrier()) return;
     }
 }
 
@@ -1568,6 +1680,7 @@ void launch_msbfs(DeviceGraph &g, const int32_t *sources, int32_t k, int32_t *di
     a.ld = ld;
     char *p = ws;
     a.ctl = reinterpret_cast<MsCtl *>(p);
+    a.cover = reinterpret_cast<int *>(p + COVER_OFF);
     p += ctl_bytes;
     a.seen = reinterpret_cast<u64 *>(p);
     p += words_bytes;
@@ -1589,6 +1702,7 @@ void launch_msbfs(DeviceGraph &g, const int32_t *sources, int32_t k, int32_t *di
     a.alpha = env_float("GU_MS_ALPHA", opt.alpha);
     a.beta = env_float("GU_MS_BETA", opt.beta);
     a.gamma = env_float("GU_MS_GAMMA", opt.gamma);
+    a.rare_frac = env_float("GU_MS_RARE", opt.rare_frac);
     int degbits = 1;
     while (degbits < 31 && (1ll << degbits) <= (long long)g.max_degree) ++degbits;
     a.degbits = degbits;
@@ -1768,6 +1882,7 @@ static void bfs_noalloc(const int32_t *R, const int32_t *C, int32_t n, int64_t m
     a.ld = ld;
     char *p = scratch;
     a.ctl = reinterpret_cast<MsCtl *>(p);
+    a.cover = reinterpret_cast<int *>(p + COVER_OFF);
     p += WS_CONTROL_BYTES;
     a.seen = reinterpret_cast<u64 *>(p);
     p += words_bytes;
@@ -1789,6 +1904,7 @@ static void bfs_noalloc(const int32_t *R, const int32_t *C, int32_t n, int64_t m
     a.alpha = 0.f;  // never switch to bottom-up
     a.beta = 24.f;
     a.gamma = 4.f;
+    a.rare_frac = 0.f;
     int degbits = 1;
     while (degbits < 31 && (1ll << degbits) <= (long long)m) ++degbits;
     a.degbits = degbits;

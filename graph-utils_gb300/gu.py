@@ -225,7 +225,7 @@ class Graph:
         check(lib().gu_graph_level_profile(self._h, max_entries, _ptr(b), _ptr(lv), _ptr(kd),
                                            fv.ctypes.data_as(_i64p), fe.ctypes.data_as(_i64p),
                                            t.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), ctypes.byref(cnt)))
-        kinds = {0: "top-down", 1: "bottom-up", 2: "rows", 4: "init", 5: "bu-light", 6: "bu-mid"}
+        kinds = {0: "top-down", 1: "bottom-up", 2: "rows", 4: "init", 5: "bu-final", 6: "bu-light", 7: "bu-scan"}
         return [dict(batch=int(b[i]), level=int(lv[i]), kind=kinds.get(int(kd[i]), "?"),
                      frontier_vertices=int(fv[i]), frontier_edges=int(fe[i]), t_ms=float(t[i]))
                 for i in range(cnt.value)]

@@ -126,9 +126,10 @@ gu_status gu_graph_last_launch(gu_graph g, double *kernel_seconds, int *td_level
 
 /* Profiling hook: the per-phase timeline of the last batched search on g (up to
  * max_entries phases).  Entry i: batch, level j of the phase, kind (0 top-down,
- * 1 bottom-up, 2 distance write-out, 4 batch initialised; 5 and 6 mark, inside a
- * bottom-up phase, the end of the light sweep and of the mid-degree class as
- * seen by warp 0 of each CTA), vertices and out-edges of the frontier it
+ * 1 bottom-up, 2 distance write-out, 4 batch initialised; inside a bottom-up
+ * phase 5 marks the end of the finalise step, 6 the end of the light class's
+ * scan as seen by warp 0 of each CTA, 7 the end of the scans before the rare
+ * sources' top-down expansion), vertices and out-edges of the frontier it
  * expanded, and the time the slowest CTA finished it, in ms from the end of
  * entry 0.  No reference counterpart (the reference times whole calls only). */
 gu_status gu_graph_level_profile(gu_graph g, int max_entries, int32_t *batch, int32_t *level, int32_t *kind,
