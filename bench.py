@@ -49,6 +49,9 @@ def parse_args():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cpu-seconds", type=float, default=15.0, help="budget of the cpu_baseline sample")
     p.add_argument("--kernel-only", action="store_true", help="skip e2e (for profiling runs)")
+    p.add_argument("--workload", choices=["c2", "c1", "c3", "c4", "c5"], default="c2",
+                   help="c2: the headline BFS line (default); c1/c3/c4/c5: the other configurations, "
+                        "one JSON line each (bench_configs.py)")
     return p.parse_args()
 
 
@@ -334,7 +337,10 @@ def run_ours(args):
 
 def main():
     args = parse_args()
-    if args.impl == "reference":
+    if args.workload != "c2":
+        import bench_configs
+        bench_configs.run(args.workload, args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

@@ -1,0 +1,290 @@
+"""The non-headline benchmark configurations, one JSON line each (`bench.py --workload cN`).
+
+    c1  ER G(198, 2742) seed 1 and the jazz graph: BFS and exact BC from every vertex.
+    c3  R-MAT scale 18 (ef 16), 8192 sources: sigma (u64) and FP64 Brandes BC with
+        64, 128, 256, 512 and 1024 sources per pass.
+    c4  2048 x 2048 4-neighbour grid, each edge deleted with probability 0.05 (seed 7),
+        256 sources: BFS (batched and the one-CTA-per-source form), diameter, and
+        load-balanced search over the int32 degree array.
+    c5  serving: R-MAT graphs and random DAGs resident on the device, Poisson arrivals
+        of BFS / BC / reachability requests at several rates, p50 / p99 latency.
+
+GPU times are CUDA-event kernel times of the library's own launch (`last_launch`)
+unless named `call_ms` (wall time of the synchronous C-ABI call).  CPU times are
+the oracle (test infrastructure: the C restatement of the reference checkers) on
+one host thread and on all host threads; long CPU runs are timed on a seeded
+subset of the sources and extrapolated per source, and say so.
+"""
+import json
+import os
+import statistics
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "graph-utils_gb300"))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+INF = 2147483647
+
+
+def _torch():
+    import torch
+    torch.cuda.set_device(0)
+    return torch
+
+
+def _median_kernel_ms(g, fn, reps=5):
+    times = []
+    for _ in range(reps):
+        fn()
+        times.append(g.last_launch()[0] * 1e3)
+    return statistics.median(times)
+
+
+def _median_call_ms(fn, reps=3):
+    times = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        fn()
+        times.append((time.perf_counter() - t0) * 1e3)
+    return statistics.median(times)
+
+
+def _edges_reached(torch, g, srcs, deg):
+    """Sum over sources of scanned CSR entries (E_s) and reached vertices, via the engine's rows."""
+    E = V = 0.0
+    for b in range(0, len(srcs), 1024):
+        s = torch.as_tensor(srcs[b:b + 1024], device="cuda")
+        d = torch.empty((len(s), g.n), dtype=torch.int32, device="cuda")
+        g.bfs(s, d)
+        r = (d != INF).to(torch.float64)
+        E += float((r @ deg).sum())
+        V += float(r.sum())
+        del d, r
+    return E, V
+
+
+def _cpu(fn, *a, **kw):
+    t0 = time.perf_counter()
+    out = fn(*a, **kw)
+    return out, time.perf_counter() - t0
+
+
+def _emit(line):
+    print(json.dumps(line), flush=True)
+
+
+def wl_c1(args):
+    import gu
+    import oracle
+    torch = _torch()
+    cores = os.cpu_count() or 1
+    d = dict(np.load(os.path.join(ROOT, "tests", "golden", "graph_jazz.npz")))
+    graphs = {"er198_m2742_seed1": gu.HostGraph.er(198, 2742, seed=1),
+              "jazz": gu.HostGraph(d["R"], d["C"], int(d["n"]), bool(d["directed"]))}
+    out = {}
+    for name, hg in graphs.items():
+        g = gu.Graph(hg)
+        srcs = np.arange(hg.n, dtype=np.int32)
+        s = torch.as_tensor(srcs, device="cuda")
+        dist = torch.empty((hg.n, hg.n), dtype=torch.int32, device="cuda")
+        bc = torch.empty(hg.n, dtype=torch.float64, device="cuda")
+        deg = torch.as_tensor(np.diff(hg.R).astype(np.float64), device="cuda")
+        E, V = _edges_reached(torch, g, srcs, deg)
+        edges = E / 2.0
+        t_b = _median_kernel_ms(g, lambda: g.bfs(s, dist, variant="auto"))
+        t_p = _median_kernel_ms(g, lambda: g.bfs(s, dist, variant="plain"))
+        t_bc = _median_kernel_ms(g, lambda: g.bc(s, bc))
+        c_bc = _median_call_ms(lambda: g.bc(s, bc))
+        _, t1 = _cpu(oracle.bfs_multi, hg.R, hg.C, hg.n, srcs, nthreads=1)
+        _, tN = _cpu(oracle.bfs_multi, hg.R, hg.C, hg.n, srcs, nthreads=cores)
+        _, b1 = _cpu(oracle.bc, hg.R, hg.C, hg.n, srcs, nthreads=1)
+        _, bN = _cpu(oracle.bc, hg.R, hg.C, hg.n, srcs, nthreads=cores)
+        out[name] = {"n": hg.n, "m_csr": hg.m, "sources": len(srcs), "edges_per_bfs": edges,
+                     "bfs_batched_kernel_ms": t_b, "bfs_plain_kernel_ms": t_p,
+                     "bfs_batched_gteps": edges / t_b / 1e6, "bfs_plain_gteps": edges / t_p / 1e6,
+                     "bc_kernel_ms": t_bc, "bc_call_ms": c_bc, "bc_gteps": edges / t_bc / 1e6,
+                     "cpu_bfs_ms_1thread": t1 * 1e3, f"cpu_bfs_ms_{cores}threads": tN * 1e3,
+                     "cpu_bc_f64_ms_1thread": b1 * 1e3, f"cpu_bc_f64_ms_{cores}threads": bN * 1e3}
+        g.close()
+    _emit({"workload": "c1_er198_jazz_all_sources", "metric": "BFS and exact BC, all sources",
+           "unit": "ms / GTEPS", "results": out, "cpu_cores": cores,
+           "note": "tiny graphs: launch- and barrier-latency bound, GTEPS is not the point"})
+
+
+def wl_c3(args):
+    import gu
+    import oracle
+    torch = _torch()
+    cores = os.cpu_count() or 1
+    hg = gu.HostGraph.rmat(18, 16, 0.57, 0.19, 0.19, seed=1, permute=True)
+    g = gu.Graph(hg)
+    srcs = gu.sources(hg.n, 8192, seed=2)
+    deg = torch.as_tensor(np.diff(hg.R).astype(np.float64), device="cuda")
+    E, V = _edges_reached(torch, g, srcs, deg)
+    edges = E / 2.0  # per direction (forward sweep); the backward sweep walks the same edges again
+    s = torch.as_tensor(srcs, device="cuda")
+    bc = torch.empty(hg.n, dtype=torch.float64, device="cuda")
+    res = {}
+    for batch in (64, 128, 256, 512, 1024):
+        t = _median_kernel_ms(g, lambda: g.bc(s, bc, batch=batch), reps=3)
+        res[f"bc_batch{batch}_kernel_ms"] = t
+        res[f"bc_batch{batch}_gteps"] = edges / t / 1e6
+    ks = 1024
+    s1 = s[:ks]
+    sig = torch.empty((ks, hg.n), dtype=torch.int64, device="cuda")
+    dst = torch.empty((ks, hg.n), dtype=torch.int32, device="cuda")
+    res["sigma_1024src_kernel_ms"] = _median_kernel_ms(g, lambda: g.sigma(s1, sig, dist_dev=dst), reps=3)
+    del sig, dst
+    # BC algorithmic bytes, 28n + 32 V_s + 40 E_s per source (SURVEY 8(d) model)
+    alg = len(srcs) * 28.0 * hg.n + 32.0 * V + 40.0 * E
+    best = min(res[f"bc_batch{b}_kernel_ms"] for b in (64, 128, 256, 512, 1024))
+    sub1, subN = srcs[:4], srcs[:4 * cores]
+    _, c1 = _cpu(oracle.bc, hg.R, hg.C, hg.n, sub1, nthreads=1)
+    _, cN = _cpu(oracle.bc, hg.R, hg.C, hg.n, subN, nthreads=cores)
+    _emit({"workload": "c3_rmat18_ef16_8192src_bc", "metric": "FP64 Brandes BC GTEPS (forward-sweep edges)",
+           "unit": "GTEPS", "value": edges / best / 1e6, "n": hg.n, "m_csr": hg.m, "sources": len(srcs),
+           "edges": edges, "results": res,
+           "roofline": {"bound": "hbm", "alg_bytes": alg, "achieved_gbs": alg / best / 1e6,
+                        "model": "per-source 28n + 32 V_s + 40 E_s (effective: a pass shares reads)"},
+           "cpu_bc_f64": {"per_source_ms_1thread": c1 * 1e3 / len(sub1),
+                          f"per_source_ms_{cores}threads": cN * 1e3 / len(subN),
+                          "extrapolated_8192_s_all_threads": cN / len(subN) * 8192,
+                          "sample": f"first {len(sub1)} sources on 1 thread, first {len(subN)} on {cores}"}})
+
+
+def wl_c4(args):
+    import gu
+    import oracle
+    torch = _torch()
+    cores = os.cpu_count() or 1
+    hg = gu.HostGraph.grid(2048, 2048, 0.05, seed=7)
+    g = gu.Graph(hg)
+    srcs = gu.sources(hg.n, 256, seed=2)
+    s = torch.as_tensor(srcs, device="cuda")
+    deg_np = np.diff(hg.R).astype(np.int32)
+    deg = torch.as_tensor(deg_np.astype(np.float64), device="cuda")
+    E, V = _edges_reached(torch, g, srcs, deg)
+    edges = E / 2.0
+    dist = torch.empty((len(srcs), hg.n), dtype=torch.int32, device="cuda")
+    t_b = _median_kernel_ms(g, lambda: g.bfs(s, dist, variant="auto"), reps=3)
+    levels = g.last_launch()[1:]
+    t_p = _median_kernel_ms(g, lambda: g.bfs(s, dist, variant="plain"), reps=1)
+    c_d = _median_call_ms(lambda: g.diameter(s), reps=3)
+    diam = g.diameter(s)
+    # load-balanced search over the degree array
+    counts = torch.as_tensor(deg_np, device="cuda")
+    scanned = torch.empty_like(counts)
+    result = torch.empty(int(deg_np.sum()), dtype=torch.int32, device="cuda")
+    c_l = _median_call_ms(lambda: gu.lbs(counts, scanned, result), reps=5)
+    lbs_bytes = 4.0 * len(deg_np) * 2 + 4.0 * int(deg_np.sum())
+    sub = srcs[:cores]
+    _, cb = _cpu(oracle.bfs_multi, hg.R, hg.C, hg.n, sub, nthreads=cores)
+    _, cl = _cpu(oracle.lbs, deg_np)
+    _emit({"workload": "c4_grid2048_p005_256src", "metric": "multi-source BFS GTEPS (high diameter)",
+           "unit": "GTEPS", "value": edges / t_b / 1e6, "n": hg.n, "m_csr": hg.m, "sources": len(srcs),
+           "edges": edges, "diameter_of_sample": diam, "levels_td_bu_max": levels,
+           "bfs_batched_kernel_ms": t_b, "bfs_plain_kernel_ms": t_p, "plain_gteps": edges / t_p / 1e6,
+           "diameter_call_ms": c_d,
+           "lbs": {"N": len(deg_np), "total": int(deg_np.sum()), "call_ms": c_l,
+                   "alg_gbs": lbs_bytes / c_l / 1e6, "cpu_ms_1thread": cl * 1e3,
+                   "model": "4N counts + 4N scanned + 4 total result bytes"},
+           "cpu_bfs": {"gteps": (E / len(srcs) * len(sub) / 2.0) / cb / 1e9, "cores": cores,
+                       "sample": f"first {len(sub)} sources, per-source edges from the full set"}})
+
+
+def wl_c5(args):
+    import gu
+    import oracle
+    torch = _torch()
+    rng = np.random.default_rng(5)
+    # 12 R-MAT graphs, scales 12-18 and edge factors 8/16/32, and 4 random DAGs
+    # (n from 2^16 to 2^18, m = 8n): the resident set of a serving replica
+    rmats, dags = [], []
+    for i in range(12):
+        sc, ef = int(rng.integers(12, 19)), int(rng.choice([8, 16, 32]))
+        hg = gu.HostGraph.rmat(sc, ef, 0.57, 0.19, 0.19, seed=100 + i, permute=True)
+        rmats.append((f"rmat{sc}_ef{ef}_s{100 + i}", hg, gu.Graph(hg)))
+    for i in range(4):
+        n = int(2 ** rng.uniform(16, 18))
+        hg = gu.HostGraph.dag(n, 8 * n, seed=200 + i)
+        dags.append((f"dag{n}_s{200 + i}", hg, gu.Graph(hg)))
+    torch.cuda.synchronize()
+    results = []
+    cpu_ms = []
+    import queue
+    import threading
+    for rate in (100.0, 400.0, 1600.0):
+        srv = gu.Server(hbm_budget_bytes=64 << 30, slots=4, max_batch=1024)
+        plan, t = [], 0.0
+        dur = 2.0
+        while t < dur:
+            t += float(rng.exponential(1.0 / rate))
+            u = rng.random()
+            if u < 0.6:
+                name, hg, g = rmats[int(rng.integers(len(rmats)))]
+                k = int(rng.integers(1, 257))
+                plan.append((t, gu.QUERY_BFS, hg, g, rng.choice(hg.n, k, replace=False).astype(np.int32)))
+            elif u < 0.8:
+                name, hg, g = rmats[int(rng.integers(len(rmats)))]
+                k = int(rng.integers(64, 257))
+                plan.append((t, gu.QUERY_BC, hg, g, rng.choice(hg.n, k, replace=False).astype(np.int32)))
+            else:
+                name, hg, g = dags[int(rng.integers(len(dags)))]
+                k = int(rng.integers(1, 257))
+                plan.append((t, gu.QUERY_REACH, hg, g, rng.choice(hg.n, k, replace=False).astype(np.int32)))
+        pending = queue.Queue()
+
+        def waiter():  # waits in submission order, so finished outputs are released as it goes
+            while True:
+                rid = pending.get()
+                if rid is None:
+                    return
+                srv.wait(rid)
+
+        th = threading.Thread(target=waiter)
+        th.start()
+        t0 = time.perf_counter()
+        for (ta, q, hg, g, srcs) in plan:
+            now = time.perf_counter() - t0
+            if ta > now:
+                time.sleep(ta - now)
+            if q == gu.QUERY_BFS:
+                out = np.empty((len(srcs), hg.n), np.int32)
+            elif q == gu.QUERY_BC:
+                out = np.empty(hg.n, np.float64)
+            else:
+                out = np.empty(len(srcs), np.int64)
+            pending.put(srv.submit(g, q, srcs, out))
+        pending.put(None)
+        th.join()
+        wall = time.perf_counter() - t0
+        st = srv.stats()
+        srv.close()
+        results.append({"offered_rate_per_s": rate, "requests": len(plan), "wall_s": wall,
+                        "served_per_s": len(plan) / wall, "p50_ms": st["p50_s"] * 1e3,
+                        "p99_ms": st["p99_s"] * 1e3, "batches": st["batches"],
+                        "mean_requests_per_batch": st["mean_requests_per_batch"]})
+    # CPU: per-request oracle time on a sample of requests of each kind
+    for (t_, q, hg, g, srcs) in plan[:24]:
+        if q == gu.QUERY_BC:
+            _, c = _cpu(oracle.bc, hg.R, hg.C, hg.n, srcs[:8], nthreads=os.cpu_count() or 1)
+            c *= len(srcs) / 8.0
+        elif q == gu.QUERY_REACH:
+            _, c = _cpu(oracle.reach_count, hg.R, hg.C, hg.n, srcs, nthreads=os.cpu_count() or 1)
+        else:
+            _, c = _cpu(oracle.bfs_multi, hg.R, hg.C, hg.n, srcs, nthreads=os.cpu_count() or 1)
+        cpu_ms.append(c * 1e3)
+    _emit({"workload": "c5_serving_mix", "metric": "request latency p50 / p99", "unit": "ms",
+           "graphs": [n for n, _, _ in rmats + dags], "results": results,
+           "mix": "60% BFS rows (1-256 sources), 20% BC (64-256 sources), 20% DAG reachable counts (1-256)",
+           "cpu_per_request_ms_median": statistics.median(cpu_ms),
+           "cpu_sample": "first 24 requests of the last rate, oracle on all host threads (BC extrapolated "
+                         "from 8 sources per request)"})
+
+
+def run(workload, args):
+    {"c1": wl_c1, "c3": wl_c3, "c4": wl_c4, "c5": wl_c5}[workload](args)

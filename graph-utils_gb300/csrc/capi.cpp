@@ -571,4 +571,23 @@ gu_status gu_diameter(gu_graph g, const int32_t *sources_dev, int32_t k, int32_t
     });
 }
 
+gu_status gu_reach(gu_graph g, const int32_t *sources_dev, int32_t k, int64_t *counts_dev, void *stream)
+{
+    return guarded([&] {
+        if (!g || (k > 0 && !counts_dev)) throw gu_error(GU_ERR_INVALID_ARGUMENT, "null argument");
+        DeviceGraph &dg = *g->g;
+        std::lock_guard<std::mutex> lk(dg.mu);
+        DeviceScope ds(dg.device);
+        cudaStream_t st = (cudaStream_t)stream;
+        check_sources_device(dg, sources_dev, k, st);
+        if (k == 0) return;
+        GU_CUDA_CHECK(cudaMemsetAsync(counts_dev, 0, sizeof(int64_t) * (size_t)k, st));
+        MsOptions opt;
+        opt.variant = GU_BFS_AUTO;
+        opt.reach = reinterpret_cast<unsigned long long *>(counts_dev);
+        launch_msbfs(dg, sources_dev, k, nullptr, dg.n, opt, st, nullptr);
+        check_dev_status(dg, st);
+    });
+}
+
 }  // extern "C"

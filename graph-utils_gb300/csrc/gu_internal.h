@@ -147,6 +147,7 @@ struct MsOptions {
     Workspace *ws = nullptr;  // scratch to use (default: the graph's)
     int max_blocks = 0;       // cap on the persistent grid (0: the whole GPU)
     bool timed = true;        // record the graph's launch events
+    unsigned long long *reach = nullptr;  // device, k per-source reachable counts (zeroed by the caller)
 };
 
 // Per-call options of the batched sigma / Brandes engine.

@@ -117,6 +117,7 @@ struct MsArgs {
     const int32_t *sources;
     int32_t k;
     int32_t *dist;
+    unsigned long long *reach;  // per-source reachable-vertex counts (null: none)
     int64_t ld;
     u64 *seen;
     u64 *fr[3];
@@ -1383,6 +1384,47 @@ __device__ void write_distances(const MsArgs &a, int row0, int nb, int nplanes_u
     }
 }
 
+// Reachable-vertex count of every source of the batch (the source itself
+// included, reachability.cu:11-33), from seen at the end of the batch: a warp
+// takes 32 vertices, and for each of a word's 64 sources one ballot over the
+// lanes' seen words counts the 32 vertices at once; lane b keeps sources b and
+// b + 32.  Per-CTA sums in shared memory, one global atomic per source per CTA.
+template <int W, class G>
+__device__ void count_reached(const MsArgs &a, int row0, int nb)
+{
+    __shared__ unsigned long long s_cnt[64 * MAXW];
+    for (int i = threadIdx.x; i < 64 * W; i += blockDim.x) s_cnt[i] = 0;
+    __syncthreads();
+    const int lane = lane_id();
+    const long long nw = G::size() >> 5;
+    unsigned c[2 * W] = {};
+    for (long long base = (G::rank() >> 5) * 32; base < a.n; base += nw * 32) {  // warp-uniform
+        const long long v = base + lane;
+        u64 sw[W] = {};
+        if (v < a.n) ldw<W>(a.seen + (size_t)v * W, sw);
+#pragma unroll
+        for (int q = 0; q < W; ++q) {
+            for (int b = 0; b < 32; ++b) {
+                const unsigned lo = __ballot_sync(FULL_MASK, (sw[q] >> b) & 1ull);
+                const unsigned hi = __ballot_sync(FULL_MASK, (sw[q] >> (b + 32)) & 1ull);
+                if (lane == b) {
+                    c[2 * q] += __popc(lo);
+                    c[2 * q + 1] += __popc(hi);
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < W; ++q) {
+        if (c[2 * q]) atomicAdd(&s_cnt[64 * q + lane], (unsigned long long)c[2 * q]);
+        if (c[2 * q + 1]) atomicAdd(&s_cnt[64 * q + 32 + lane], (unsigned long long)c[2 * q + 1]);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < nb; i += blockDim.x)
+        if (s_cnt[i]) atomicAdd(a.reach + row0 + i, s_cnt[i]);
+    __syncthreads();
+}
+
 template <int VARIANT, int W>
 __global__ void __launch_bounds__(MS_THREADS, MS_MIN_BLOCKS) ms_grid_kernel(MsArgs a)
 {
@@ -1576,7 +1618,8 @@ __global__ void __launch_bounds__(MS_THREADS, MS_MIN_BLOCKS) ms_grid_kernel(MsAr
         // F_{j-1} is empty: levels of this batch are 0..j-2
         int used = 0;
         while (used < 31 && ((j - 2) >> used) != 0) ++used;
-        if (a.dist) write_distances<W, GridG>(a, row0, nb, used);  // no rows: diameter queries
+        if (a.dist) write_distances<W, GridG>(a, row0, nb, used);  // no rows: diameter, reach queries
+        if (a.reach) count_reached<W, GridG>(a, row0, nb);
         if (threadIdx.x == 0) record_event(ctl, ev_idx, rank == 0, b, j, 2, 0, 0);  // distance rows written
         ++ev_idx;
         if (!barrier()) return;
@@ -1677,6 +1720,7 @@ void launch_msbfs(DeviceGraph &g, const int32_t *sources, int32_t k, int32_t *di
     a.sources = sources;
     a.k = k;
     a.dist = dist;
+    a.reach = opt.reach;
     a.ld = ld;
     char *p = ws;
     a.ctl = reinterpret_cast<MsCtl *>(p);
@@ -1879,6 +1923,7 @@ static void bfs_noalloc(const int32_t *R, const int32_t *C, int32_t n, int64_t m
     a.sources = sources;
     a.k = k;
     a.dist = dist;
+    a.reach = nullptr;
     a.ld = ld;
     char *p = scratch;
     a.ctl = reinterpret_cast<MsCtl *>(p);

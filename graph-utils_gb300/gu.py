@@ -16,7 +16,7 @@ LIB_PATH = os.path.join(_HERE, "lib", "libgu_gb300.so")
 
 OK = 0
 STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "out of memory", 4: "capacity exceeded",
-          5: "overflow", 6: "device wait timed out", 7: "unsupported", 8: "internal error"}
+          5: "overflow", 6: "device wait timed out", 7: "unsupported", 8: "internal error", 9: "pending"}
 
 BFS_AUTO, BFS_LINEAR, BFS_EDGE, BFS_WARP, BFS_CTA_WARP, BFS_SCAN, BFS_SHUFFLE, BFS_BOTTOM_UP, BFS_PLAIN = range(9)
 VARIANTS = {"auto": BFS_AUTO, "linear": BFS_LINEAR, "edge": BFS_EDGE, "warp": BFS_WARP,
@@ -81,6 +81,7 @@ def lib():
         "gu_sigma": ([_vp, _vp, ctypes.c_int32, _vp, _vp, ctypes.c_int64, _vp], ctypes.c_int),
         "gu_bc": ([_vp, _vp, ctypes.c_int32, ctypes.c_int32, _vp, _vp, ctypes.c_int64, _vp], ctypes.c_int),
         "gu_diameter": ([_vp, _vp, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32), _vp], ctypes.c_int),
+        "gu_reach": ([_vp, _vp, ctypes.c_int32, _vp, _vp], ctypes.c_int),
         "gu_lbs": ([_vp, ctypes.c_int32, _vp, _vp, ctypes.c_int64, _vp, _i64p, _vp], ctypes.c_int),
         "gu_race_and_resolve": ([_vp, ctypes.c_int32, _vp, _vp], ctypes.c_int),
         "gu_server_create": ([ctypes.c_size_t, ctypes.c_int, ctypes.c_int, ctypes.POINTER(_vp)], ctypes.c_int),
@@ -258,6 +259,11 @@ class Graph:
         check(lib().gu_diameter(self._h, sources_dev.data_ptr(), int(sources_dev.numel()), ctypes.byref(d),
                                 _stream_handle(stream)))
         return d.value
+
+    def reach(self, sources_dev, counts_dev, stream=None):
+        """counts_dev (int64 cuda tensor, k): vertices reachable from each source, itself included."""
+        check(lib().gu_reach(self._h, sources_dev.data_ptr(), int(sources_dev.numel()), counts_dev.data_ptr(),
+                             _stream_handle(stream)))
 
     def bfs_host(self, sources_host, variant="auto", out=None, stream=None):
         """Host form: numpy sources in, numpy k x n int32 distances out."""

@@ -172,6 +172,13 @@ gu_status gu_bc(gu_graph g, const int32_t *sources_dev, int32_t k, int32_t batch
  * diameter_sampling_setup (diameter_sampling/diameter_sampling.cuh:13). */
 gu_status gu_diameter(gu_graph g, const int32_t *sources_dev, int32_t k, int32_t *diameter, void *stream);
 
+/* counts_dev[i] (int64) = number of vertices reachable from sources_dev[i],
+ * the source included (reachability.cu:11-33 counts reachable ordered pairs,
+ * self pairs included), without materialising distance rows.  The counting
+ * form of transitive_closure_setup (transitive_closure/transitive_closure.cuh:13),
+ * whose rows gu_bfs returns. */
+gu_status gu_reach(gu_graph g, const int32_t *sources_dev, int32_t k, int64_t *counts_dev, void *stream);
+
 /* ---- load-balanced search and race-and-resolve ------------------------------- */
 /* Load-balanced search over N work counts (device pointers, counts >= 0):
  * scanned_dev[i] = exclusive prefix sum of counts (int32), total = sum, and
