@@ -104,8 +104,8 @@ def wl_c1(args):
         _, b1 = _cpu(oracle.bc, hg.R, hg.C, hg.n, srcs, nthreads=1)
         _, bN = _cpu(oracle.bc, hg.R, hg.C, hg.n, srcs, nthreads=cores)
         out[name] = {"n": hg.n, "m_csr": hg.m, "sources": len(srcs), "edges_per_bfs": edges,
-                     "bfs_batched_kernel_ms": t_b, "bfs_plain_kernel_ms": t_p,
-                     "bfs_batched_gteps": edges / t_b / 1e6, "bfs_plain_gteps": edges / t_p / 1e6,
+                     "bfs_auto_kernel_ms": t_b, "bfs_plain_kernel_ms": t_p,
+                     "bfs_auto_gteps": edges / t_b / 1e6, "bfs_plain_gteps": edges / t_p / 1e6,
                      "bc_kernel_ms": t_bc, "bc_call_ms": c_bc, "bc_gteps": edges / t_bc / 1e6,
                      "cpu_bfs_ms_1thread": t1 * 1e3, f"cpu_bfs_ms_{cores}threads": tN * 1e3,
                      "cpu_bc_f64_ms_1thread": b1 * 1e3, f"cpu_bc_f64_ms_{cores}threads": bN * 1e3}
@@ -187,7 +187,7 @@ def wl_c4(args):
     _emit({"workload": "c4_grid2048_p005_256src", "metric": "multi-source BFS GTEPS (high diameter)",
            "unit": "GTEPS", "value": edges / t_b / 1e6, "n": hg.n, "m_csr": hg.m, "sources": len(srcs),
            "edges": edges, "diameter_of_sample": diam, "levels_td_bu_max": levels,
-           "bfs_batched_kernel_ms": t_b, "bfs_plain_kernel_ms": t_p, "plain_gteps": edges / t_p / 1e6,
+           "bfs_auto_kernel_ms": t_b, "bfs_plain_kernel_ms": t_p, "plain_gteps": edges / t_p / 1e6,
            "diameter_call_ms": c_d,
            "lbs": {"N": len(deg_np), "total": int(deg_np.sum()), "call_ms": c_l,
                    "alg_gbs": lbs_bytes / c_l / 1e6, "cpu_ms_1thread": cl * 1e3,

@@ -328,6 +328,17 @@ static void bfs_device(DeviceGraph &g, int variant, const int32_t *sources_dev, 
         GU_CUDA_CHECK(cudaGetLastError());
         return;
     }
+    if (variant == GU_BFS_AUTO) {
+        const AutoEngine eng = auto_engine(g, true);
+        if (eng == AutoEngine::LOCAL && launch_local_bfs(g, sources_dev, k, dist_dev, ld, nullptr, nullptr, stream))
+            return;
+        if (eng == AutoEngine::PLAIN) {
+            launch_plain_bfs(g, sources_dev, k, dist_dev, ld, stream);
+            GU_CUDA_CHECK(cudaStreamSynchronize(stream));
+            GU_CUDA_CHECK(cudaGetLastError());
+            return;
+        }
+    }
     MsOptions opt;
     opt.variant = variant;
     launch_msbfs(g, sources_dev, k, dist_dev, ld, opt, stream, nullptr);
@@ -561,11 +572,17 @@ gu_status gu_diameter(gu_graph g, const int32_t *sources_dev, int32_t k, int32_t
         check_sources_device(dg, sources_dev, k, st);
         *diameter = 0;
         if (k == 0) return;
+        int ml = 0;
+        if (auto_engine(dg, false) == AutoEngine::LOCAL &&
+            launch_local_bfs(dg, sources_dev, k, nullptr, dg.n, nullptr, &ml, st)) {
+            *diameter = ml;
+            return;
+        }
         MsOptions opt;
         opt.variant = GU_BFS_AUTO;
         launch_msbfs(dg, sources_dev, k, nullptr, dg.n, opt, st, nullptr);
         check_dev_status(dg, st);
-        int err = 0, td = 0, bu = 0, ml = 0;
+        int err = 0, td = 0, bu = 0;
         msbfs_read_status(dg, &err, &td, &bu, &ml);
         *diameter = ml;
     });
@@ -582,9 +599,14 @@ gu_status gu_reach(gu_graph g, const int32_t *sources_dev, int32_t k, int64_t *c
         check_sources_device(dg, sources_dev, k, st);
         if (k == 0) return;
         GU_CUDA_CHECK(cudaMemsetAsync(counts_dev, 0, sizeof(int64_t) * (size_t)k, st));
+        auto *cnt = reinterpret_cast<unsigned long long *>(counts_dev);
+        if (auto_engine(dg, false) == AutoEngine::LOCAL &&
+            launch_local_bfs(dg, sources_dev, k, nullptr, dg.n, cnt, nullptr, st))
+            return;
+        GU_CUDA_CHECK(cudaMemsetAsync(counts_dev, 0, sizeof(int64_t) * (size_t)k, st));
         MsOptions opt;
         opt.variant = GU_BFS_AUTO;
-        opt.reach = reinterpret_cast<unsigned long long *>(counts_dev);
+        opt.reach = cnt;
         launch_msbfs(dg, sources_dev, k, nullptr, dg.n, opt, st, nullptr);
         check_dev_status(dg, st);
     });

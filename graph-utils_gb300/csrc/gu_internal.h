@@ -165,6 +165,13 @@ void launch_msbfs(DeviceGraph &g, const int32_t *sources, int32_t k, int32_t *di
                   const MsOptions &opt, cudaStream_t stream, int *dev_err_out);
 void launch_plain_bfs(DeviceGraph &g, const int32_t *sources, int32_t k, int32_t *dist, int64_t ld,
                       cudaStream_t stream);
+// Per-source engine for low-degree graphs (AUTO's choice there): rows
+// (dist non-null) or counts (reach, deepest level).  Synchronises; returns false
+// if a frontier overflowed its shared queues (rerun on the batched engine).
+enum class AutoEngine { LOCAL, PLAIN, BATCHED };
+AutoEngine auto_engine(const DeviceGraph &g, bool rows);
+bool launch_local_bfs(DeviceGraph &g, const int32_t *sources, int32_t k, int32_t *dist, int64_t ld,
+                      unsigned long long *reach, int *max_level_host, cudaStream_t stream);
 // Batched sigma / Brandes: bc (n doubles, may be null), optional rows (k x ld).
 void launch_bc(DeviceGraph &g, const int32_t *sources, int32_t k, const BcOptions &opt, double *bc, int32_t *dist_rows,
                uint64_t *sigma_rows, double *delta_rows, int64_t ld, bool backward, cudaStream_t stream);

@@ -48,7 +48,10 @@ typedef enum gu_status {
  *   SCAN      block-scan ranked gather     (multi_search/scan_based.cu:43-194)
  *   SHUFFLE   warp per vertex, dynamic queue (multi_search/shuffle_based.cuh:81-286)
  *   BOTTOM_UP frontier bitmap pull (no reference counterpart)
- *   AUTO      per-level direction and gather choice (autotuned)
+ *   AUTO      engine by graph shape -- per-source BFS with shared-memory queues
+ *             for out-degree <= 16 (meshes; falls back on frontier overflow), the
+ *             PLAIN form for n <= 4096, else the batched engine with per-level
+ *             direction and gather choice
  *   PLAIN     one CTA per source, int32 distance row as the visited set -- the
  *             reference's own structure, kept as the one-launch-per-request baseline.
  * All but PLAIN run 64 sources per bitmap word in one persistent launch. */

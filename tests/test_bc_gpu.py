@@ -122,7 +122,10 @@ def test_directed_dag_bc():
     close(bc, oracle.bc(hg.R, hg.C, hg.n, srcs, pull=True, nthreads=8))
 
 
-def test_diameter(golden_graphs):
+@pytest.mark.parametrize("engine", ["auto", "batched"])
+def test_diameter(golden_graphs, engine, monkeypatch):
+    if engine == "batched":  # AUTO would take the per-source engine on these graphs
+        monkeypatch.setenv("GU_AUTO_LOCAL", "0")
     for name, (g, d) in golden_graphs.items():
         assert g.diameter(dev(d["sources"].astype(np.int32))) == int(d["diameter"]), name
     hg = gu.HostGraph.grid(60, 50, 0.05, seed=7)

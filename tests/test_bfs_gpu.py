@@ -4,6 +4,8 @@ Distances must be bit-exact.  Small cases compare against the golden vectors
 of the reference's own checkers and against oracle/gu_oracle.c; the full-size
 R-MAT scale-20 case is checked through BFS certificates that hold at any size.
 """
+import os
+
 import numpy as np
 import pytest
 
@@ -14,7 +16,10 @@ from conftest import golden_names, load_golden
 torch = pytest.importorskip("torch")
 pytestmark = pytest.mark.gpu
 
-VARIANTS = ["auto", "linear", "edge", "warp", "cta_warp", "scan", "shuffle", "bottom_up", "plain"]
+# "auto" lets AUTO pick its engine (the per-source one on small or low-degree
+# graphs); "auto_batched" keeps AUTO on the batched bit-matrix engine
+# (GU_AUTO_LOCAL=0), so both engines are checked on the same graphs.
+VARIANTS = ["auto", "auto_batched", "linear", "edge", "warp", "cta_warp", "scan", "shuffle", "bottom_up", "plain"]
 
 
 def run_bfs(g, srcs, variant, ld=None):
@@ -22,7 +27,14 @@ def run_bfs(g, srcs, variant, ld=None):
     s = torch.as_tensor(np.asarray(srcs, np.int32), device=dev)
     ld = g.n if ld is None else ld
     out = torch.full((max(len(srcs), 1), ld), -7, dtype=torch.int32, device=dev)
-    g.bfs(s, out, variant=variant, ld=ld)
+    if variant == "auto_batched":
+        os.environ["GU_AUTO_LOCAL"] = "0"
+        try:
+            g.bfs(s, out, variant="auto", ld=ld)
+        finally:
+            del os.environ["GU_AUTO_LOCAL"]
+    else:
+        g.bfs(s, out, variant=variant, ld=ld)
     torch.cuda.synchronize()
     return out[: len(srcs), : g.n].cpu().numpy(), out.cpu().numpy()
 
@@ -54,7 +66,7 @@ def test_rmat14_vs_oracle(variant):
     np.testing.assert_array_equal(got, ref)
 
 
-@pytest.mark.parametrize("variant", ["auto", "linear", "scan", "bottom_up", "plain"])
+@pytest.mark.parametrize("variant", ["auto", "auto_batched", "linear", "scan", "bottom_up", "plain"])
 def test_grid_high_diameter_vs_oracle(variant):
     hg = gu.HostGraph.grid(96, 80, 0.05, seed=7)
     g = gu.Graph(hg)
@@ -64,7 +76,7 @@ def test_grid_high_diameter_vs_oracle(variant):
     np.testing.assert_array_equal(got, ref)
 
 
-@pytest.mark.parametrize("variant", ["auto", "shuffle", "bottom_up", "edge"])
+@pytest.mark.parametrize("variant", ["auto", "auto_batched", "shuffle", "bottom_up", "edge"])
 def test_directed_dag_vs_oracle(variant):
     hg = gu.HostGraph.dag(5000, 40000, seed=4)
     g = gu.Graph(hg)
@@ -98,9 +110,12 @@ def test_edge_cases():
     assert e.value.status == 1
 
 
+@pytest.mark.parametrize("engine", ["auto", "batched"])
 @pytest.mark.parametrize("kind", ["rmat", "dag", "jazz"])
-def test_reach_counts_vs_oracle(kind, golden_graphs):
+def test_reach_counts_vs_oracle(kind, engine, golden_graphs, monkeypatch):
     """gu_reach counts (source included) equal the oracle's reachable pairs per source."""
+    if engine == "batched":
+        monkeypatch.setenv("GU_AUTO_LOCAL", "0")
     if kind == "rmat":
         hg = gu.HostGraph.rmat(14, 8, seed=6)
         srcs = gu.sources(hg.n, 300, seed=7)  # two batches of the 256-source engine
@@ -120,6 +135,23 @@ def test_reach_counts_vs_oracle(kind, golden_graphs):
     np.testing.assert_array_equal(got, ref)
     if kind == "jazz":
         assert got.sum() == 39204  # reachability.cu known answer: every ordered pair
+
+
+def test_per_source_engine_overflow_falls_back():
+    """A low-degree graph whose frontiers outgrow the per-source engine's shared
+    queues (an expander: ER with mean degree 3) is rerun on the batched engine."""
+    hg = gu.HostGraph.er(200000, 300000, seed=11)
+    assert hg.degrees().max() <= 16  # AUTO picks the per-source engine first
+    g = gu.Graph(hg)
+    srcs = gu.sources(hg.n, 40, seed=3)
+    ref, _ = oracle.bfs_multi(hg.R, hg.C, hg.n, srcs, nthreads=8)
+    got, _ = run_bfs(g, srcs, "auto")
+    np.testing.assert_array_equal(got, ref)
+    s = torch.as_tensor(srcs, device="cuda")
+    assert g.diameter(s) == int(ref[ref != gu.UNREACHABLE].max())
+    cnt = torch.empty(len(srcs), dtype=torch.int64, device="cuda")
+    g.reach(s, cnt)
+    np.testing.assert_array_equal(cnt.cpu().numpy(), (ref != gu.UNREACHABLE).sum(1))
 
 
 def test_host_form_matches_device_form():
