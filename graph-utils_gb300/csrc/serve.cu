@@ -2,17 +2,19 @@
 //
 // Requests (BFS rows, BC over a source set, reachable-vertex counts) arrive from
 // any host thread.  A worker thread keeps a FIFO of pending requests and a fixed
-// set of slots (stream, workspace, pinned staging).  Whenever a slot is free it
-// forms a batch from the oldest pending request and every later pending request
-// of the same graph and kind (up to max_batch sources; a larger request runs
-// alone), admits it if the batch's device footprint (engine workspace + rows)
+// set of slots (stream, workspace, pinned staging of the inputs).  Whenever a
+// slot is free it forms a batch from the oldest pending request and every later
+// pending request of the same graph and kind (up to max_batch sources; a larger
+// request runs alone), admits it if the batch's device footprint (engine workspace + rows)
 // fits the HBM budget next to the batches already running, and launches it on
 // the slot's stream with a persistent grid of 1/slots of the GPU, so batches of
 // different slots overlap on the device.  Requests that arrive while batches
 // run are admitted as slots and memory free up.  Per-request state lives on the
 // device for the batch's lifetime: BFS requests own contiguous row ranges, BC
 // requests own contiguous source ranges with their own bc vector
-// (BcOptions::req_start), reachability requests own contiguous count ranges.
+// (BcOptions::req_start), reachability requests own contiguous count ranges
+// (counted in the kernel, no rows).  Each request's result is copied from the
+// device straight into its own host buffer on the slot's stream.
 // A request's result does not depend on its batch-mates: BFS rows and counts
 // are exact; BC sums its sources in batch order, within 1e-12 of running alone.
 #include "device_utils.cuh"
@@ -35,25 +37,6 @@ int msbfs_ws_error(const Workspace &ws);
 int bc_ws_error(const Workspace &ws);
 
 using Clock = std::chrono::steady_clock;
-
-__global__ void count_reached_kernel(const int32_t *__restrict__ dist, int32_t n, int32_t k, long long *__restrict__ counts)
-{
-    __shared__ long long s_warp[32];
-    for (int r = blockIdx.x; r < k; r += gridDim.x) {
-        long long c = 0;
-        for (int32_t v = threadIdx.x; v < n; v += blockDim.x) c += dist[(int64_t)r * n + v] != INT_MAX;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(FULL_MASK, c, o);
-        if (lane_id() == 0) s_warp[warp_in_block()] = c;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            long long t = 0;
-            for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += s_warp[w];
-            counts[r] = t;
-        }
-        __syncthreads();
-    }
-}
 
 struct SRequest {
     int64_t id = 0;
@@ -96,7 +79,9 @@ struct Slot {
     DeviceGraph *g = nullptr;
     std::vector<SRequest *> reqs;
     size_t need = 0;
-    size_t out_off = 0;  // byte offset of the outputs in stage
+    char *dres = nullptr;  // device results of the running batch, request after request
+    bool copying = false;  // kernels done, results being copied out by the copier thread
+    cudaError_t done_status = cudaSuccess;
 };
 
 class Server {
@@ -113,6 +98,7 @@ public:
             GU_CUDA_CHECK(cudaEventCreateWithFlags(&s.ev, cudaEventDisableTiming));
         }
         worker_ = std::thread([this] { loop(); });
+        copier_ = std::thread([this] { copy_loop(); });
     }
 
     ~Server()
@@ -122,7 +108,13 @@ public:
             stop_ = true;
         }
         cv_work_.notify_all();
-        if (worker_.joinable()) worker_.join();
+        if (worker_.joinable()) worker_.join();  // returns once every slot's results are out
+        {
+            std::lock_guard<std::mutex> lk(mu_);
+            stop_copier_ = true;
+        }
+        cv_copy_.notify_all();
+        if (copier_.joinable()) copier_.join();
         cudaSetDevice(device_);
         for (Slot &s : slots_) {
             if (s.st) cudaStreamSynchronize(s.st);
@@ -202,7 +194,6 @@ private:
     {
         size_t ws = kind == GU_QUERY_BC ? bc_workspace_bytes(g, k, 0, true) : msbfs_workspace_bytes(g, k);
         size_t io = (size_t)k * 4 + (size_t)(nreq + 1) * 4 + 1024 + out_bytes;
-        if (kind == GU_QUERY_REACH) io += (size_t)k * (size_t)g.n * sizeof(int32_t);  // rows before counting
         return ws + io;
     }
 
@@ -282,10 +273,10 @@ private:
     {
         GU_CUDA_CHECK(cudaSetDevice(device_));
         const int nreq = (int)batch.size();
-        // pinned staging: sources | request offsets | outputs
+        // pinned staging of the inputs: sources | request offsets
         const size_t src_b = ((size_t)k * 4 + 255) / 256 * 256;
         const size_t off_b = ((size_t)(nreq + 1) * 4 + 255) / 256 * 256;
-        char *stage = (char *)s.stage.get(src_b + off_b + out_bytes + 256);
+        char *stage = (char *)s.stage.get(src_b + off_b + 256);
         int32_t *hs = reinterpret_cast<int32_t *>(stage);
         int32_t *hoff = reinterpret_cast<int32_t *>(stage + src_b);
         int32_t pos = 0;
@@ -295,15 +286,12 @@ private:
             pos += (int32_t)batch[i]->src.size();
         }
         hoff[nreq] = pos;
-        s.out_off = src_b + off_b;
-        // device io: sources | offsets | rows or bc | counts
-        const size_t rows_b = (kind == GU_QUERY_BC) ? (size_t)nreq * g.n * sizeof(double)
-                                                    : ((size_t)k * g.n * sizeof(int32_t) + 255) / 256 * 256;
-        const size_t cnt_b = kind == GU_QUERY_REACH ? (size_t)k * sizeof(long long) : 0;
-        char *io = (char *)s.io.get(src_b + off_b + rows_b + cnt_b + 256);
+        // device io: sources | offsets | outputs (BFS rows, bc vectors or reachable counts)
+        const size_t res_b = (out_bytes + 255) / 256 * 256;
+        char *io = (char *)s.io.get(src_b + off_b + res_b + 256);
         int32_t *dsrc = reinterpret_cast<int32_t *>(io);
         int32_t *doff = reinterpret_cast<int32_t *>(io + src_b);
-        char *drows = io + src_b + off_b;
+        char *dres = io + src_b + off_b;
         GU_CUDA_CHECK(cudaMemcpyAsync(dsrc, hs, src_b + off_b, cudaMemcpyHostToDevice, s.st));
         {
             std::lock_guard<std::mutex> glk(g.mu);  // lazily built graph-side structures
@@ -314,24 +302,23 @@ private:
                 o.timed = false;
                 o.req_start = doff;
                 o.nreq = nreq;
-                launch_bc(g, dsrc, k, o, reinterpret_cast<double *>(drows), nullptr, nullptr, nullptr, g.n, true, s.st);
+                launch_bc(g, dsrc, k, o, reinterpret_cast<double *>(dres), nullptr, nullptr, nullptr, g.n, true, s.st);
             } else {
                 MsOptions o;
                 o.variant = GU_BFS_AUTO;
                 o.ws = &s.ws;
                 o.max_blocks = blocks_per_slot_;
                 o.timed = false;
-                launch_msbfs(g, dsrc, k, reinterpret_cast<int32_t *>(drows), g.n, o, s.st, nullptr);
+                if (kind == GU_QUERY_REACH) {  // counts in the kernel, no rows
+                    GU_CUDA_CHECK(cudaMemsetAsync(dres, 0, out_bytes, s.st));
+                    o.reach = reinterpret_cast<unsigned long long *>(dres);
+                    launch_msbfs(g, dsrc, k, nullptr, g.n, o, s.st, nullptr);
+                } else {
+                    launch_msbfs(g, dsrc, k, reinterpret_cast<int32_t *>(dres), g.n, o, s.st, nullptr);
+                }
             }
         }
-        if (kind == GU_QUERY_REACH) {
-            long long *dcnt = reinterpret_cast<long long *>(drows + rows_b);
-            count_reached_kernel<<<std::min(k, 4096), 256, 0, s.st>>>(reinterpret_cast<int32_t *>(drows), g.n, k, dcnt);
-            GU_CUDA_CHECK(cudaGetLastError());
-            GU_CUDA_CHECK(cudaMemcpyAsync(stage + s.out_off, dcnt, (size_t)k * sizeof(long long), cudaMemcpyDeviceToHost, s.st));
-        } else {
-            GU_CUDA_CHECK(cudaMemcpyAsync(stage + s.out_off, drows, out_bytes, cudaMemcpyDeviceToHost, s.st));
-        }
+        s.dres = dres;
         GU_CUDA_CHECK(cudaEventRecord(s.ev, s.st));
         s.busy = true;
         s.kind = kind;
@@ -339,39 +326,71 @@ private:
         s.reqs = batch;
     }
 
-    // Completes slot s's batch if its work is done (mu_ held).
+    // Hands slot s's batch to the copier once its kernels are done (mu_ held).
     bool poll(Slot &s)
     {
-        if (!s.busy) return false;
+        if (!s.busy || s.copying) return false;
         const cudaError_t q = cudaEventQuery(s.ev);
         if (q == cudaErrorNotReady) return false;
-        gu_status st = GU_OK;
-        std::string err;
-        if (q != cudaSuccess) {
-            st = GU_ERR_CUDA;
-            err = cudaGetErrorString(q);
-        } else {
-            const int e = s.kind == GU_QUERY_BC ? bc_ws_error(s.ws) : msbfs_ws_error(s.ws);
-            if (e == DEV_ERR_BARRIER_TIMEOUT) {
-                st = GU_ERR_TIMEOUT;
-                err = "a device-side wait exceeded its limit";
-            } else if (e != 0) {
-                st = e == 3 && s.kind == GU_QUERY_BC ? GU_ERR_CAPACITY : GU_ERR_INTERNAL;
-                err = "device reported error code " + std::to_string(e);
-            }
-        }
-        const char *out = (const char *)s.stage.p + s.out_off;
-        size_t off = 0;
-        for (SRequest *r : s.reqs) {
-            const size_t b = row_bytes(r);
-            if (st == GU_OK) std::memcpy(r->out, out + off, b);
-            off += b;
-            finish(r, st, err);
-        }
-        s.busy = false;
-        s.reqs.clear();
-        cv_done_.notify_all();
+        s.done_status = q;
+        s.copying = true;
+        done_q_.push_back(&s);
+        cv_copy_.notify_one();
         return true;
+    }
+
+    // Copies finished batches' results from the device straight into each
+    // request's own host buffer, outside the server lock: on a coherent host
+    // link a copy into pageable memory may run synchronously, and the worker
+    // must keep launching meanwhile.
+    void copy_loop()
+    {
+        cudaSetDevice(device_);
+        std::unique_lock<std::mutex> lk(mu_);
+        while (true) {
+            cv_copy_.wait(lk, [&] { return !done_q_.empty() || stop_copier_; });
+            if (done_q_.empty()) break;
+            Slot &s = *done_q_.front();
+            done_q_.pop_front();
+            const std::vector<SRequest *> reqs = s.reqs;
+            lk.unlock();
+            gu_status st = GU_OK;
+            std::string err;
+            if (s.done_status != cudaSuccess) {
+                st = GU_ERR_CUDA;
+                err = cudaGetErrorString(s.done_status);
+            } else {
+                const int e = s.kind == GU_QUERY_BC ? bc_ws_error(s.ws) : msbfs_ws_error(s.ws);
+                if (e == DEV_ERR_BARRIER_TIMEOUT) {
+                    st = GU_ERR_TIMEOUT;
+                    err = "a device-side wait exceeded its limit";
+                } else if (e != 0) {
+                    st = e == 3 && s.kind == GU_QUERY_BC ? GU_ERR_CAPACITY : GU_ERR_INTERNAL;
+                    err = "device reported error code " + std::to_string(e);
+                }
+            }
+            if (st == GU_OK) {
+                size_t off = 0;
+                cudaError_t ce = cudaSuccess;
+                for (SRequest *r : reqs) {
+                    const size_t b = row_bytes(r);
+                    if (ce == cudaSuccess) ce = cudaMemcpyAsync(r->out, s.dres + off, b, cudaMemcpyDeviceToHost, s.st);
+                    off += b;
+                }
+                if (ce == cudaSuccess) ce = cudaStreamSynchronize(s.st);
+                if (ce != cudaSuccess) {
+                    st = GU_ERR_CUDA;
+                    err = cudaGetErrorString(ce);
+                }
+            }
+            lk.lock();
+            for (SRequest *r : reqs) finish(r, st, err);
+            s.reqs.clear();
+            s.copying = false;
+            s.busy = false;
+            cv_done_.notify_all();
+            cv_work_.notify_all();
+        }
     }
 
     void loop()
@@ -407,7 +426,10 @@ private:
     int64_t next_id_ = 0, completed_ = 0, batches_ = 0, batched_reqs_ = 0;
     std::vector<double> latencies_;
     bool stop_ = false;
-    std::thread worker_;
+    std::thread worker_, copier_;
+    std::condition_variable cv_copy_;
+    std::deque<Slot *> done_q_;
+    bool stop_copier_ = false;
 };
 
 Server *server_create(size_t budget, int nslots, int max_batch) { return new Server(budget, nslots, max_batch); }
