@@ -4,6 +4,7 @@
 // message (the reference exits the process instead, util_device.cuh:10-22).
 #include "gu_internal.h"
 
+#include <algorithm>
 #include <climits>
 #include <cstring>
 #include <functional>
@@ -391,10 +392,23 @@ gu_status gu_bfs_host(gu_graph g, int variant, const int32_t *sources_host, int3
         int32_t *d_src = reinterpret_cast<int32_t *>(io);
         int32_t *d_dist = reinterpret_cast<int32_t *>(io + src_bytes);
         GU_CUDA_CHECK(cudaMemcpyAsync(d_src, sources_host, sizeof(int32_t) * (size_t)k, cudaMemcpyHostToDevice, st));
-        bfs_device(dg, variant, d_src, k, d_dist, dg.n, st);
-        GU_CUDA_CHECK(cudaMemcpy2DAsync(dist_host, sizeof(int32_t) * (size_t)ld, d_dist, sizeof(int32_t) * (size_t)dg.n,
-                                        sizeof(int32_t) * (size_t)dg.n, (size_t)k, cudaMemcpyDeviceToHost, st));
-        GU_CUDA_CHECK(cudaStreamSynchronize(st));
+        // Rows leave the device while later sources are still being searched: the
+        // sources go in chunks (a small first one, so the host link starts early,
+        // then one 256-source engine batch each), each searched on `st`, and each
+        // chunk's rows are copied on the graph's copy stream once its search has
+        // finished.  The host link, not the search, then bounds the call.
+        if (!dg.copy_st) GU_CUDA_CHECK(cudaStreamCreateWithFlags(&dg.copy_st, cudaStreamNonBlocking));
+        const size_t row = sizeof(int32_t) * (size_t)dg.n;
+        int32_t b = 0;
+        while (b < k) {
+            const int32_t e = b == 0 ? std::min(k, 64) : std::min(k, b + 256);
+            bfs_device(dg, variant, d_src + b, e - b, d_dist + (size_t)b * dg.n, dg.n, st);  // synchronises st
+            GU_CUDA_CHECK(cudaMemcpy2DAsync(dist_host + (size_t)b * (size_t)ld, sizeof(int32_t) * (size_t)ld,
+                                            d_dist + (size_t)b * dg.n, row, row, (size_t)(e - b),
+                                            cudaMemcpyDeviceToHost, dg.copy_st));
+            b = e;
+        }
+        GU_CUDA_CHECK(cudaStreamSynchronize(dg.copy_st));
     });
 }
 

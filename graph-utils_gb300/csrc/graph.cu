@@ -75,6 +75,7 @@ DeviceGraph::~DeviceGraph()
     cudaSetDevice(device);
     if (ev_start) cudaEventDestroy(ev_start);
     if (ev_stop) cudaEventDestroy(ev_stop);
+    if (copy_st) cudaStreamDestroy(copy_st);
     ws.release();
     io.release();
     if (F) cudaFree(F);

@@ -128,6 +128,7 @@ struct DeviceGraph {
     std::vector<void *> extra_allocs;  // freed with the graph
     // events bracketing the last main kernel launch (kernel-only timing)
     cudaEvent_t ev_start = nullptr, ev_stop = nullptr;
+    cudaStream_t copy_st = nullptr;  // host-form calls copy rows out on it while later sources run
     bool timed = false;
     void mark_start(cudaStream_t s);
     void mark_stop(cudaStream_t s);
