@@ -49,8 +49,8 @@ def parse_args():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cpu-seconds", type=float, default=15.0, help="budget of the cpu_baseline sample")
     p.add_argument("--kernel-only", action="store_true", help="skip e2e (for profiling runs)")
-    p.add_argument("--workload", choices=["c2", "c1", "c3", "c4", "c5"], default="c2",
-                   help="c2: the headline BFS line (default); c1/c3/c4/c5: the other configurations, "
+    p.add_argument("--workload", choices=["c2", "c1", "c3", "c4", "c5", "io"], default="c2",
+                   help="c2: the headline BFS line (default); c1/c3/c4/c5/io: the other configurations, "
                         "one JSON line each (bench_configs.py)")
     return p.parse_args()
 

@@ -8,6 +8,8 @@
         load-balanced search over the int32 degree array.
     c5  serving: R-MAT graphs and random DAGs resident on the device, Poisson arrivals
         of BFS / BC / reachability requests at several rates, p50 / p99 latency.
+    io  graph files: R-MAT scale 20 as METIS / SNAP / MatrixMarket text and the
+        binary CSR cache, read by this library and by the reference parser.
 
 GPU times are CUDA-event kernel times of the library's own launch (`last_launch`)
 unless named `call_ms` (wall time of the synchronous C-ABI call).  CPU times are
@@ -291,5 +293,60 @@ def wl_c5(args):
                          "from 8 sources per request)"})
 
 
+def wl_io(args):
+    """Graph files at the boundary: R-MAT scale 20 (ef 16) written as METIS, SNAP
+    and MatrixMarket text and as the binary CSR cache, read back by this library
+    and -- where oracle/_ref holds the reference parser built from its sources --
+    by the reference parser (parse.cpp:88-441).  Host only."""
+    import subprocess
+    import tempfile
+    import gu
+    hg = gu.HostGraph.rmat(20, 16, 0.57, 0.19, 0.19, seed=1, permute=True)
+    ref = os.path.join(ROOT, "oracle", "_ref", "ref_oracle")
+    res = {}
+    with tempfile.TemporaryDirectory() as tmp:
+        files = {}
+        p = os.path.join(tmp, "g.graph")  # METIS: header, then 1-based neighbour lists
+        with open(p, "w") as f:
+            f.write(f"{hg.n} {hg.m // 2}\n")
+            for v in range(0, hg.n, 65536):
+                lo, hi = v, min(hg.n, v + 65536)
+                f.write("".join(" ".join(map(str, (hg.C[hg.R[u]:hg.R[u + 1]] + 1).tolist())) + "\n"
+                                for u in range(lo, hi)))
+        files["dimacs"] = p
+        # SNAP wants every id in 0..n-1 present: relabel away the isolated vertices
+        keep = np.diff(hg.R) > 0
+        newid = np.cumsum(keep) - 1
+        Rk = np.concatenate([[0], np.cumsum(np.diff(hg.R)[keep])]).astype(np.int32)
+        dense = gu.HostGraph(Rk, newid[hg.C].astype(np.int32), int(keep.sum()), True)
+        p = os.path.join(tmp, "g.txt")
+        dense.write_edgelist(p)
+        files["edgelist"] = p
+        p = os.path.join(tmp, "g.mtx")
+        src = np.repeat(np.arange(hg.n, dtype=np.int64), np.diff(hg.R))
+        keep = src < hg.C
+        with open(p, "w") as f:
+            f.write(f"%%MatrixMarket matrix coordinate pattern symmetric\n{hg.n} {hg.n} {int(keep.sum())}\n")
+            np.savetxt(f, np.stack([src[keep] + 1, hg.C[keep].astype(np.int64) + 1], 1), fmt="%d")
+        files["market"] = p
+        p = os.path.join(tmp, "g.csr")
+        hg.write_csr(p)
+        files["csrbin"] = p
+        for fmt, path in files.items():
+            mb = os.path.getsize(path) / 1e6
+            _, t = _cpu(gu.HostGraph.parse, path, fmt)
+            row = {"file_mb": mb, "ours_s": t, "ours_mb_per_s": mb / t}
+            if fmt != "csrbin" and os.path.exists(ref):
+                t0 = time.perf_counter()
+                subprocess.run([ref, "parse", path, fmt, os.path.join(tmp, "ref_" + fmt)], check=True,
+                               stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+                row["reference_s"] = time.perf_counter() - t0
+                row["speedup"] = row["reference_s"] / t
+            res[fmt] = row
+    _emit({"workload": "io_rmat20_ef16_graph_files", "metric": "graph file read time", "unit": "s",
+           "n": hg.n, "m_csr": hg.m, "results": res,
+           "note": "reference_s includes writing its CSR out (a few hundred MB), a small share"})
+
+
 def run(workload, args):
-    {"c1": wl_c1, "c3": wl_c3, "c4": wl_c4, "c5": wl_c5}[workload](args)
+    {"c1": wl_c1, "c3": wl_c3, "c4": wl_c4, "c5": wl_c5, "io": wl_io}[workload](args)

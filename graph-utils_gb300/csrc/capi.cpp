@@ -216,6 +216,53 @@ gu_status gu_hgraph_arrays(gu_hgraph h, const int32_t **R, const int32_t **C, in
     });
 }
 
+gu_status gu_hgraph_from_csr(const int32_t *R, const int32_t *C, int32_t n, int64_t m, int directed, gu_hgraph *out)
+{
+    return make_hgraph(out, [&] {
+        if (n < 0 || m < 0 || !R || (m > 0 && !C)) throw gu_error(GU_ERR_INVALID_ARGUMENT, "bad CSR arrays");
+        if (R[0] != 0 || R[n] != m) throw gu_error(GU_ERR_INVALID_ARGUMENT, "R must start at 0 and end at m");
+        for (int32_t v = 0; v < n; ++v)
+            if (R[v + 1] < R[v]) throw gu_error(GU_ERR_INVALID_ARGUMENT, "R must be non-decreasing");
+        for (int64_t e = 0; e < m; ++e)
+            if (C[e] < 0 || C[e] >= n) throw gu_error(GU_ERR_INVALID_ARGUMENT, "column index out of range");
+        HostGraph g;
+        g.n = n;
+        g.directed = directed != 0;
+        g.R.assign(R, R + n + 1);
+        g.C.assign(C, C + m);
+        return g;
+    });
+}
+
+gu_status gu_hgraph_parse(const char *path, const char *format, gu_hgraph *out)
+{
+    return make_hgraph(out, [&] { return parse_graph_file(path, format); });
+}
+
+gu_status gu_hgraph_write_csr(gu_hgraph h, const char *path)
+{
+    return guarded([&] {
+        if (!h) throw gu_error(GU_ERR_INVALID_ARGUMENT, "null graph");
+        write_csr_cache(h->h, path);
+    });
+}
+
+gu_status gu_hgraph_write_edgelist(gu_hgraph h, const char *path, int header)
+{
+    return guarded([&] {
+        if (!h) throw gu_error(GU_ERR_INVALID_ARGUMENT, "null graph");
+        write_edgelist(h->h, path, header != 0);
+    });
+}
+
+gu_status gu_hgraph_count_degree_zero(gu_hgraph h, uint64_t *count)
+{
+    return guarded([&] {
+        if (!h || !count) throw gu_error(GU_ERR_INVALID_ARGUMENT, "null argument");
+        *count = count_degree_zero(h->h);
+    });
+}
+
 gu_status gu_hgraph_destroy(gu_hgraph h)
 {
     delete h;

@@ -68,6 +68,11 @@ HostGraph gen_grid(int32_t rows, int32_t cols, double p_delete, uint64_t seed);
 HostGraph gen_dag(int32_t n, int64_t m, uint64_t seed);
 std::vector<int32_t> gen_sources(int32_t n, int32_t k, uint64_t seed);
 HostGraph transpose(const HostGraph &g);
+// Graph files (io.cpp): "dimacs"/"metis", "edgelist", "edgelist_h", "market", "csrbin".
+HostGraph parse_graph_file(const char *path, const char *format);
+void write_csr_cache(const HostGraph &g, const char *path);
+void write_edgelist(const HostGraph &g, const char *path, bool header);
+uint64_t count_degree_zero(const HostGraph &g);
 void sort_adjacency_by_key(const int32_t *R, int32_t *C, int32_t n, const int32_t *key);
 void build_csr(int32_t n, const std::vector<int32_t> &eu, const std::vector<int32_t> &ev, bool symmetric,
                std::vector<int32_t> &R, std::vector<int32_t> &C);

@@ -64,6 +64,12 @@ def lib():
         "gu_hgraph_arrays": ([_vp, ctypes.POINTER(_i32p), ctypes.POINTER(_i32p), _i32p, _i64p,
                               ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
         "gu_hgraph_destroy": ([_vp], ctypes.c_int),
+        "gu_hgraph_from_csr": ([_i32p, _i32p, ctypes.c_int32, ctypes.c_int64, ctypes.c_int, ctypes.POINTER(_vp)],
+                               ctypes.c_int),
+        "gu_hgraph_parse": ([ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(_vp)], ctypes.c_int),
+        "gu_hgraph_write_csr": ([_vp, ctypes.c_char_p], ctypes.c_int),
+        "gu_hgraph_write_edgelist": ([_vp, ctypes.c_char_p, ctypes.c_int], ctypes.c_int),
+        "gu_hgraph_count_degree_zero": ([_vp, ctypes.POINTER(ctypes.c_uint64)], ctypes.c_int),
         "gu_sources": ([ctypes.c_int32, ctypes.c_int32, ctypes.c_uint64, _i32p], ctypes.c_int),
         "gu_graph_create": ([_i32p, _i32p, ctypes.c_int32, ctypes.c_int64, ctypes.c_int, _vp, ctypes.POINTER(_vp)],
                             ctypes.c_int),
@@ -167,6 +173,39 @@ class HostGraph:
 
     def degrees(self):
         return np.diff(self.R)
+
+    @staticmethod
+    def parse(path, fmt):
+        """Read a graph file: "dimacs"/"metis", "edgelist", "edgelist_h", "market" or "csrbin"."""
+        h = _vp()
+        check(lib().gu_hgraph_parse(os.fsencode(path), fmt.encode(), ctypes.byref(h)))
+        return HostGraph._from_handle(h)
+
+    def _handle(self):
+        h = _vp()
+        check(lib().gu_hgraph_from_csr(_ptr(self.R), _ptr(self.C) if self.m else None, self.n, self.m,
+                                       int(self.directed), ctypes.byref(h)))
+        return h
+
+    def _with_handle(self, fn):
+        h = self._handle()
+        try:
+            return fn(h)
+        finally:
+            lib().gu_hgraph_destroy(h)
+
+    def write_csr(self, path):
+        """Binary CSR cache (read back with parse(path, "csrbin"))."""
+        self._with_handle(lambda h: check(lib().gu_hgraph_write_csr(h, os.fsencode(path))))
+
+    def write_edgelist(self, path, header=False):
+        """The reference's write_edgelist_to_file: optional "n m" line, "u v" per CSR entry."""
+        self._with_handle(lambda h: check(lib().gu_hgraph_write_edgelist(h, os.fsencode(path), int(header))))
+
+    def count_degree_zero(self):
+        c = ctypes.c_uint64()
+        self._with_handle(lambda h: check(lib().gu_hgraph_count_degree_zero(h, ctypes.byref(c))))
+        return c.value
 
 
 def sources(n, k, seed=2):

@@ -102,11 +102,29 @@ gu_status gu_hgraph_dag(int32_t n, int64_t m, uint64_t seed, gu_hgraph *out);
 /* CSR from an edge list (u[i], v[i]); symmetric != 0 adds both directions. */
 gu_status gu_hgraph_from_edges(int32_t n, const int32_t *u, const int32_t *v, int64_t count, int symmetric,
                                gu_hgraph *out);
+/* A host graph holding a copy of the given CSR as it is (validated, not rebuilt). */
+gu_status gu_hgraph_from_csr(const int32_t *R, const int32_t *C, int32_t n, int64_t m, int directed, gu_hgraph *out);
 gu_status gu_hgraph_arrays(gu_hgraph h, const int32_t **R, const int32_t **C, int32_t *n, int64_t *m,
                            int *directed);
 gu_status gu_hgraph_destroy(gu_hgraph h);
 /* k distinct sources drawn uniformly without replacement from [0, n). */
 gu_status gu_sources(int32_t n, int32_t k, uint64_t seed, int32_t *out_host);
+
+/* ---- graph files ------------------------------------------------------------ */
+/* Reads a graph file.  format: "dimacs" (or "metis"), "edgelist", "edgelist_h",
+ * "market" -- the reference's formats, giving the same CSR as its parser
+ * (parse(), parse.cpp:88-113; parse_metis 115-208, parse_market 210-346,
+ * parse_snap 349-441) -- or "csrbin", the binary CSR cache written by
+ * gu_hgraph_write_csr.  Malformed files give GU_ERR_INVALID_ARGUMENT (the
+ * reference exits or reads out of bounds). */
+gu_status gu_hgraph_parse(const char *path, const char *format, gu_hgraph *out);
+/* Binary CSR cache: magic "GUCSR1", n, m, directed, R, C (little-endian). */
+gu_status gu_hgraph_write_csr(gu_hgraph h, const char *path);
+/* host_graph::write_edgelist_to_file (parse.cpp:443-465): optional "n m" line,
+ * then "source target" per CSR entry. */
+gu_status gu_hgraph_write_edgelist(gu_hgraph h, const char *path, int header);
+/* host_graph::count_degree_zero_vertices (parse.cpp:467-478). */
+gu_status gu_hgraph_count_degree_zero(gu_hgraph h, uint64_t *count);
 
 /* ---- device graphs ------------------------------------------------------- */
 /* Copies the CSR (R: n+1 offsets, C: m neighbours, host pointers) to the

@@ -13,9 +13,13 @@ small seeded synthetic graphs, and writes one compressed .npz per case:
   delta_f32                  examples/betweenness_centrality/bc.cu:11-57
   diameter                   examples/diameter_sampling/diameter_sampling_test.cu:9-38
   dag_pairs (DAG cases)      graph-utils/dag_reachability.cpp:36-65
-and lbs_*.npz with counts, scanned, result (examples/load_balanced_search/lbs.cu:18-31).
+and lbs_*.npz with counts, scanned, result (examples/load_balanced_search/lbs.cu:18-31),
+and parse_<case>.{graph,txt,mtx} + parse_<case>.npz: small graph files in the
+reference's three text formats, written with the quirks its parser has to cope
+with (comments, double separators, '\r' line ends, extra fields, unsorted
+lines), and the CSR the reference parser (parse.cpp:88-441) builds from them.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [--only parse]
 """
 import os
 import subprocess
@@ -69,10 +73,89 @@ def golden_case(tmp, name, R, C, n, directed, sources, dag=False):
     print(f"graph_{name}: n={n} m={len(C)} k={k} diameter={out['diameter']}")
 
 
+def write_metis(path, R, C, n, rng):
+    """METIS text with comments, a header, and per-line quirks: double spaces
+    (the reference drops the field that follows), tabs, trailing blanks and
+    '\r' line ends (the reference drops a field ending in '\r')."""
+    lines = ["% written for the parser parity fixtures", f"{n} {len(C) // 2} "]
+    for v in range(n):
+        nb = [str(int(c) + 1) for c in C[R[v]:R[v + 1]]]
+        sep = [" "] * max(len(nb) - 1, 0)
+        for i in range(len(sep)):
+            u = rng.random()
+            sep[i] = "  " if u < 0.05 else ("\t" if u < 0.15 else " ")
+        line = "".join(x + y for x, y in zip(nb, sep + [""]))
+        u = rng.random()
+        if u < 0.1:
+            line += " "
+        elif u < 0.15:
+            line += "\r"
+        lines.append(line)
+        if rng.random() < 0.02:
+            lines.append("% a comment between vertex lines")
+    with open(path, "w", newline="") as f:
+        f.write("\n".join(lines) + "\n")
+
+
+def write_snap(path, R, C, n, rng, shuffle_some=False):
+    """SNAP edge list, 0-based, '#' comments, tabs or spaces, some extra fields;
+    optionally a few lines out of source order (the reference induces R as if
+    sorted, and the parity covers that too)."""
+    rows = [(v, int(c)) for v in range(n) for c in C[R[v]:R[v + 1]]]
+    if shuffle_some:
+        for _ in range(3):
+            i, j = rng.integers(0, len(rows), 2)
+            rows[i], rows[j] = rows[j], rows[i]
+    lines = ["# Directed graph written for the parser parity fixtures", "# FromNodeId\tToNodeId"]
+    for u, v in rows:
+        sep = "\t" if rng.random() < 0.5 else " "
+        extra = " 1.0" if rng.random() < 0.05 else ""
+        lines.append(f"{u}{sep}{v}{extra}")
+    with open(path, "w", newline="") as f:
+        f.write("\n".join(lines) + "\n")
+
+
+def write_market(path, R, C, n, rng):
+    """MatrixMarket pattern matrix: one entry per undirected edge, in random order."""
+    ent = [(v + 1, int(c) + 1) for v in range(n) for c in C[R[v]:R[v + 1]] if v < c]
+    rng.shuffle(ent)
+    lines = ["%%MatrixMarket matrix coordinate pattern symmetric", "% parser parity fixture", f"{n} {n} {len(ent)}"]
+    lines += [f"{a} {b}" for a, b in ent]
+    with open(path, "w", newline="") as f:
+        f.write("\n".join(lines) + "\n")
+
+
+def parse_cases(tmp):
+    import gu
+    rng = np.random.default_rng(17)
+    g = gu.HostGraph.rmat(8, 8, seed=23)
+    d = gu.HostGraph.dag(200, 900, seed=29)
+    cases = [("metis_rmat8", "graph", "dimacs", lambda p: write_metis(p, g.R, g.C, g.n, rng)),
+             ("snap_dag200", "txt", "edgelist", lambda p: write_snap(p, d.R, d.C, d.n, rng)),
+             ("snap_unsorted", "txt", "edgelist", lambda p: write_snap(p, d.R, d.C, d.n, rng, True)),
+             ("snap_h_dag200", "txt", "edgelist_h", lambda p: write_snap(p, d.R, d.C, d.n, rng)),
+             ("market_rmat8", "mtx", "market", lambda p: write_market(p, g.R, g.C, g.n, rng))]
+    for name, ext, fmt, writer in cases:
+        path = os.path.join(HERE, f"parse_{name}.{ext}")
+        writer(path)
+        pre = os.path.join(tmp, "parse_" + name)
+        run("parse", path, fmt, pre)
+        R, C, n, directed = read_csr(pre)
+        C = C[: R[n]]  # the reference sizes C from the header; only R[n] entries are the graph
+        np.savez_compressed(os.path.join(HERE, f"parse_{name}.npz"), R=R, C=C, n=np.int32(n),
+                            directed=np.bool_(directed), format=np.str_(fmt), input=np.str_(os.path.basename(path)))
+        print(f"parse_{name}: {fmt} n={n} m={R[n]}")
+
+
 def main():
     subprocess.run(["bash", os.path.join(ROOT, "oracle", "build_ref.sh")], check=True)
+    if sys.argv[1:] == ["--only", "parse"]:
+        with tempfile.TemporaryDirectory() as tmp:
+            parse_cases(tmp)
+        return
     import gu
     with tempfile.TemporaryDirectory() as tmp:
+        parse_cases(tmp)
         # the reference's own fixtures, parsed by the reference parser
         files = [(f"test{i}", f"test{i}.graph", "dimacs") for i in range(1, 7)]
         files += [("jazz", "jazz.graph", "dimacs"), ("test7", "test7.txt", "edgelist")]
