@@ -649,6 +649,17 @@ gu_status gu_diameter(gu_graph g, const int32_t *sources_dev, int32_t k, int32_t
     });
 }
 
+gu_status gu_dag_reach(gu_graph g, int64_t *counts_dev, int64_t *total_pairs, void *stream)
+{
+    return guarded([&] {
+        if (!g || !total_pairs || (g->g->n > 0 && !counts_dev)) throw gu_error(GU_ERR_INVALID_ARGUMENT, "null argument");
+        DeviceGraph &dg = *g->g;
+        std::lock_guard<std::mutex> lk(dg.mu);
+        DeviceScope ds(dg.device);
+        dag_reach(dg, counts_dev, total_pairs, (cudaStream_t)stream);
+    });
+}
+
 gu_status gu_reach(gu_graph g, const int32_t *sources_dev, int32_t k, int64_t *counts_dev, void *stream)
 {
     return guarded([&] {

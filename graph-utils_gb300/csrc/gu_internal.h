@@ -174,6 +174,8 @@ void launch_plain_bfs(DeviceGraph &g, const int32_t *sources, int32_t k, int32_t
 // Per-source engine for low-degree graphs (AUTO's choice there): rows
 // (dist non-null) or counts (reach, deepest level).  Synchronises; returns false
 // if a frontier overflowed its shared queues (rerun on the batched engine).
+// Reachable-set sizes of every vertex of a DAG (self excluded) and their sum.
+void dag_reach(DeviceGraph &g, int64_t *counts, int64_t *total_host, cudaStream_t st);
 enum class AutoEngine { LOCAL, PLAIN, BATCHED };
 AutoEngine auto_engine(const DeviceGraph &g, bool rows);
 bool launch_local_bfs(DeviceGraph &g, const int32_t *sources, int32_t k, int32_t *dist, int64_t ld,

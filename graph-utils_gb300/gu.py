@@ -88,6 +88,7 @@ def lib():
         "gu_bc": ([_vp, _vp, ctypes.c_int32, ctypes.c_int32, _vp, _vp, ctypes.c_int64, _vp], ctypes.c_int),
         "gu_diameter": ([_vp, _vp, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32), _vp], ctypes.c_int),
         "gu_reach": ([_vp, _vp, ctypes.c_int32, _vp, _vp], ctypes.c_int),
+        "gu_dag_reach": ([_vp, _vp, _i64p, _vp], ctypes.c_int),
         "gu_lbs": ([_vp, ctypes.c_int32, _vp, _vp, ctypes.c_int64, _vp, _i64p, _vp], ctypes.c_int),
         "gu_race_and_resolve": ([_vp, ctypes.c_int32, _vp, _vp], ctypes.c_int),
         "gu_server_create": ([ctypes.c_size_t, ctypes.c_int, ctypes.c_int, ctypes.POINTER(_vp)], ctypes.c_int),
@@ -303,6 +304,13 @@ class Graph:
         """counts_dev (int64 cuda tensor, k): vertices reachable from each source, itself included."""
         check(lib().gu_reach(self._h, sources_dev.data_ptr(), int(sources_dev.numel()), counts_dev.data_ptr(),
                              _stream_handle(stream)))
+
+    def dag_reach(self, counts_dev, stream=None):
+        """counts_dev (int64 cuda tensor, n): reachable-set size of every vertex of the DAG
+        (itself excluded); returns the total number of reachable pairs."""
+        tot = ctypes.c_int64()
+        check(lib().gu_dag_reach(self._h, counts_dev.data_ptr(), ctypes.byref(tot), _stream_handle(stream)))
+        return tot.value
 
     def bfs_host(self, sources_host, variant="auto", out=None, stream=None):
         """Host form: numpy sources in, numpy k x n int32 distances out."""

@@ -13,7 +13,8 @@
 // diameter_sampling_setup (diameter_sampling.cuh:13); transitive_closure_setup
 // (transitive_closure.cuh:13); extract_edges_{block,warp}
 // (load_balanced_search.cuh:12-13, called as host functions here, without the
-// <<<1, BLOCK_SIZE>>> launch configuration).
+// <<<1, BLOCK_SIZE>>> launch configuration); parse / parse_metis / parse_snap /
+// parse_market (parse.h:37-40); get_reachability_dag (dag_reachability.h:15).
 //
 // Semantics kept: every source in [start, end) is searched; the returned rows
 // are those of the last R = min(end - start, #SMs) sources, source s in row
@@ -25,6 +26,7 @@
 #include <algorithm>
 #include <cstdint>
 #include <cstdio>
+#include <set>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -290,4 +292,63 @@ inline void extract_edges_block(int vertex_frontier_size, int *edge_counts, int 
 inline void extract_edges_warp(int vertex_frontier_size, int *edge_counts, int *scanned_edges, int *result, int *edges)
 {
     extract_edges_block(vertex_frontier_size, edge_counts, scanned_edges, result, edges);
+}
+
+// ---- graph files (parse.h:37-40) ----------------------------------------------
+namespace gu_shim {
+// host_graph from a file through the library's readers (same CSR as the
+// reference parser), with F (each entry's source) filled as the reference's is.
+inline host_graph read_graph(const char *file, const char *format)
+{
+    gu_hgraph h = nullptr;
+    check(gu_hgraph_parse(file, format, &h), "parse");
+    const int32_t *R = nullptr, *C = nullptr;
+    int32_t n = 0;
+    int64_t m = 0;
+    int directed = 0;
+    gu_status st = gu_hgraph_arrays(h, &R, &C, &n, &m, &directed);
+    host_graph g;
+    if (st == GU_OK) {
+        g.n = n;
+        g.m = (int)m;
+        g.directed = directed != 0;
+        g.R.assign(R, R + n + 1);
+        g.C.assign(C, C + m);
+        g.F.resize((size_t)m);
+        for (int v = 0; v < n; ++v)
+            for (int e = R[v]; e < R[v + 1]; ++e) g.F[(size_t)e] = v;
+    }
+    gu_hgraph_destroy(h);
+    check(st, "parse");
+    return g;
+}
+}  // namespace gu_shim
+
+inline host_graph parse_metis(char *file) { return gu_shim::read_graph(file, "dimacs"); }
+inline host_graph parse_snap(char *file, bool header) { return gu_shim::read_graph(file, header ? "edgelist_h" : "edgelist"); }
+inline host_graph parse_market(char *file) { return gu_shim::read_graph(file, "market"); }
+inline host_graph parse(const program_options &op) { return gu_shim::read_graph(op.infile, op.format ? op.format : ""); }
+
+// ---- DAG reachability (dag_reachability.h:15) ----------------------------------
+// The reachable set of every vertex (itself excluded), from the batched search's
+// distance rows.  Needs a directed graph, as the reference's does.
+inline std::vector<std::set<int> > get_reachability_dag(host_graph &g)
+{
+    if (!g.directed) throw std::runtime_error("get_reachability_dag: the graph must be directed");
+    device_graph dg(g);
+    std::vector<std::set<int> > reach((size_t)g.n);
+    const int chunk = 256;
+    gu_shim::dbuf<int32_t> src((size_t)chunk), dist((size_t)chunk * (size_t)g.n);
+    std::vector<int32_t> hs((size_t)chunk), row((size_t)chunk * (size_t)g.n);
+    for (int c0 = 0; c0 < g.n; c0 += chunk) {
+        const int k = std::min(chunk, g.n - c0);
+        for (int i = 0; i < k; ++i) hs[(size_t)i] = c0 + i;
+        cudaMemcpy(src.p, hs.data(), sizeof(int32_t) * k, cudaMemcpyHostToDevice);
+        gu_shim::check(gu_bfs(dg.handle, GU_BFS_AUTO, src.p, k, dist.p, g.n, nullptr), "get_reachability_dag");
+        cudaMemcpy(row.data(), dist.p, sizeof(int32_t) * (size_t)k * g.n, cudaMemcpyDeviceToHost);
+        for (int i = 0; i < k; ++i)
+            for (int v = 0; v < g.n; ++v)
+                if (v != c0 + i && row[(size_t)i * g.n + v] != GU_DIST_UNREACHABLE) reach[(size_t)(c0 + i)].insert(v);
+    }
+    return reach;
 }

@@ -200,6 +200,14 @@ gu_status gu_diameter(gu_graph g, const int32_t *sources_dev, int32_t k, int32_t
  * whose rows gu_bfs returns. */
 gu_status gu_reach(gu_graph g, const int32_t *sources_dev, int32_t k, int64_t *counts_dev, void *stream);
 
+/* All-vertex reachability of a DAG: counts_dev[v] (int64, n) = size of the set
+ * of vertices reachable from v, v itself excluded, and *total_pairs their sum --
+ * the sets get_reachability_dag (graph-utils/dag_reachability.cpp:36-65)
+ * returns, as sizes (gu_bfs rows give the sets).  The graph must be directed
+ * (GU_ERR_INVALID_ARGUMENT otherwise, as the reference exits); like the
+ * reference it assumes no cycles. */
+gu_status gu_dag_reach(gu_graph g, int64_t *counts_dev, int64_t *total_pairs, void *stream);
+
 /* ---- load-balanced search and race-and-resolve ------------------------------- */
 /* Load-balanced search over N work counts (device pointers, counts >= 0):
  * scanned_dev[i] = exclusive prefix sum of counts (int32), total = sum, and

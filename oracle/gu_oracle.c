@@ -365,6 +365,14 @@ int32_t oracle_race_and_resolve(uint32_t vote, int32_t lane)
 /* ---- DAG reachable pairs: graph-utils/dag_reachability.cpp:36-65 ---------- */
 int64_t oracle_dag_reach_pairs(const int32_t *R, const int32_t *C, int32_t n)
 {
+    return oracle_dag_reach_counts(R, C, n, NULL);
+}
+
+/* Per-vertex sizes of the reachable sets (the vertex itself excluded) that
+ * get_reachability_dag (graph-utils/dag_reachability.cpp:36-65) returns;
+ * counts may be NULL.  Returns their sum. */
+int64_t oracle_dag_reach_counts(const int32_t *R, const int32_t *C, int32_t n, int64_t *counts)
+{
     /* Kahn order, then bitset union in reverse topological order. */
     int32_t *indeg = (int32_t *)calloc((size_t)(n > 0 ? n : 1), sizeof(int32_t));
     int32_t *order = (int32_t *)malloc(sizeof(int32_t) * (size_t)(n > 0 ? n : 1));
@@ -389,7 +397,10 @@ int64_t oracle_dag_reach_pairs(const int32_t *R, const int32_t *C, int32_t n)
             bv[w >> 6] |= 1ull << (w & 63);
             for (size_t q = 0; q < words; ++q) bv[q] |= bw[q];
         }
-        for (size_t q = 0; q < words; ++q) pairs += __builtin_popcountll(bv[q]);
+        int64_t cnt = 0;
+        for (size_t q = 0; q < words; ++q) cnt += __builtin_popcountll(bv[q]);
+        if (counts) counts[v] = cnt;
+        pairs += cnt;
     }
     free(bits);
     free(indeg);

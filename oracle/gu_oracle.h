@@ -104,6 +104,7 @@ int32_t oracle_race_and_resolve(uint32_t vote, int32_t lane);
  * and v reachable from u; semantics of graph-utils/dag_reachability.cpp:36-65
  * (computed iteratively in reverse topological order, no recursion). */
 int64_t oracle_dag_reach_pairs(const int32_t *R, const int32_t *C, int32_t n);
+int64_t oracle_dag_reach_counts(const int32_t *R, const int32_t *C, int32_t n, int64_t *counts);
 
 #ifdef __cplusplus
 }

@@ -50,6 +50,8 @@ def lib():
         L.oracle_race_and_resolve.restype = ctypes.c_int32
         L.oracle_dag_reach_pairs.argtypes = [_i32p, _i32p, ctypes.c_int32]
         L.oracle_dag_reach_pairs.restype = ctypes.c_int64
+        L.oracle_dag_reach_counts.argtypes = [_i32p, _i32p, ctypes.c_int32, ctypes.POINTER(ctypes.c_int64)]
+        L.oracle_dag_reach_counts.restype = ctypes.c_int64
         _lib = L
     return _lib
 
@@ -148,3 +150,11 @@ def race_and_resolve(vote, lane):
 def dag_reach_pairs(R, C, n):
     R, C = _csr(R, C)
     return int(lib().oracle_dag_reach_pairs(_p(R), _p(C), n))
+
+
+def dag_reach_counts(R, C, n):
+    """Per-vertex reachable-set sizes (self excluded) of a DAG; returns (counts, total)."""
+    R, C = _csr(R, C)
+    out = np.zeros(max(n, 1), np.int64)
+    tot = lib().oracle_dag_reach_counts(_p(R), _p(C), n, out.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)))
+    return out[:n], int(tot)

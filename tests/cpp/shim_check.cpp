@@ -9,7 +9,10 @@
 #include "graph_utils.hpp"
 
 #include <cmath>
+#include <cstdio>
 #include <cstdlib>
+#include <set>
+#include <unistd.h>
 
 #include "gu_oracle.h"
 
@@ -142,6 +145,52 @@ int main(int argc, char **argv)
         oracle_lbs(counts.data(), n, es.data(), er.data(), m, &et);
         report("Scan", scanned == es);
         report("Load-balanced search", total == et && result == er);
+    }
+    {
+        // parse_snap on a graph's edge list (write_edgelist_to_file's format) gives
+        // back its CSR and COO sources (a grid: every id appears, as SNAP needs)
+        gu_hgraph w = nullptr;
+        gu_hgraph_grid(30, 40, 0.0, 1, &w);
+        const int32_t *WR, *WC;
+        int32_t wn;
+        int64_t wm;
+        int wd;
+        gu_hgraph_arrays(w, &WR, &WC, &wn, &wm, &wd);
+        std::vector<int> F((size_t)wm);
+        for (int v = 0; v < wn; ++v)
+            for (int e = WR[v]; e < WR[v + 1]; ++e) F[(size_t)e] = v;
+        char path[] = "/tmp/gu_shim_edgesXXXXXX";
+        const int fd = mkstemp(path);
+        if (fd >= 0) close(fd);
+        gu_hgraph_write_edgelist(w, path, 0);
+        host_graph p = parse_snap(path, false);
+        std::remove(path);
+        report("Parse (SNAP edge list)", p.n == wn && p.R == std::vector<int>(WR, WR + wn + 1) &&
+                                             p.C == std::vector<int>(WC, WC + wm) && p.F == F && p.directed);
+        gu_hgraph_destroy(w);
+    }
+    {
+        // get_reachability_dag on a random DAG: set sizes against the oracle
+        gu_hgraph dh = nullptr;
+        gu_hgraph_dag(3000, 20000, 5, &dh);
+        const int32_t *DR, *DC;
+        int32_t dn;
+        int64_t dm;
+        int dd;
+        gu_hgraph_arrays(dh, &DR, &DC, &dn, &dm, &dd);
+        host_graph d;
+        d.R.assign(DR, DR + dn + 1);
+        d.C.assign(DC, DC + dm);
+        d.n = dn;
+        d.m = (int)dm;
+        d.directed = true;
+        std::vector<int64_t> cnt((size_t)dn);
+        oracle_dag_reach_counts(DR, DC, dn, cnt.data());
+        gu_hgraph_destroy(dh);
+        const std::vector<std::set<int> > reach = get_reachability_dag(d);
+        bool ok = (int)reach.size() == dn;
+        for (int v = 0; ok && v < dn; ++v) ok = (int64_t)reach[(size_t)v].size() == cnt[(size_t)v];
+        report("DAG reachability", ok);
     }
     std::printf("%s\n", failures ? "FAILED" : "ALL PASSED");
     return failures ? 1 : 0;

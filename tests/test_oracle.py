@@ -71,6 +71,26 @@ def test_diameter_matches_reference(name):
     assert oracle.diameter(g["R"], g["C"], int(g["n"]), g["sources"]) == int(g["diameter"])
 
 
+def test_dag_reach_counts_sum_to_pairs():
+    import gu
+    for seed in (1, 2):
+        hg = gu.HostGraph.dag(400, 3000, seed=seed)
+        counts, tot = oracle.dag_reach_counts(hg.R, hg.C, hg.n)
+        assert tot == counts.sum() == oracle.dag_reach_pairs(hg.R, hg.C, hg.n)
+        # a vertex's set is its successors and their sets (the reference's recursion)
+        for v in range(0, hg.n, 37):
+            succ = hg.C[hg.R[v]:hg.R[v + 1]]
+            reach = set(succ.tolist())
+            frontier = list(succ)
+            while frontier:
+                w = frontier.pop()
+                for x in hg.C[hg.R[w]:hg.R[w + 1]]:
+                    if x not in reach:
+                        reach.add(int(x))
+                        frontier.append(int(x))
+            assert counts[v] == len(reach)
+
+
 def test_dag_reachability_matches_reference():
     for name in ("test7", "dag300"):
         g = load_golden(name)
