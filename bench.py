@@ -49,6 +49,8 @@ def parse_args():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cpu-seconds", type=float, default=15.0, help="budget of the cpu_baseline sample")
     p.add_argument("--kernel-only", action="store_true", help="skip e2e (for profiling runs)")
+    p.add_argument("--power", action="store_true",
+                   help="sample board power (NVML, read-only) during the timed region: adds a power object")
     p.add_argument("--workload", choices=["c2", "c1", "c3", "c4", "c5", "io"], default="c2",
                    help="c2: the headline BFS line (default); c1/c3/c4/c5/io: the other configurations, "
                         "one JSON line each (bench_configs.py)")
@@ -255,7 +257,11 @@ def run_ours(args):
 
     kernel_times = []
     levels = None
+    power = None
+    psampler = gu.PowerSampler(local, 10) if args.power else None
     with ClockSampler(local) as clk:
+        if psampler:
+            psampler.__enter__()
         barrier()
         ev0 = torch.cuda.Event(enable_timing=True)
         ev1 = torch.cuda.Event(enable_timing=True)
@@ -267,6 +273,8 @@ def run_ours(args):
             levels = (td, bu, ml)
         ev1.record(stream)
         barrier()
+        if psampler:
+            psampler.__exit__(None, None, None)
     clocks = clk.summary()
     t_total = ev0.elapsed_time(ev1) / 1e3
     if ws > 1:
@@ -274,6 +282,10 @@ def run_ours(args):
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         t_total = float(t.item())
     value = ws * gteps_edges * args.steps / t_total / 1e9
+    if psampler:
+        power = {"avg_w": psampler.watts, "samples": psampler.samples,
+                 "gteps_per_w": value / ws / psampler.watts if psampler.watts else None,
+                 "source": "NVML power draw of this rank's GPU, sampled every 10 ms over the timed region"}
 
     e2e = None
     if not args.kernel_only:
@@ -329,6 +341,8 @@ def run_ours(args):
                            "edges_per_step": gteps_edges, "levels_td_bu_max": levels},
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
                 "gpu_launches": args.steps}
+        if power:
+            line["power"] = power
         print(json.dumps(line), flush=True)
     g.close()
     if ws > 1:

@@ -69,7 +69,7 @@ def build_library(verbose=False, ptxas_verbose=False):
         with ThreadPoolExecutor(max_workers=min(len(jobs), os.cpu_count() or 4)) as ex:
             logs = list(ex.map(_run, jobs))
     if jobs or _stale(LIB, objs):
-        _run([NVCC] + ARCH + ["-shared", "-o", LIB] + objs + ["-lpthread"])
+        _run([NVCC] + ARCH + ["-shared", "-o", LIB] + objs + ["-lpthread", "-ldl"])
     if verbose:
         for lg in logs:
             if lg.strip():

@@ -74,6 +74,9 @@ struct gu_graph_s {
 struct gu_hgraph_s {
     HostGraph h;
 };
+struct gu_power_s {
+    PowerSampler *s = nullptr;
+};
 struct gu_timer_s {
     cudaEvent_t a = nullptr, b = nullptr;
 };
@@ -646,6 +649,28 @@ gu_status gu_diameter(gu_graph g, const int32_t *sources_dev, int32_t k, int32_t
         int err = 0, td = 0, bu = 0;
         msbfs_read_status(dg, &err, &td, &bu, &ml);
         *diameter = ml;
+    });
+}
+
+gu_status gu_power_start(int device, int period_ms, gu_power *out)
+{
+    return guarded([&] {
+        if (!out) throw gu_error(GU_ERR_INVALID_ARGUMENT, "null output handle");
+        std::unique_ptr<gu_power_s> p(new gu_power_s());
+        p->s = power_start(device, period_ms);
+        *out = p.release();
+    });
+}
+
+gu_status gu_power_stop(gu_power p, double *avg_watts, int64_t *samples)
+{
+    return guarded([&] {
+        if (!p) throw gu_error(GU_ERR_INVALID_ARGUMENT, "null sampler");
+        std::unique_ptr<gu_power_s> h(p);
+        long long n = 0;
+        power_stop(h->s, avg_watts, &n);
+        h->s = nullptr;
+        if (samples) *samples = n;
     });
 }
 

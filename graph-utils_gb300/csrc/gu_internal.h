@@ -191,6 +191,11 @@ void launch_lbs(const int32_t *counts, int32_t N, int32_t *scanned, int32_t *res
                 int32_t *total_dev, int64_t *total_host, void *scratch_ptr, size_t scratch_bytes, cudaStream_t st);
 void launch_race_and_resolve(const int32_t *pred, int32_t nwarps, int32_t *winner, cudaStream_t st);
 
+// Board power sampling through NVML loaded at run time (power.cpp).
+struct PowerSampler;
+PowerSampler *power_start(int device, int period_ms);
+void power_stop(PowerSampler *s, double *avg_w, long long *samples);  // joins and frees
+
 class Server;
 Server *server_create(size_t budget, int nslots, int max_batch);
 void server_destroy(Server *s);

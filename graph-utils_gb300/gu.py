@@ -89,6 +89,8 @@ def lib():
         "gu_diameter": ([_vp, _vp, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32), _vp], ctypes.c_int),
         "gu_reach": ([_vp, _vp, ctypes.c_int32, _vp, _vp], ctypes.c_int),
         "gu_dag_reach": ([_vp, _vp, _i64p, _vp], ctypes.c_int),
+        "gu_power_start": ([ctypes.c_int, ctypes.c_int, ctypes.POINTER(_vp)], ctypes.c_int),
+        "gu_power_stop": ([_vp, ctypes.POINTER(ctypes.c_double), _i64p], ctypes.c_int),
         "gu_lbs": ([_vp, ctypes.c_int32, _vp, _vp, ctypes.c_int64, _vp, _i64p, _vp], ctypes.c_int),
         "gu_race_and_resolve": ([_vp, ctypes.c_int32, _vp, _vp], ctypes.c_int),
         "gu_server_create": ([ctypes.c_size_t, ctypes.c_int, ctypes.c_int, ctypes.POINTER(_vp)], ctypes.c_int),
@@ -338,6 +340,28 @@ def race_and_resolve(pred_dev, winners_dev, stream=None):
     check(lib().gu_race_and_resolve(pred_dev.data_ptr(), int(pred_dev.numel()) // 32, winners_dev.data_ptr(),
                                     _stream_handle(stream)))
     return winners_dev
+
+
+class PowerSampler:
+    """Mean board power over a region (gu_power_*): `with PowerSampler(0) as p: ...; p.watts`."""
+
+    def __init__(self, device=0, period_ms=10):
+        self.device, self.period_ms = device, period_ms
+        self.watts, self.samples = None, 0
+        self._h = None
+
+    def __enter__(self):
+        h = _vp()
+        check(lib().gu_power_start(self.device, self.period_ms, ctypes.byref(h)))
+        self._h = h
+        return self
+
+    def __exit__(self, *exc):
+        w, n = ctypes.c_double(), ctypes.c_int64()
+        h, self._h = self._h, None
+        check(lib().gu_power_stop(h, ctypes.byref(w), ctypes.byref(n)))
+        self.watts, self.samples = w.value, n.value
+        return False
 
 
 QUERY_BFS, QUERY_BC, QUERY_REACH = 0, 1, 2

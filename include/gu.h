@@ -87,6 +87,16 @@ typedef struct gu_timer_s *gu_timer;
 gu_status gu_timer_start(void *stream, gu_timer *out);
 gu_status gu_timer_stop(gu_timer t, void *stream, double *seconds); /* also frees t */
 
+/* Board power during a run (power_measurer::start_power_sample /
+ * end_power_sample, util_device.cu:78-130): a background thread reads the
+ * device's power draw every period_ms until gu_power_stop, which returns the
+ * mean in watts and the sample count and frees the sampler.  NVML is loaded at
+ * run time (libnvidia-ml.so.1, or $GU_NVML_LIBRARY); without it the start
+ * returns GU_ERR_UNSUPPORTED.  Reads only: no GPU setting is changed. */
+typedef struct gu_power_s *gu_power;
+gu_status gu_power_start(int device, int period_ms, gu_power *out);
+gu_status gu_power_stop(gu_power p, double *avg_watts, int64_t *samples);
+
 /* ---- host graphs (generators; no reference counterpart) ------------------ */
 /* R-MAT: 2^scale vertices, edge_factor*2^scale edge draws, quadrant
  * probabilities a,b,c (d = 1-a-b-c); symmetrised, duplicates and self-loops
