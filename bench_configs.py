@@ -10,6 +10,7 @@
         of BFS / BC / reachability requests at several rates, p50 / p99 latency.
     io  graph files: R-MAT scale 20 as METIS / SNAP / MatrixMarket text and the
         binary CSR cache, read by this library and by the reference parser.
+    dag all-vertex reachability of random DAGs (m = 8n), n = 2^16 and 2^18.
 
 GPU times are CUDA-event kernel times of the library's own launch (`last_launch`)
 unless named `call_ms` (wall time of the synchronous C-ABI call).  CPU times are
@@ -348,5 +349,32 @@ def wl_io(args):
            "note": "reference_s includes writing its CSR out (a few hundred MB), a small share"})
 
 
+def wl_dag(args):
+    """All-vertex reachability of random DAGs (m = 8n): gu_dag_reach against the
+    oracle's bitset closure (n = 2^16) and a per-vertex BFS sample (n = 2^18)."""
+    import gu
+    import oracle
+    torch = _torch()
+    cores = os.cpu_count() or 1
+    res = {}
+    for n, seed in ((1 << 16, 1), (1 << 18, 2)):
+        hg = gu.HostGraph.dag(n, 8 * n, seed=seed)
+        g = gu.Graph(hg)
+        cnt = torch.empty(n, dtype=torch.int64, device="cuda")
+        tot = g.dag_reach(cnt)
+        c = _median_call_ms(lambda: g.dag_reach(cnt), reps=3)
+        row = {"m": hg.m, "pairs": tot, "gpu_call_ms": c}
+        if n <= 1 << 16:
+            (_, rtot), t = _cpu(oracle.dag_reach_counts, hg.R, hg.C, hg.n)
+            row.update({"cpu_bitset_closure_ms_1thread": t * 1e3, "pairs_match": rtot == tot})
+        sub = np.arange(0, n, max(1, n // (4 * cores)), dtype=np.int32)[: 4 * cores]
+        _, t = _cpu(oracle.reach_count, hg.R, hg.C, hg.n, sub, nthreads=cores)
+        row[f"cpu_bfs_per_vertex_extrapolated_ms_{cores}threads"] = t / len(sub) * n * 1e3
+        res[f"n{n}"] = row
+        g.close()
+    _emit({"workload": "dag_reach_m8n", "metric": "all-vertex DAG reachability", "unit": "ms", "results": res,
+           "note": "the reference's recursion with std::set per vertex is the baseline these restate"})
+
+
 def run(workload, args):
-    {"c1": wl_c1, "c3": wl_c3, "c4": wl_c4, "c5": wl_c5, "io": wl_io}[workload](args)
+    {"c1": wl_c1, "c3": wl_c3, "c4": wl_c4, "c5": wl_c5, "io": wl_io, "dag": wl_dag}[workload](args)

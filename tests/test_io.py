@@ -111,3 +111,22 @@ def test_missing_file():
     with pytest.raises(gu.GuError) as e:
         gu.HostGraph.parse("no/such/file.graph", "dimacs")
     assert e.value.status == 1
+
+
+def test_convert_tool(tmp_path, capsys):
+    """The convert example's flow: METIS in, edge list (or CSR cache) out."""
+    import convert
+    ref = dict(np.load(os.path.join(GOLDEN, "parse_metis_rmat8.npz")))
+    src = os.path.join(GOLDEN, str(ref["input"]))
+    out = tmp_path / "g.txt"
+    assert convert.main(["-i", src, "-f", "dimacs", "-o", str(out)]) == 0
+    assert f"Number of vertices: {int(ref['n'])}" in capsys.readouterr().out
+    rows = np.loadtxt(out, dtype=np.int64).reshape(-1, 2)
+    np.testing.assert_array_equal(rows[:, 1], ref["C"])
+    np.testing.assert_array_equal(np.bincount(rows[:, 0], minlength=int(ref["n"])), np.diff(ref["R"]))
+    csr = tmp_path / "g.csr"
+    assert convert.main(["-i", src, "-f", "dimacs", "-o", str(csr), "--csr"]) == 0
+    h = gu.HostGraph.parse(csr, "csrbin")
+    np.testing.assert_array_equal(h.R, ref["R"])
+    np.testing.assert_array_equal(h.C, ref["C"])
+    assert convert.main(["-i", src, "-f", "dimacs"]) == 1
