@@ -19,14 +19,16 @@
 // during the search: the level bit-planes are transposed into the int32
 // distance rows once per batch, each row segment written whole and coalesced.
 //
-// Phase j of a batch (one grid barrier per level):
-//   * finalise F_{j-1}: seen |= F_{j-1}, set the level bits of j-1 in the
-//     planes (lazily; readers use seen|F_{j-1}, invariant during the phase)
+// Phase j of a batch (one grid barrier per level; bottom-up levels add one or
+// two, see the bottom-up section):
+//   * finalise F_{j-1}: set the level bits of j-1 in the planes (seen took the
+//     bits when they were discovered)
 //   * clear F_{j-2}
 //   * discover F_j top-down (gather the adjacency of the F_{j-1} queue and claim
-//     new bits with 64-bit atomicOr) or bottom-up (each vertex still missing
-//     some active source ORs its in-neighbours' F_{j-1} words, stopping as soon
-//     as every missing active source is found).
+//     the bits missing from seen with 64-bit OR reductions into seen and F_j) or
+//     bottom-up (each vertex still missing some active source ORs its
+//     in-neighbours' F_{j-1} words, stopping as soon as every missing active
+//     source is found).
 // A source is active while its frontier is non-empty; the active mask of F_j is
 // OR-reduced per CTA in shared memory during phase j.  Direction: top-down ->
 // bottom-up when the frontier's out-edges exceed m / alpha, back when it holds
@@ -377,25 +379,48 @@ __device__ void cta_flush(const MsArgs &a, const Lvl &L, const CtaQ &cq)
 }
 
 // ---- top-down visit: frontier bits f arrive at vertex w over one edge ----------------
+// seen(w) holds every source that has reached w, this level's finds included:
+// a visit claims the bits f & ~seen with fire-and-forget OR reductions into
+// seen and into the next frontier.  A stale read (a bit another visit set a
+// moment ago) only repeats an idempotent reduction; "first" (the one append of
+// w to the next queue) is decided by the level stamp (W > 1) or by the
+// frontier word having been zero (W = 1).
+__device__ __forceinline__ void red_or(u64 *p, u64 v)
+{
+    // volatile: kept in order with the grid barrier's own (volatile) fences
+    asm volatile("red.relaxed.gpu.global.or.b64 [%0], %1;" ::"l"(p), "l"(v));
+}
+
+template <int W>
+__device__ __forceinline__ bool claim(const MsArgs &a, const Lvl &L, size_t o, const u64 (&nb)[W], bool &first)
+{
+    bool found = false;
+#pragma unroll
+    for (int q = 0; q < W; ++q) {
+        if (nb[q]) {
+            red_or(a.seen + o + q, nb[q]);
+            if (W == 1) {
+                if (atomicOr(L.fnxt + o + q, nb[q]) == 0) first = true;
+            } else {
+                red_or(L.fnxt + o + q, nb[q]);
+            }
+            found = true;
+        }
+    }
+    return found;
+}
+
 template <int W, class Q = GlobalQ>
 __device__ __forceinline__ void td_visit(const MsArgs &a, const Lvl &L, const u64 (&f)[W], int32_t w,
                                          const Q &qu = Q())
 {
     const size_t o = (size_t)w * W;
-    u64 s[W], c[W], x[W], nb[W];
-    ldw_l1<W>(a.seen + o, s);
-    ldw_l1<W>(L.fcur + o, c);
-    ldw<W>(L.fnxt + o, x);
-    bool found = false, first = false;
+    u64 s[W], nb[W];
+    ldw<W>(a.seen + o, s);
 #pragma unroll
-    for (int q = 0; q < W; ++q) {
-        nb[q] = f[q] & ~(s[q] | c[q] | x[q]);
-        if (nb[q]) {
-            const u64 old = atomicOr(L.fnxt + o + q, nb[q]);
-            found = true;
-            if (W == 1 && old == 0) first = true;
-        }
-    }
+    for (int q = 0; q < W; ++q) nb[q] = f[q] & ~s[q];
+    bool first = false;
+    const bool found = claim<W>(a, L, o, nb, first);
     if (W > 1 && found) first = atomicMax(a.stamp + w, L.tag) < L.tag;
     if (first) qu.push(a, L, w);
 }
@@ -406,33 +431,18 @@ __device__ __forceinline__ void td_visit2(const MsArgs &a, const Lvl &L, const u
                                           const u64 (&f2)[W], int32_t w2, const Q &qu = Q())
 {
     const size_t o = (size_t)w * W, o2 = (size_t)(w2 < 0 ? w : w2) * W;
-    u64 s[W], c[W], x[W], s2[W], c2[W], x2[W];
-    ldw_l1<W>(a.seen + o, s);
-    ldw_l1<W>(L.fcur + o, c);
-    ldw<W>(L.fnxt + o, x);
-    ldw_l1<W>(a.seen + o2, s2);
-    ldw_l1<W>(L.fcur + o2, c2);
-    ldw<W>(L.fnxt + o2, x2);
+    u64 s[W], s2[W];
+    ldw<W>(a.seen + o, s);
+    ldw<W>(a.seen + o2, s2);
     u64 nb[W], nb2[W];
 #pragma unroll
     for (int q = 0; q < W; ++q) {
-        nb[q] = f[q] & ~(s[q] | c[q] | x[q]);
-        nb2[q] = w2 < 0 ? 0ull : (f2[q] & ~(s2[q] | c2[q] | x2[q]));
+        nb[q] = f[q] & ~s[q];
+        nb2[q] = w2 < 0 ? 0ull : (f2[q] & ~s2[q]);
     }
-    bool found = false, found2 = false, first = false, first2 = false;
-#pragma unroll
-    for (int q = 0; q < W; ++q) {
-        if (nb[q]) {
-            const u64 old = atomicOr(L.fnxt + o + q, nb[q]);
-            found = true;
-            if (W == 1 && old == 0) first = true;
-        }
-        if (nb2[q]) {
-            const u64 old = atomicOr(L.fnxt + o2 + q, nb2[q]);
-            found2 = true;
-            if (W == 1 && old == 0) first2 = true;
-        }
-    }
+    bool first = false, first2 = false;
+    const bool found = claim<W>(a, L, o, nb, first);
+    const bool found2 = claim<W>(a, L, o2, nb2, first2);
     if (W > 1) {
         if (found) first = atomicMax(a.stamp + w, L.tag) < L.tag;
         if (found2) first2 = atomicMax(a.stamp + w2, L.tag) < L.tag;
@@ -441,14 +451,11 @@ __device__ __forceinline__ void td_visit2(const MsArgs &a, const Lvl &L, const u
     if (first2) qu.push(a, L, w2);
 }
 
-// Finalise F_{j-1} bits of one vertex: seen and the level bit-planes.  Only the
-// thread that owns the vertex in this phase calls it.
+// Finalise F_{j-1} bits of one vertex: the level bit-planes (seen took them at
+// discovery).  Only the thread that owns the vertex in this phase calls it.
 template <int W>
-__device__ __forceinline__ void finalise(const MsArgs &a, int32_t lev, size_t o, const u64 (&f)[W], u64 (&s)[W])
+__device__ __forceinline__ void finalise(const MsArgs &a, int32_t lev, size_t o, const u64 (&f)[W])
 {
-#pragma unroll
-    for (int q = 0; q < W; ++q) s[q] |= f[q];
-    stw<W>(a.seen + o, s);
     const size_t pstride = (size_t)a.n * W;
     for (int b = 0; (lev >> b) != 0; ++b) {
         if (!((lev >> b) & 1)) continue;
@@ -484,10 +491,9 @@ __device__ void td_update(const MsArgs &a, const Lvl &L)
     for (long long i = rank; i < L.qlen; i += size) {
         const int32_t v = __ldcg(L.qcur + i);
         const size_t o = (size_t)v * W;
-        u64 f[W], s[W];
+        u64 f[W];
         ldw<W>(L.fcur + o, f);
-        ldw<W>(a.seen + o, s);
-        finalise<W>(a, L.lev, o, f, s);
+        finalise<W>(a, L.lev, o, f);
 #pragma unroll
         for (int q = 0; q < W; ++q) act[q] |= f[q];
     }
@@ -867,9 +873,7 @@ __device__ __forceinline__ void bu_finalise(const MsArgs &a, const Lvl &L, int32
     u64 f[W];
     ldw<W>(L.fcur + o, f);
     if (anyw<W>(f)) {
-        u64 s[W];
-        ldw<W>(a.seen + o, s);
-        finalise<W>(a, L.lev, o, f, s);
+        finalise<W>(a, L.lev, o, f);
 #pragma unroll
         for (int q = 0; q < W; ++q) act[q] |= f[q];
     }
@@ -907,6 +911,9 @@ __device__ __forceinline__ void bu_found(const MsArgs &a, const Lvl &L, const Ct
     for (int q = 0; q < W; ++q) nb[q] = acc[q] & need[q];
     if (!anyw<W>(nb)) return;
     stw<W>(L.fnxt + (size_t)w * W, nb);  // the vertex's only writer in part B
+#pragma unroll
+    for (int q = 0; q < W; ++q)
+        if (nb[q]) red_or(a.seen + (size_t)w * W + q, nb[q]);
     if (W > 1 && L.rare_td) a.stamp[w] = L.tag;  // part C's visits must not append w again
     cq.push(a, L, w);
 }
@@ -1397,27 +1404,22 @@ __device__ void count_reached(const MsArgs &a, int row0, int nb)
     __syncthreads();
     const int lane = lane_id();
     const long long nw = G::size() >> 5;
-    unsigned c[2 * W] = {};
-    for (long long base = (G::rank() >> 5) * 32; base < a.n; base += nw * 32) {  // warp-uniform
-        const long long v = base + lane;
-        u64 sw[W] = {};
-        if (v < a.n) ldw<W>(a.seen + (size_t)v * W, sw);
-#pragma unroll
-        for (int q = 0; q < W; ++q) {
+    for (int q = 0; q < W; ++q) {  // one source word at a time: few live registers
+        unsigned c0 = 0, c1 = 0;
+        for (long long base = (G::rank() >> 5) * 32; base < a.n; base += nw * 32) {  // warp-uniform
+            const long long v = base + lane;
+            const u64 sw = v < a.n ? __ldcg(a.seen + (size_t)v * W + q) : 0ull;
             for (int b = 0; b < 32; ++b) {
-                const unsigned lo = __ballot_sync(FULL_MASK, (sw[q] >> b) & 1ull);
-                const unsigned hi = __ballot_sync(FULL_MASK, (sw[q] >> (b + 32)) & 1ull);
+                const unsigned lo = __ballot_sync(FULL_MASK, (sw >> b) & 1ull);
+                const unsigned hi = __ballot_sync(FULL_MASK, (sw >> (b + 32)) & 1ull);
                 if (lane == b) {
-                    c[2 * q] += __popc(lo);
-                    c[2 * q + 1] += __popc(hi);
+                    c0 += __popc(lo);
+                    c1 += __popc(hi);
                 }
             }
         }
-    }
-#pragma unroll
-    for (int q = 0; q < W; ++q) {
-        if (c[2 * q]) atomicAdd(&s_cnt[64 * q + lane], (unsigned long long)c[2 * q]);
-        if (c[2 * q + 1]) atomicAdd(&s_cnt[64 * q + 32 + lane], (unsigned long long)c[2 * q + 1]);
+        if (c0) atomicAdd(&s_cnt[64 * q + lane], (unsigned long long)c0);
+        if (c1) atomicAdd(&s_cnt[64 * q + 32 + lane], (unsigned long long)c1);
     }
     __syncthreads();
     for (int i = threadIdx.x; i < nb; i += blockDim.x)
@@ -1474,6 +1476,7 @@ __global__ void __launch_bounds__(MS_THREADS, MS_MIN_BLOCKS) ms_grid_kernel(MsAr
             const int q = (int)rank >> 6;
             const u64 bit = 1ull << (rank & 63);
             const u64 old = atomicOr(a.fr[0] + (size_t)s * W + q, bit);
+            red_or(a.seen + (size_t)s * W + q, bit);
             atomicOr(&ctl->active[0][q], bit);
             bool first;
             if (W == 1) first = old == 0;
