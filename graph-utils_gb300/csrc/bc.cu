@@ -20,9 +20,11 @@
 //   part[slots][W][64]  backward partial sums of vertices split into several items
 //   bc[n] double        accumulated over batches (output)
 // Work items (graph-static, ChunkMap): one per <= 256 edges of a vertex's in-
-// (forward) or out-adjacency (backward), times the W source words; a warp per
-// item, lane l owning sources 64q+l and 64q+32+l of word q.  One grid barrier
-// per level (two for backward levels with split vertices).
+// (forward) or out-adjacency (backward), times the word groups of the batch (up
+// to four source words, 256 sources, per group); a warp per item, lane l owning
+// sources 64q+l and 64q+32+l of each word q of the group, so an adjacency range
+// is read once for 256 sources.  One grid barrier per level (two for backward
+// levels with split vertices).
 #include "device_utils.cuh"
 #include "gu_internal.h"
 
@@ -81,12 +83,13 @@ struct BcArgs {
     BcCtl *ctl;
 };
 
-// Takes the next (up to) four set lanes of a ballot in ascending lane order; a
+// Takes the next (up to) K set lanes of a ballot in ascending lane order; a
 // missing one is reported as -1.
-__device__ __forceinline__ void next4(unsigned &bal, int (&src)[4])
+template <int K>
+__device__ __forceinline__ void next_lanes(unsigned &bal, int (&src)[K])
 {
 #pragma unroll
-    for (int t = 0; t < 4; ++t) {
+    for (int t = 0; t < K; ++t) {
         src[t] = bal ? __ffs(bal) - 1 : -1;
         if (bal) bal &= bal - 1;
     }
@@ -95,67 +98,177 @@ __device__ __forceinline__ void next4(unsigned &bal, int (&src)[4])
 __device__ __forceinline__ long long gwarp() { return ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; }
 __device__ __forceinline__ long long nwarps() { return ((long long)gridDim.x * blockDim.x) >> 5; }
 
-// Forward level j, word q, one work item (a range of w's in-edges): new bits =
-// sources of an in-neighbour's level j-1 not known at w (levels <= j-1);
-// sigma(w) += sum of the in-neighbours' sigma, each lane for its two sources.
-// seen lags one level: known = seen | lvl[j-1] is invariant while the first
-// item of w folds lvl[j-1] into seen.
-__device__ void bc_forward_item(const BcArgs &a, int j, int q, int c, u64 act, u64 &found_any)
+// A word group is NQ consecutive source words (NQ = min(W, 4)) handled by one
+// warp item: lane l owns sources 64q+l and 64q+32+l of each word q of the group.
+// The group's words of a vertex are contiguous and 8*NQ-byte aligned, so they
+// move as one vector access.
+template <int NQ>
+__device__ __forceinline__ void ldq(const u64 *p, u64 (&x)[NQ])
+{
+    if constexpr (NQ == 1) {
+        x[0] = __ldcg(p);
+    } else if constexpr (NQ == 2) {
+        const ulonglong2 v = __ldcg(reinterpret_cast<const ulonglong2 *>(p));
+        x[0] = v.x;
+        x[1] = v.y;
+    } else {
+        static_assert(NQ == 4, "word group of 1, 2 or 4 words");
+        asm volatile("ld.global.cg.v4.u64 {%0, %1, %2, %3}, [%4];"
+                     : "=l"(x[0]), "=l"(x[1]), "=l"(x[2]), "=l"(x[3]) : "l"(p) : "memory");
+    }
+}
+
+template <int NQ>
+__device__ __forceinline__ void stq(u64 *p, const u64 (&x)[NQ])
+{
+    if constexpr (NQ == 1) {
+        p[0] = x[0];
+    } else if constexpr (NQ == 2) {
+        *reinterpret_cast<ulonglong2 *>(p) = make_ulonglong2(x[0], x[1]);
+    } else {
+        asm volatile("st.global.v4.u64 [%0], {%1, %2, %3, %4};" ::"l"(p), "l"(x[0]), "l"(x[1]), "l"(x[2]), "l"(x[3])
+                     : "memory");
+    }
+}
+
+template <int NQ>
+__device__ __forceinline__ bool any_bits(const u64 (&x)[NQ])
+{
+    u64 o = 0;
+#pragma unroll
+    for (int t = 0; t < NQ; ++t) o |= x[t];
+    return o != 0;
+}
+
+// Per-warp staging of one 32-edge slice of an adjacency range: each lane
+// stores its edge's neighbour and mask, and the warp then walks the edges that
+// have work with broadcast reads (no shuffles, and the masks stay out of
+// registers while the loads are in flight).
+template <int NQ>
+struct EdgeStage {
+    u64 m[NQ][32];
+    int32_t v[32];
+    u64 k[NQ];  // forward: ~known at w; backward: the sources at w's level
+};
+
+// Writes lane t's copy of x[t] (t < NQ) to dst[t] without dynamic register indexing.
+template <int NQ>
+__device__ __forceinline__ void lanes_store(u64 *dst, const u64 (&x)[NQ], bool invert)
 {
     const int lane = lane_id();
-    const int B = 64 * a.W;
-    const size_t nW = (size_t)a.n * a.W;
+    u64 y = 0;
+#pragma unroll
+    for (int t = 0; t < NQ; ++t)
+        if (t == lane) y = x[t];
+    if (lane < NQ) dst[lane] = invert ? ~y : y;
+}
+
+// Forward level j, word group q0..q0+NQ-1, one work item (a range of w's
+// in-edges): new bits = sources of an in-neighbour's level j-1 not known at w
+// (levels <= j-1); sigma(w) += sum of the in-neighbours' sigma, each lane for
+// its sources, in CSR order.  seen lags one level: known = seen | lvl[j-1] is
+// invariant while the first item of w folds lvl[j-1] into seen.
+// act: the sources with a non-empty level j-1; new bits are ORed into found
+// (both in shared memory: they stay out of registers across items).
+template <int NQ>
+__device__ void bc_forward_item(const BcArgs &a, EdgeStage<NQ> &st, int j, int q0, int c, const u64 *act, u64 *found)
+{
+    constexpr int EPT = 4 / NQ;  // in-neighbours per trip: 8 sigma loads in flight per lane
+    const int lane = lane_id();
+    const int W = a.W, B = 64 * W;
+    const size_t nW = (size_t)a.n * W;
     const int32_t w = __ldg(a.cin.v + c);
-    const size_t wo = (size_t)w * a.W + q;
-    const u64 prevw = __ldcg(a.lvl + (size_t)(j - 1) * nW + wo);
-    const u64 known = __ldcg(a.seen + wo) | prevw;
+    const size_t wo = (size_t)w * W + q0;
     const int32_t e0 = __ldg(a.cin.e0 + c), e1 = __ldg(a.cin.e1 + c);
-    const bool first_item = e0 == __ldg(a.RT + w);
-    if (first_item && lane == 0 && prevw) a.seen[wo] = known;
-    if ((act & ~known) == 0) return;
-    const u64 *prev = a.lvl + (size_t)(j - 1) * nW;
-    u64 nb = 0, acc0 = 0, acc1 = 0;
+    {
+        u64 known[NQ], prevw[NQ];
+        ldq<NQ>(a.lvl + (size_t)(j - 1) * nW + wo, prevw);
+        ldq<NQ>(a.seen + wo, known);
+        u64 need = 0;
+#pragma unroll
+        for (int t = 0; t < NQ; ++t) {
+            known[t] |= prevw[t];
+            need |= act[t] & ~known[t];
+        }
+        if (any_bits(prevw) && lane == 0 && e0 == __ldg(a.RT + w)) stq<NQ>(a.seen + wo, known);
+        if (need == 0) return;
+        lanes_store<NQ>(st.k, known, true);
+    }
+    __syncwarp();
+    const u64 *prev = a.lvl + (size_t)(j - 1) * nW + q0;
+    const u64 *sig = a.sigma + 64 * q0 + lane;
+    u64 acc0[NQ], acc1[NQ];
+#pragma unroll
+    for (int t = 0; t < NQ; ++t) acc0[t] = acc1[t] = 0;
+    unsigned hit = 0;  // bit 2t+h: the lane's source 64(q0+t)+32h+lane has a predecessor
     for (int32_t eb = e0; eb < e1; eb += 32) {
         const int32_t e = eb + lane;
-        int32_t v = -1;
-        u64 m = 0;
+        bool any = false;
         if (e < e1) {
-            v = __ldg(a.CT + e);
-            m = __ldcg(prev + (size_t)v * a.W + q) & ~known;
-        }
-        unsigned bal = __ballot_sync(FULL_MASK, m != 0);
-        while (bal) {  // four in-neighbours per trip: eight loads in flight per lane
-            int src[4];
-            next4(bal, src);
-            u64 x0[4], x1[4];
+            const int32_t v = __ldg(a.CT + e);
+            u64 m[NQ];
+            ldq<NQ>(prev + (size_t)v * W, m);
 #pragma unroll
-            for (int t = 0; t < 4; ++t) {
-                const int sl = src[t] < 0 ? src[0] : src[t];
-                const int32_t vv = __shfl_sync(FULL_MASK, v, sl);
-                const u64 mm = src[t] < 0 ? 0ull : __shfl_sync(FULL_MASK, m, sl);
-                nb |= mm;
-                const u64 *sv = a.sigma + (size_t)vv * B + 64 * q;
-                x0[t] = ((mm >> lane) & 1ull) ? __ldcg(sv + lane) : 0ull;
-                x1[t] = ((mm >> (lane + 32)) & 1ull) ? __ldcg(sv + lane + 32) : 0ull;
+            for (int t = 0; t < NQ; ++t) {
+                m[t] &= st.k[t];
+                st.m[t][lane] = m[t];
             }
-            acc0 += (x0[0] + x0[1]) + (x0[2] + x0[3]);
-            acc1 += (x1[0] + x1[1]) + (x1[2] + x1[3]);
+            st.v[lane] = v;
+            any = any_bits(m);
         }
+        unsigned bal = __ballot_sync(FULL_MASK, any);
+        __syncwarp();
+        while (bal) {
+            int src[EPT];
+            next_lanes<EPT>(bal, src);
+            u64 x0[EPT][NQ], x1[EPT][NQ];
+#pragma unroll
+            for (int u = 0; u < EPT; ++u) {
+                const bool ok = src[u] >= 0;
+                const int sl = ok ? src[u] : 0;
+                const u64 *sv = sig + (size_t)st.v[sl] * B;
+#pragma unroll
+                for (int t = 0; t < NQ; ++t) {
+                    const u64 mm = ok ? st.m[t][sl] : 0ull;
+                    const unsigned h0 = (unsigned)(mm >> lane) & 1u, h1 = (unsigned)(mm >> (lane + 32)) & 1u;
+                    hit |= (h0 | (h1 << 1)) << (2 * t);
+                    x0[u][t] = h0 ? __ldcg(sv + 64 * t) : 0ull;
+                    x1[u][t] = h1 ? __ldcg(sv + 64 * t + 32) : 0ull;
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < EPT; ++u)
+#pragma unroll
+                for (int t = 0; t < NQ; ++t) {
+                    acc0[t] += x0[u][t];
+                    acc1[t] += x1[u][t];
+                }
+        }
+        __syncwarp();
     }
-    if (!nb) return;
+    u64 nb[NQ];
+#pragma unroll
+    for (int t = 0; t < NQ; ++t)
+        nb[t] = (u64)__ballot_sync(FULL_MASK, (hit >> (2 * t)) & 1u) |
+                ((u64)__ballot_sync(FULL_MASK, (hit >> (2 * t + 1)) & 1u) << 32);
+    if (!any_bits(nb)) return;
     const bool split = __ldg(a.cin.slot + c) >= 0;
-    u64 *sw = a.sigma + (size_t)w * B + 64 * q;
+    u64 *sw = a.sigma + (size_t)w * B + 64 * q0 + lane;
     u64 *lw = a.lvl + (size_t)j * nW + wo;
-    if (split) {  // sigma rows of split vertices were zeroed for the batch
-        if ((nb >> lane) & 1ull) atomicAdd(sw + lane, acc0);
-        if ((nb >> (lane + 32)) & 1ull) atomicAdd(sw + lane + 32, acc1);
-        if (lane == 0) atomicOr(lw, nb);
-    } else {
-        if ((nb >> lane) & 1ull) sw[lane] = acc0;
-        if ((nb >> (lane + 32)) & 1ull) sw[lane + 32] = acc1;
-        if (lane == 0) *lw = nb;
+#pragma unroll
+    for (int t = 0; t < NQ; ++t) {
+        const bool h0 = (hit >> (2 * t)) & 1u, h1 = (hit >> (2 * t + 1)) & 1u;
+        if (split) {  // sigma rows of split vertices were zeroed for the batch
+            if (h0) atomicAdd(sw + 64 * t, acc0[t]);
+            if (h1) atomicAdd(sw + 64 * t + 32, acc1[t]);
+            if (lane == 0 && nb[t]) atomicOr(lw + t, nb[t]);
+        } else {
+            if (h0) sw[64 * t] = acc0[t];
+            if (h1) sw[64 * t + 32] = acc1[t];
+        }
+        if (lane == 0 && nb[t] & ~found[t]) atomicOr(found + t, nb[t]);
     }
-    found_any |= nb;
+    if (!split && lane == 0) stq<NQ>(lw, nb);
 }
 
 // Backward dependencies are carried as beta_s(v) = (1 + delta_s(v)) / sigma_s(v):
@@ -171,87 +284,168 @@ __device__ __forceinline__ void finish_delta(const BcArgs &a, size_t o, double S
     a.beta[o] = (1.0 + d) / sg;
 }
 
-// Backward level l, word q, one work item (a range of w's out-edges): for the
-// sources whose level of w is l, sum beta over successors v (level l+1) in CSR
-// order.  Unsplit vertices finish delta/beta directly; split ones store
-// per-item partial sums, added in item order by bc_combine_item after a barrier.
-__device__ void bc_backward_item(const BcArgs &a, int l, int L, int q, int c)
+// Backward level l, word group q0.., one work item (a range of w's out-edges):
+// for the sources whose level of w is l, sum beta over successors v (level
+// l+1) in CSR order.  Unsplit vertices finish delta/beta directly; split ones
+// store per-item partial sums, added in item order by bc_combine_item after a
+// barrier.
+//
+// FP64 instructions are the scarce resource here (a warp instruction costs the
+// same however few of its lanes have work), so the sums live in shared memory,
+// one per source of the group, and the adds are compacted: for each successor
+// the set bits of its mask become a dense list of sources, and a warp
+// instruction adds 32 of them.  Each source still receives its successors'
+// terms one at a time in CSR order (a successor's list holds a source at most
+// once, and successive lists are separated by __syncwarp), so the sums are the
+// sequential CSR-order sums.
+template <int NQ>
+struct SumStage {
+    double acc[64 * NQ];
+    unsigned char pos[4][64 * NQ];  // dense source lists of up to four successors
+};
+
+// Writes the positions (0 .. 64*NQ-1) of the set bits of m into list in
+// ascending order; returns how many there are.
+template <int NQ>
+__device__ __forceinline__ int compact_bits(const u64 (&m)[NQ], unsigned char *list)
 {
     const int lane = lane_id();
-    const int B = 64 * a.W;
-    const size_t nW = (size_t)a.n * a.W;
+    const unsigned below = (1u << lane) - 1u;
+    int base = 0;
+#pragma unroll
+    for (int t = 0; t < NQ; ++t) {
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const unsigned x = (unsigned)(m[t] >> (32 * h));
+            if ((x >> lane) & 1u) list[base + __popc(x & below)] = (unsigned char)(64 * t + 32 * h + lane);
+            base += __popc(x);
+        }
+    }
+    return base;
+}
+
+template <int NQ>
+__device__ void bc_backward_item(const BcArgs &a, EdgeStage<NQ> &st, SumStage<NQ> &ss, int l, int L, int q0, int c)
+{
+    const int lane = lane_id();
+    const int W = a.W, B = 64 * W;
+    const size_t nW = (size_t)a.n * W;
     const int32_t w = __ldg(a.cout.v + c);
-    const u64 lm = __ldcg(a.lvl + (size_t)l * nW + (size_t)w * a.W + q);
-    if (lm == 0) return;
-    const bool own0 = (lm >> lane) & 1ull, own1 = (lm >> (lane + 32)) & 1ull;
-    double acc0 = 0.0, acc1 = 0.0;
+    {
+        u64 lm[NQ];
+        ldq<NQ>(a.lvl + (size_t)l * nW + (size_t)w * W + q0, lm);
+        if (!any_bits(lm)) return;
+        lanes_store<NQ>(st.k, lm, false);
+    }
+#pragma unroll
+    for (int t = 0; t < 2 * NQ; ++t) ss.acc[32 * t + lane] = 0.0;
+    __syncwarp();
     if (l < L) {
-        const u64 *next = a.lvl + (size_t)(l + 1) * nW;
+        const u64 *next = a.lvl + (size_t)(l + 1) * nW + q0;
+        const double *bet = a.beta + 64 * q0;
         const int32_t e0 = __ldg(a.cout.e0 + c), e1 = __ldg(a.cout.e1 + c);
         for (int32_t eb = e0; eb < e1; eb += 32) {
             const int32_t e = eb + lane;
-            int32_t v = -1;
-            u64 m = 0;
+            bool any = false;
             if (e < e1) {
-                v = __ldg(a.C + e);
-                m = __ldcg(next + (size_t)v * a.W + q) & lm;
+                const int32_t v = __ldg(a.C + e);
+                u64 m[NQ];
+                ldq<NQ>(next + (size_t)v * W, m);
+#pragma unroll
+                for (int t = 0; t < NQ; ++t) {
+                    m[t] &= st.k[t];
+                    st.m[t][lane] = m[t];
+                }
+                st.v[lane] = v;
+                any = any_bits(m);
             }
-            unsigned bal = __ballot_sync(FULL_MASK, m != 0);
-            while (bal) {  // four successors per trip, added in CSR order
+            unsigned bal = __ballot_sync(FULL_MASK, any);
+            __syncwarp();
+            while (bal) {  // up to four successors at a time, in CSR order
                 int src[4];
-                next4(bal, src);
-                double b0[4], b1[4];
-                bool h0[4], h1[4];
+                next_lanes<4>(bal, src);
+                int cnt[4], cum[4], rounds = 0;
 #pragma unroll
-                for (int t = 0; t < 4; ++t) {
-                    const int sl = src[t] < 0 ? src[0] : src[t];
-                    const int32_t vv = __shfl_sync(FULL_MASK, v, sl);
-                    const u64 mm = src[t] < 0 ? 0ull : __shfl_sync(FULL_MASK, m, sl);
-                    const double *bv = a.beta + (size_t)vv * B + 64 * q;
-                    h0[t] = (mm >> lane) & 1ull;
-                    h1[t] = (mm >> (lane + 32)) & 1ull;
-                    b0[t] = h0[t] ? __ldcg(bv + lane) : 0.0;
-                    b1[t] = h1[t] ? __ldcg(bv + lane + 32) : 0.0;
+                for (int u = 0; u < 4; ++u) {
+                    cnt[u] = 0;
+                    if (src[u] >= 0) {
+                        u64 mm[NQ];
+#pragma unroll
+                        for (int t = 0; t < NQ; ++t) mm[t] = st.m[t][src[u]];
+                        cnt[u] = compact_bits<NQ>(mm, ss.pos[u]);
+                    }
+                    rounds += (cnt[u] + 31) >> 5;
+                    cum[u] = rounds;
                 }
+                __syncwarp();
+                for (int r0 = 0; r0 < rounds; r0 += 4) {
+                    double b[4];
+                    int s[4];
 #pragma unroll
-                for (int t = 0; t < 4; ++t) {
-                    if (h0[t]) acc0 += b0[t];
-                    if (h1[t]) acc1 += b1[t];
+                    for (int z = 0; z < 4; ++z) {  // four loads in flight per lane
+                        const int rr = r0 + z;
+                        const int u = (rr >= cum[0]) + (rr >= cum[1]) + (rr >= cum[2]);
+                        const int first = u == 0 ? 0 : u == 1 ? cum[0] : u == 2 ? cum[1] : cum[2];
+                        const int n_u = u == 0 ? cnt[0] : u == 1 ? cnt[1] : u == 2 ? cnt[2] : cnt[3];
+                        const int s_u = u == 0 ? src[0] : u == 1 ? src[1] : u == 2 ? src[2] : src[3];
+                        const int i = 32 * (rr - first) + lane;
+                        s[z] = -1;
+                        b[z] = 0.0;
+                        if (rr < rounds && i < n_u) {
+                            s[z] = ss.pos[u][i];
+                            b[z] = __ldcg(bet + (size_t)st.v[s_u] * B + s[z]);
+                        }
+                    }
+#pragma unroll
+                    for (int z = 0; z < 4; ++z) {
+                        if (s[z] >= 0) ss.acc[s[z]] += b[z];
+                        __syncwarp();
+                    }
                 }
             }
+            __syncwarp();
         }
     }
+    // the sources of w at level l, densely: one division per source
+    u64 lm[NQ];
+#pragma unroll
+    for (int t = 0; t < NQ; ++t) lm[t] = st.k[t];
+    const int cnt = compact_bits<NQ>(lm, ss.pos[0]);
+    __syncwarp();
     const int32_t slot = __ldg(a.cout.slot + c);
-    if (slot >= 0) {
-        double *p = a.part + ((size_t)slot * a.W + q) * 64;
-        p[lane] = own0 ? acc0 : 0.0;
-        p[lane + 32] = own1 ? acc1 : 0.0;
-    } else {
-        const size_t o = (size_t)w * B + 64 * q;
-        if (own0) finish_delta(a, o + lane, acc0);
-        if (own1) finish_delta(a, o + lane + 32, acc1);
+    for (int i = lane; i < cnt; i += 32) {
+        const int s = ss.pos[0][i];
+        const double S = ss.acc[s];
+        if (slot >= 0) a.part[((size_t)slot * W + q0) * 64 + s] = S;
+        else finish_delta(a, (size_t)w * B + 64 * q0 + s, S);
     }
+    __syncwarp();
 }
 
-// delta of a split vertex = its items' partials added in item order.
-__device__ void bc_combine_item(const BcArgs &a, int l, int q, int i)
+// delta of a split vertex = its items' partials added in item order, for the
+// vertex's sources at level l taken densely.
+template <int NQ>
+__device__ void bc_combine_item(const BcArgs &a, EdgeStage<NQ> &st, SumStage<NQ> &ss, int l, int q0, int i)
 {
     const int lane = lane_id();
-    const int B = 64 * a.W;
-    const size_t nW = (size_t)a.n * a.W;
+    const int W = a.W, B = 64 * W;
+    const size_t nW = (size_t)a.n * W;
     const int32_t w = __ldg(a.cout.mv + i);
-    const u64 lm = __ldcg(a.lvl + (size_t)l * nW + (size_t)w * a.W + q);
-    if (lm == 0) return;
+    u64 lm[NQ];
+    ldq<NQ>(a.lvl + (size_t)l * nW + (size_t)w * W + q0, lm);
+    if (!any_bits(lm)) return;
+    const int cnt = compact_bits<NQ>(lm, ss.pos[0]);
+    __syncwarp();
     const int32_t c0 = __ldg(a.cout.mfirst + i), nc = __ldg(a.cout.mcount + i);
-    double s0 = 0.0, s1 = 0.0;
-    for (int32_t c = c0; c < c0 + nc; ++c) {
-        const double *p = a.part + ((size_t)__ldg(a.cout.slot + c) * a.W + q) * 64;
-        s0 += __ldcg(p + lane);
-        s1 += __ldcg(p + lane + 32);
+    for (int k = lane; k < cnt; k += 32) {
+        const int s = ss.pos[0][k];
+        double S = 0.0;
+        for (int32_t c = c0; c < c0 + nc; ++c)
+            S += __ldcg(a.part + ((size_t)__ldg(a.cout.slot + c) * W + q0) * 64 + s);
+        finish_delta(a, (size_t)w * B + 64 * q0 + s, S);
     }
-    const size_t o = (size_t)w * B + 64 * q;
-    if ((lm >> lane) & 1ull) finish_delta(a, o + lane, s0);
-    if ((lm >> (lane + 32)) & 1ull) finish_delta(a, o + lane + 32, s1);
+    __syncwarp();
+    (void)st;
 }
 
 // bc_r[w] += sum of delta over the batch's sources of request r whose level of
@@ -333,9 +527,14 @@ __device__ void bc_rows_item(const BcArgs &a, int32_t w, int q, int row0, int nb
     }
 }
 
+// NQ = words per work item: min(W, 4).
+template <int NQ>
 __global__ void __launch_bounds__(BC_THREADS, 2) bc_grid_kernel(BcArgs a, int do_backward)
 {
     __shared__ u64 s_act[16];
+    __shared__ EdgeStage<NQ> s_stage[BC_THREADS / 32];
+    extern __shared__ __align__(16) unsigned char s_dyn[];  // SumStage<NQ> per warp (backward only)
+    SumStage<NQ> *s_sum = reinterpret_cast<SumStage<NQ> *>(s_dyn);
     __shared__ BcCtl s_ctl;  // control block as read by thread 0 after each barrier
     unsigned epoch = 0;
     BcCtl *ctl = a.ctl;
@@ -387,12 +586,13 @@ __global__ void __launch_bounds__(BC_THREADS, 2) bc_grid_kernel(BcArgs a, int do
                 for (int q = 0; q < 16; ++q) ctl->active[j & 1][q] = 0;
             }
             if (!barrier()) return;
-            for (int q = 0; q < W; ++q) {
-                const u64 act = s_ctl.active[(j - 1) & 1][q];
-                u64 found = 0;
+            for (int q0 = 0; q0 < W; q0 += NQ) {
+                const u64 *act = &s_ctl.active[(j - 1) & 1][q0];
+                u64 any = 0;
+                for (int t = 0; t < NQ; ++t) any |= act[t];
+                if (!any) continue;
                 for (long long c = gwarp(); c < a.cin.nchunks; c += nwarps())
-                    bc_forward_item(a, j, q, (int)c, act, found);
-                if (lane_id() == 0 && found) atomicOr(&s_act[q], found);
+                    bc_forward_item<NQ>(a, s_stage[warp_in_block()], j, q0, (int)c, act, &s_act[q0]);
             }
             __syncthreads();
             if (threadIdx.x < W && s_act[threadIdx.x]) {
@@ -409,12 +609,14 @@ __global__ void __launch_bounds__(BC_THREADS, 2) bc_grid_kernel(BcArgs a, int do
         if (rank == 0 && L > ctl->max_level) ctl->max_level = L;
         if (do_backward) {
             for (int l = L; l >= 1; --l) {
-                for (int q = 0; q < W; ++q)
-                    for (long long c = gwarp(); c < a.cout.nchunks; c += nwarps()) bc_backward_item(a, l, L, q, (int)c);
+                for (int q0 = 0; q0 < W; q0 += NQ)
+                    for (long long c = gwarp(); c < a.cout.nchunks; c += nwarps())
+                        bc_backward_item<NQ>(a, s_stage[warp_in_block()], s_sum[warp_in_block()], l, L, q0, (int)c);
                 if (!barrier()) return;
                 if (a.cout.nmulti) {
-                    for (int q = 0; q < W; ++q)
-                        for (long long i = gwarp(); i < a.cout.nmulti; i += nwarps()) bc_combine_item(a, l, q, (int)i);
+                    for (int q0 = 0; q0 < W; q0 += NQ)
+                        for (long long i = gwarp(); i < a.cout.nmulti; i += nwarps())
+                            bc_combine_item<NQ>(a, s_stage[warp_in_block()], s_sum[warp_in_block()], l, q0, (int)i);
                     if (!barrier()) return;
                 }
             }
@@ -586,9 +788,17 @@ void launch_bc(DeviceGraph &g, const int32_t *sources, int32_t k, const BcOption
     a.delta_rows = delta_rows;
     a.ld = ld;
     GU_CUDA_CHECK(cudaMemsetAsync(a.ctl, 0, sizeof(BcCtl), stream));
-    static int blocks_per_sm = -1;
+    const void *kern = W == 1 ? (const void *)bc_grid_kernel<1>
+                       : W == 2 ? (const void *)bc_grid_kernel<2> : (const void *)bc_grid_kernel<4>;
+    const int ki = W == 1 ? 0 : W == 2 ? 1 : 2;
+    const size_t dyn = (size_t)(BC_THREADS / 32) * (W == 1   ? sizeof(SumStage<1>)
+                                                    : W == 2 ? sizeof(SumStage<2>)
+                                                             : sizeof(SumStage<4>));
+    static int occupancy[3] = {-1, -1, -1};
+    int &blocks_per_sm = occupancy[ki];
     if (blocks_per_sm < 0) {
-        GU_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, bc_grid_kernel, BC_THREADS, 0));
+        GU_CUDA_CHECK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
+        GU_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, kern, BC_THREADS, dyn));
         if (blocks_per_sm < 1) throw gu_error(GU_ERR_INTERNAL, "bc kernel cannot be resident");
     }
     int nblocks = g.sm_count * blocks_per_sm;
@@ -597,7 +807,7 @@ void launch_bc(DeviceGraph &g, const int32_t *sources, int32_t k, const BcOption
     int do_backward = backward ? 1 : 0;
     void *params[] = {&a, &do_backward};
     if (opt.timed) g.mark_start(stream);
-    GU_CUDA_CHECK(cudaLaunchCooperativeKernel((const void *)bc_grid_kernel, grid, block, params, 0, stream));
+    GU_CUDA_CHECK(cudaLaunchCooperativeKernel(kern, grid, block, params, dyn, stream));
     if (opt.timed) g.mark_stop(stream);
 }
 
