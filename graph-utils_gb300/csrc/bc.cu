@@ -28,21 +28,25 @@
 #include "device_utils.cuh"
 #include "gu_internal.h"
 
+#include <algorithm>
 #include <climits>
 #include <cstdlib>
 #include <memory>
+#include <vector>
 
 namespace gu {
 
 constexpr int BC_THREADS = 512;
+constexpr int BC_UNIT_COST = 512;     // edges per work unit (about)
+constexpr int BC_ITEM_OVERHEAD = 16;  // an item's fixed cost, in edges
 
 struct __align__(128) BcCtl {
     unsigned bar;
     int err;
     int max_level;  // deepest forward level over all batches
-    int pad0;
-    int found[2];   // forward: any new bit at level j (by parity)
-    int pad1[2];
+    unsigned fwork;   // forward: next work unit of the level
+    int found[2];     // forward: any new bit at level j (by parity)
+    unsigned work[2]; // backward: next work unit of level l (by parity)
     u64 active[2][16];  // sources with a non-empty level, by parity
 };
 static_assert(sizeof(BcCtl) <= 512, "control block");
@@ -52,6 +56,8 @@ enum : int { DEV_ERR_LEVELS = 3 };
 struct DevChunks {
     const int32_t *v, *e0, *e1, *slot;
     int32_t nchunks;
+    const int32_t *order, *ustart;
+    int32_t nunits;
     const int32_t *mv, *mfirst, *mcount;
     int32_t nmulti;
 };
@@ -148,7 +154,9 @@ template <int NQ>
 struct EdgeStage {
     u64 m[NQ][32];
     int32_t v[32];
-    u64 k[NQ];  // forward: ~known at w; backward: the sources at w's level
+    u64 k[NQ];        // forward: ~known at w; backward: the sources at w's level
+    u64 tk[NQ][32];   // triage of a work unit: lane t's item's k words
+    int32_t tc[32];   // ... and the item
 };
 
 // Writes lane t's copy of x[t] (t < NQ) to dst[t] without dynamic register indexing.
@@ -171,7 +179,7 @@ __device__ __forceinline__ void lanes_store(u64 *dst, const u64 (&x)[NQ], bool i
 // act: the sources with a non-empty level j-1; new bits are ORed into found
 // (both in shared memory: they stay out of registers across items).
 template <int NQ>
-__device__ void bc_forward_item(const BcArgs &a, EdgeStage<NQ> &st, int j, int q0, int c, const u64 *act, u64 *found)
+__device__ void bc_forward_item(const BcArgs &a, EdgeStage<NQ> &st, int j, int q0, int c, u64 *found)
 {
     constexpr int EPT = 4 / NQ;  // in-neighbours per trip: 8 sigma loads in flight per lane
     const int lane = lane_id();
@@ -180,21 +188,6 @@ __device__ void bc_forward_item(const BcArgs &a, EdgeStage<NQ> &st, int j, int q
     const int32_t w = __ldg(a.cin.v + c);
     const size_t wo = (size_t)w * W + q0;
     const int32_t e0 = __ldg(a.cin.e0 + c), e1 = __ldg(a.cin.e1 + c);
-    {
-        u64 known[NQ], prevw[NQ];
-        ldq<NQ>(a.lvl + (size_t)(j - 1) * nW + wo, prevw);
-        ldq<NQ>(a.seen + wo, known);
-        u64 need = 0;
-#pragma unroll
-        for (int t = 0; t < NQ; ++t) {
-            known[t] |= prevw[t];
-            need |= act[t] & ~known[t];
-        }
-        if (any_bits(prevw) && lane == 0 && e0 == __ldg(a.RT + w)) stq<NQ>(a.seen + wo, known);
-        if (need == 0) return;
-        lanes_store<NQ>(st.k, known, true);
-    }
-    __syncwarp();
     const u64 *prev = a.lvl + (size_t)(j - 1) * nW + q0;
     const u64 *sig = a.sigma + 64 * q0 + lane;
     u64 acc0[NQ], acc1[NQ];
@@ -271,6 +264,48 @@ __device__ void bc_forward_item(const BcArgs &a, EdgeStage<NQ> &st, int j, int q
     if (!split && lane == 0) stq<NQ>(lw, nb);
 }
 
+// Forward, one work unit of word group q0: its (up to 32) items are triaged a
+// lane each -- fold lvl[j-1] into seen at a vertex's first item, and keep the
+// items with an active source not yet known -- and the warp then runs those
+// items one at a time.  act: the sources with a non-empty level j-1 (shared).
+template <int NQ>
+__device__ void bc_forward_unit(const BcArgs &a, EdgeStage<NQ> &st, int j, int q0, int u, const u64 *act, u64 *found)
+{
+    const int lane = lane_id();
+    const int W = a.W;
+    const size_t nW = (size_t)a.n * W;
+    const int32_t i0 = __ldg(a.cin.ustart + u), i1 = __ldg(a.cin.ustart + u + 1);
+    bool need = false;
+    if (lane < i1 - i0) {
+        const int32_t c = __ldg(a.cin.order + i0 + lane);
+        const int32_t w = __ldg(a.cin.v + c);
+        const size_t wo = (size_t)w * W + q0;
+        u64 known[NQ], prevw[NQ];
+        ldq<NQ>(a.lvl + (size_t)(j - 1) * nW + wo, prevw);
+        ldq<NQ>(a.seen + wo, known);
+        u64 nd = 0;
+#pragma unroll
+        for (int t = 0; t < NQ; ++t) {
+            known[t] |= prevw[t];
+            nd |= act[t] & ~known[t];
+            st.tk[t][lane] = ~known[t];
+        }
+        st.tc[lane] = c;
+        if (any_bits(prevw) && __ldg(a.cin.e0 + c) == __ldg(a.RT + w)) stq<NQ>(a.seen + wo, known);
+        need = nd != 0;
+    }
+    unsigned bal = __ballot_sync(FULL_MASK, need);
+    __syncwarp();
+    while (bal) {
+        const int t = __ffs(bal) - 1;
+        bal &= bal - 1;
+        if (lane < NQ) st.k[lane] = st.tk[lane][t];
+        __syncwarp();
+        bc_forward_item<NQ>(a, st, j, q0, st.tc[t], found);
+        __syncwarp();
+    }
+}
+
 // Backward dependencies are carried as beta_s(v) = (1 + delta_s(v)) / sigma_s(v):
 // delta_s(w) = sigma_s(w) * sum over successors v of beta_s(v), so a successor
 // costs one FP64 add and each (vertex, source) pair one division (FP64 is the
@@ -331,12 +366,6 @@ __device__ void bc_backward_item(const BcArgs &a, EdgeStage<NQ> &st, SumStage<NQ
     const int W = a.W, B = 64 * W;
     const size_t nW = (size_t)a.n * W;
     const int32_t w = __ldg(a.cout.v + c);
-    {
-        u64 lm[NQ];
-        ldq<NQ>(a.lvl + (size_t)l * nW + (size_t)w * W + q0, lm);
-        if (!any_bits(lm)) return;
-        lanes_store<NQ>(st.k, lm, false);
-    }
 #pragma unroll
     for (int t = 0; t < 2 * NQ; ++t) ss.acc[32 * t + lane] = 0.0;
     __syncwarp();
@@ -420,6 +449,37 @@ __device__ void bc_backward_item(const BcArgs &a, EdgeStage<NQ> &st, SumStage<NQ
         else finish_delta(a, (size_t)w * B + 64 * q0 + s, S);
     }
     __syncwarp();
+}
+
+// Backward, one work unit of word group q0: lanes triage its items (keep those
+// whose vertex has a source at level l), then the warp runs them in turn.
+template <int NQ>
+__device__ void bc_backward_unit(const BcArgs &a, EdgeStage<NQ> &st, SumStage<NQ> &ss, int l, int L, int q0, int u)
+{
+    const int lane = lane_id();
+    const int W = a.W;
+    const size_t nW = (size_t)a.n * W;
+    const int32_t i0 = __ldg(a.cout.ustart + u), i1 = __ldg(a.cout.ustart + u + 1);
+    bool need = false;
+    if (lane < i1 - i0) {
+        const int32_t c = __ldg(a.cout.order + i0 + lane);
+        u64 lm[NQ];
+        ldq<NQ>(a.lvl + (size_t)l * nW + (size_t)__ldg(a.cout.v + c) * W + q0, lm);
+#pragma unroll
+        for (int t = 0; t < NQ; ++t) st.tk[t][lane] = lm[t];
+        st.tc[lane] = c;
+        need = any_bits(lm);
+    }
+    unsigned bal = __ballot_sync(FULL_MASK, need);
+    __syncwarp();
+    while (bal) {
+        const int t = __ffs(bal) - 1;
+        bal &= bal - 1;
+        if (lane < NQ) st.k[lane] = st.tk[lane][t];
+        __syncwarp();
+        bc_backward_item<NQ>(a, st, ss, l, L, q0, st.tc[t]);
+        __syncwarp();
+    }
 }
 
 // delta of a split vertex = its items' partials added in item order, for the
@@ -559,6 +619,7 @@ __global__ void __launch_bounds__(BC_THREADS, 2) bc_grid_kernel(BcArgs a, int do
         for (long long i = rank; i < (long long)a.cin.nmulti * B; i += size)
             a.sigma[(size_t)__ldg(a.cin.mv + i / B) * B + (i % B)] = 0ull;
         if (rank == 0) {
+            ctl->work[0] = ctl->work[1] = 0;
             ctl->found[0] = ctl->found[1] = 0;
             for (int q = 0; q < 16; ++q) ctl->active[0][q] = ctl->active[1][q] = 0;
         }
@@ -582,17 +643,21 @@ __global__ void __launch_bounds__(BC_THREADS, 2) bc_grid_kernel(BcArgs a, int do
             }
             for (size_t i = (size_t)rank; i < nW; i += (size_t)size) a.lvl[(size_t)j * nW + i] = 0;
             if (rank == 0) {
+                ctl->fwork = 0;
                 ctl->found[j & 1] = 0;
                 for (int q = 0; q < 16; ++q) ctl->active[j & 1][q] = 0;
             }
             if (!barrier()) return;
-            for (int q0 = 0; q0 < W; q0 += NQ) {
-                const u64 *act = &s_ctl.active[(j - 1) & 1][q0];
-                u64 any = 0;
-                for (int t = 0; t < NQ; ++t) any |= act[t];
-                if (!any) continue;
-                for (long long c = gwarp(); c < a.cin.nchunks; c += nwarps())
-                    bc_forward_item<NQ>(a, s_stage[warp_in_block()], j, q0, (int)c, act, &s_act[q0]);
+            // work units of all word groups, taken dynamically (unit x = group x / nunits)
+            const long long nfw = (long long)(W / NQ) * a.cin.nunits;
+            for (;;) {
+                long long x = 0;
+                if (lane_id() == 0) x = atomicAdd(&ctl->fwork, 1u);
+                x = __shfl_sync(FULL_MASK, x, 0);
+                if (x >= nfw) break;
+                const int q0 = (int)(x / a.cin.nunits) * NQ;
+                bc_forward_unit<NQ>(a, s_stage[warp_in_block()], j, q0, (int)(x % a.cin.nunits),
+                                    &s_ctl.active[(j - 1) & 1][q0], &s_act[q0]);
             }
             __syncthreads();
             if (threadIdx.x < W && s_act[threadIdx.x]) {
@@ -609,9 +674,16 @@ __global__ void __launch_bounds__(BC_THREADS, 2) bc_grid_kernel(BcArgs a, int do
         if (rank == 0 && L > ctl->max_level) ctl->max_level = L;
         if (do_backward) {
             for (int l = L; l >= 1; --l) {
-                for (int q0 = 0; q0 < W; q0 += NQ)
-                    for (long long c = gwarp(); c < a.cout.nchunks; c += nwarps())
-                        bc_backward_item<NQ>(a, s_stage[warp_in_block()], s_sum[warp_in_block()], l, L, q0, (int)c);
+                if (rank == 0) ctl->work[(l - 1) & 1] = 0;  // level l-1's counter (last used by level l+1)
+                const long long nbw = (long long)(W / NQ) * a.cout.nunits;
+                for (;;) {
+                    long long x = 0;
+                    if (lane_id() == 0) x = atomicAdd(&ctl->work[l & 1], 1u);
+                    x = __shfl_sync(FULL_MASK, x, 0);
+                    if (x >= nbw) break;
+                    bc_backward_unit<NQ>(a, s_stage[warp_in_block()], s_sum[warp_in_block()], l, L,
+                                         (int)(x / a.cout.nunits) * NQ, (int)(x % a.cout.nunits));
+                }
                 if (!barrier()) return;
                 if (a.cout.nmulti) {
                     for (int q0 = 0; q0 < W; q0 += NQ)
@@ -658,6 +730,23 @@ static void build_chunks(DeviceGraph &g, const std::vector<int32_t> &R, ChunkMap
         GU_CUDA_CHECK(cudaMemcpy(dst, src.data(), sizeof(int32_t) * src.size(), cudaMemcpyHostToDevice));
         g.bytes += sizeof(int32_t) * src.size();
     };
+    // work units: items by descending edge count (heavy items are taken first,
+    // light ones fill the gaps), cut into runs of at most 32 items and about
+    // BC_UNIT_COST edges (an item counts its edges plus a fixed overhead)
+    std::vector<int32_t> order(v.size()), ustart;
+    for (size_t i = 0; i < order.size(); ++i) order[i] = (int32_t)i;
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int32_t x, int32_t y) { return e1[x] - e0[x] > e1[y] - e0[y]; });
+    int cost = 0, cnt = 0;
+    for (size_t i = 0; i < order.size(); ++i) {
+        if (cnt == 0) ustart.push_back((int32_t)i);
+        cost += e1[order[i]] - e0[order[i]] + BC_ITEM_OVERHEAD;
+        if (++cnt == 32 || cost >= BC_UNIT_COST) cost = cnt = 0;
+    }
+    ustart.push_back((int32_t)order.size());
+    up(order, cm.order);
+    up(ustart, cm.ustart);
+    cm.nunits = (int32_t)ustart.size() - 1;
     up(v, cm.v);
     up(e0, cm.e0);
     up(e1, cm.e1);
@@ -701,6 +790,9 @@ static DevChunks dev_chunks(const ChunkMap &c)
     d.e1 = c.e1;
     d.slot = c.slot;
     d.nchunks = c.nchunks;
+    d.order = c.order;
+    d.ustart = c.ustart;
+    d.nunits = c.nunits;
     d.mv = c.mv;
     d.mfirst = c.mfirst;
     d.mcount = c.mcount;

@@ -100,6 +100,9 @@ struct ChunkMap {
     int32_t *mcount = nullptr; // [nmulti] their number of items
     int32_t nmulti = 0;
     int32_t nslots = 0;        // items of split vertices
+    int32_t *order = nullptr;  // [nchunks] items by descending edge count
+    int32_t *ustart = nullptr; // [nunits+1] work units: runs of order[] of <= 32 items and about 512 edges
+    int32_t nunits = 0;
     bool built = false;
 };
 
