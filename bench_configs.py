@@ -136,6 +136,12 @@ def wl_c3(args):
         t = _median_kernel_ms(g, lambda: g.bc(s, bc, batch=batch), reps=3)
         res[f"bc_batch{batch}_kernel_ms"] = t
         res[f"bc_batch{batch}_gteps"] = edges / t / 1e6
+    # per-phase timeline of one 256-source pass (the library's profiling hook)
+    g.bc(s[:256], bc, batch=256)
+    torch.cuda.synchronize()
+    tl = g.level_profile()
+    res["phases_256src_us"] = [[e["kind"], e["level"], round(1e3 * (e["t_ms"] - tl[i - 1]["t_ms"]), 1)]
+                               for i, e in enumerate(tl) if i > 0]
     ks = 1024
     s1 = s[:ks]
     sig = torch.empty((ks, hg.n), dtype=torch.int64, device="cuda")

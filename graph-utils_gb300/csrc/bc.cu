@@ -51,6 +51,42 @@ struct __align__(128) BcCtl {
 };
 static_assert(sizeof(BcCtl) <= 512, "control block");
 
+// Per-phase timeline (profiling hook, same record as the batched BFS engine's):
+// every CTA's thread 0 stamps its arrival at the grid barrier that ends phase
+// i (atomicMax of the global timer: the slowest CTA), and CTA 0 records what
+// the phase was.  Kinds, as gu_graph_level_profile reports them:
+enum : int {
+    BC_PHASE_INIT = 4,       // batch set-up and seeds
+    BC_PHASE_FORWARD = 8,    // forward level j: new bits and sigma
+    BC_PHASE_BACKWARD = 9,   // backward level l: successor sums, delta, beta
+    BC_PHASE_COMBINE = 10,   // backward level l: split vertices' partial sums
+    BC_PHASE_FINISH = 11,    // bc accumulation and per-source rows of the batch
+    BC_PHASE_CLEAR = 12,     // forward level j: clear its level bitmap
+};
+constexpr size_t BC_TIMELINE_OFF = 512;
+constexpr int BC_TIMELINE_MAX = 1024;
+struct BcEvent {
+    u64 t_last_ns;
+    int32_t batch, level;
+    int32_t kind, pad;
+    long long pad2;
+};
+constexpr size_t BC_TIMELINE_BYTES = sizeof(BcEvent) * BC_TIMELINE_MAX + 16;
+static_assert(BC_TIMELINE_OFF + BC_TIMELINE_BYTES <= WS_CONTROL_BYTES, "timeline must fit the control region");
+
+__device__ __forceinline__ void record_bc_event(BcCtl *ctl, int i, bool describe, int batch, int level, int kind)
+{
+    BcEvent *ev = reinterpret_cast<BcEvent *>(reinterpret_cast<char *>(ctl) + BC_TIMELINE_OFF);
+    if (i >= BC_TIMELINE_MAX) return;
+    atomicMax(&ev[i].t_last_ns, global_timer_ns());
+    if (describe) {
+        ev[i].batch = batch;
+        ev[i].level = level;
+        ev[i].kind = kind;
+        *reinterpret_cast<int *>(ev + BC_TIMELINE_MAX) = i + 1;
+    }
+}
+
 enum : int { DEV_ERR_LEVELS = 3 };
 
 struct DevChunks {
@@ -598,7 +634,11 @@ __global__ void __launch_bounds__(BC_THREADS, 2) bc_grid_kernel(BcArgs a, int do
     __shared__ BcCtl s_ctl;  // control block as read by thread 0 after each barrier
     unsigned epoch = 0;
     BcCtl *ctl = a.ctl;
-    auto barrier = [&]() {
+    int phase = 0;  // timeline entry of the current phase
+    int batch = 0;
+    auto barrier = [&](int kind, int level) {
+        if (threadIdx.x == 0) record_bc_event(ctl, phase, blockIdx.x == 0, batch, level, kind);
+        ++phase;
         return grid_barrier(&ctl->bar, &ctl->err, epoch, reinterpret_cast<const u64 *>(ctl), reinterpret_cast<u64 *>(&s_ctl),
                             (int)(sizeof(BcCtl) / sizeof(u64)));
     };
@@ -609,6 +649,7 @@ __global__ void __launch_bounds__(BC_THREADS, 2) bc_grid_kernel(BcArgs a, int do
     for (long long i = rank; i < (long long)a.nreq * a.n; i += size) a.bc[i] = 0.0;
     if (threadIdx.x < 16) s_act[threadIdx.x] = 0;
     for (int b = 0; b < nbatch; ++b) {
+        batch = b;
         const int row0 = b * B;
         const int nb = min(B, a.k - row0);
         for (size_t i = (size_t)rank; i < nW; i += (size_t)size) {
@@ -623,7 +664,7 @@ __global__ void __launch_bounds__(BC_THREADS, 2) bc_grid_kernel(BcArgs a, int do
             ctl->found[0] = ctl->found[1] = 0;
             for (int q = 0; q < 16; ++q) ctl->active[0][q] = ctl->active[1][q] = 0;
         }
-        if (!barrier()) return;
+        if (!barrier(BC_PHASE_INIT, 0)) return;
         if (rank < nb) {
             const int32_t s = __ldg(a.sources + row0 + rank);
             const int q = (int)rank >> 6;
@@ -632,13 +673,13 @@ __global__ void __launch_bounds__(BC_THREADS, 2) bc_grid_kernel(BcArgs a, int do
             a.sigma[(size_t)s * B + rank] = 1ull;
             atomicOr(&ctl->active[0][q], bit);
         }
-        if (!barrier()) return;
+        if (!barrier(BC_PHASE_INIT, 0)) return;
         // forward levels
         int L = 0;
         for (int j = 1;; ++j) {
             if (j > a.max_lvl) {
                 if (rank == 0) atomicCAS(&ctl->err, 0, (int)DEV_ERR_LEVELS);
-                barrier();
+                barrier(BC_PHASE_INIT, j);
                 return;
             }
             for (size_t i = (size_t)rank; i < nW; i += (size_t)size) a.lvl[(size_t)j * nW + i] = 0;
@@ -647,7 +688,7 @@ __global__ void __launch_bounds__(BC_THREADS, 2) bc_grid_kernel(BcArgs a, int do
                 ctl->found[j & 1] = 0;
                 for (int q = 0; q < 16; ++q) ctl->active[j & 1][q] = 0;
             }
-            if (!barrier()) return;
+            if (!barrier(BC_PHASE_CLEAR, j)) return;
             // work units of all word groups, taken dynamically (unit x = group x / nunits)
             const long long nfw = (long long)(W / NQ) * a.cin.nunits;
             for (;;) {
@@ -665,7 +706,7 @@ __global__ void __launch_bounds__(BC_THREADS, 2) bc_grid_kernel(BcArgs a, int do
                 atomicOr(&ctl->found[j & 1], 1);
                 s_act[threadIdx.x] = 0;
             }
-            if (!barrier()) return;
+            if (!barrier(BC_PHASE_FORWARD, j)) return;
             if (s_ctl.found[j & 1] == 0) {
                 L = j - 1;  // this pass also folded lvl[L] into seen
                 break;
@@ -684,12 +725,12 @@ __global__ void __launch_bounds__(BC_THREADS, 2) bc_grid_kernel(BcArgs a, int do
                     bc_backward_unit<NQ>(a, s_stage[warp_in_block()], s_sum[warp_in_block()], l, L,
                                          (int)(x / a.cout.nunits) * NQ, (int)(x % a.cout.nunits));
                 }
-                if (!barrier()) return;
+                if (!barrier(BC_PHASE_BACKWARD, l)) return;
                 if (a.cout.nmulti) {
                     for (int q0 = 0; q0 < W; q0 += NQ)
                         for (long long i = gwarp(); i < a.cout.nmulti; i += nwarps())
                             bc_combine_item<NQ>(a, s_stage[warp_in_block()], s_sum[warp_in_block()], l, q0, (int)i);
-                    if (!barrier()) return;
+                    if (!barrier(BC_PHASE_COMBINE, l)) return;
                 }
             }
             for (long long w = gwarp(); w < a.n; w += nwarps()) bc_accumulate_item(a, (int32_t)w, row0, nb);
@@ -698,7 +739,7 @@ __global__ void __launch_bounds__(BC_THREADS, 2) bc_grid_kernel(BcArgs a, int do
             for (int q = 0; q < W; ++q)
                 for (long long w = gwarp(); w < a.n; w += nwarps()) bc_rows_item(a, (int32_t)w, q, row0, nb, L);
         }
-        if (!barrier()) return;
+        if (!barrier(BC_PHASE_FINISH, 0)) return;
     }
 }
 
@@ -879,7 +920,7 @@ void launch_bc(DeviceGraph &g, const int32_t *sources, int32_t k, const BcOption
     a.sigma_rows = reinterpret_cast<u64 *>(sigma_rows);
     a.delta_rows = delta_rows;
     a.ld = ld;
-    GU_CUDA_CHECK(cudaMemsetAsync(a.ctl, 0, sizeof(BcCtl), stream));
+    GU_CUDA_CHECK(cudaMemsetAsync(a.ctl, 0, BC_TIMELINE_OFF + BC_TIMELINE_BYTES, stream));
     const void *kern = W == 1 ? (const void *)bc_grid_kernel<1>
                        : W == 2 ? (const void *)bc_grid_kernel<2> : (const void *)bc_grid_kernel<4>;
     const int ki = W == 1 ? 0 : W == 2 ? 1 : 2;
@@ -898,6 +939,7 @@ void launch_bc(DeviceGraph &g, const int32_t *sources, int32_t k, const BcOption
     dim3 grid(nblocks), block(BC_THREADS);
     int do_backward = backward ? 1 : 0;
     void *params[] = {&a, &do_backward};
+    if (&wsp == &g.ws) g.timeline = 1;
     if (opt.timed) g.mark_start(stream);
     GU_CUDA_CHECK(cudaLaunchCooperativeKernel(kern, grid, block, params, dyn, stream));
     if (opt.timed) g.mark_stop(stream);
@@ -908,6 +950,27 @@ int bc_ws_error(const Workspace &ws)
     BcCtl c;
     GU_CUDA_CHECK(cudaMemcpy(&c, ws.ptr, sizeof(BcCtl), cudaMemcpyDeviceToHost));
     return c.err;
+}
+
+// Copies the per-phase timeline of the last BC launch on the graph's workspace
+// (after a stream sync); frontier sizes are not recorded (reported as 0).
+int bc_read_timeline(DeviceGraph &g, int max_entries, int32_t *batch, int32_t *level, int32_t *kind,
+                     int64_t *frontier_vertices, int64_t *frontier_edges, double *t_ms)
+{
+    std::vector<char> buf(BC_TIMELINE_BYTES);
+    GU_CUDA_CHECK(cudaMemcpy(buf.data(), (char *)g.ws.ptr + BC_TIMELINE_OFF, BC_TIMELINE_BYTES, cudaMemcpyDeviceToHost));
+    const BcEvent *ev = reinterpret_cast<const BcEvent *>(buf.data());
+    const int cnt = *reinterpret_cast<const int *>(ev + BC_TIMELINE_MAX);
+    const int nout = cnt < max_entries ? cnt : max_entries;
+    for (int i = 0; i < nout; ++i) {
+        if (batch) batch[i] = ev[i].batch;
+        if (level) level[i] = ev[i].level;
+        if (kind) kind[i] = ev[i].kind;
+        if (frontier_vertices) frontier_vertices[i] = 0;
+        if (frontier_edges) frontier_edges[i] = 0;
+        if (t_ms) t_ms[i] = (double)(ev[i].t_last_ns - ev[0].t_last_ns) * 1e-6;
+    }
+    return nout;
 }
 
 void bc_read_status(DeviceGraph &g, int *dev_err, int *max_level)

@@ -345,7 +345,9 @@ gu_status gu_graph_level_profile(gu_graph g, int max_entries, int32_t *batch, in
         DeviceScope ds(dg.device);
         if (!dg.timed || !dg.ws.ptr) throw gu_error(GU_ERR_INVALID_ARGUMENT, "no launch recorded on this graph yet");
         GU_CUDA_CHECK(cudaEventSynchronize(dg.ev_stop));
-        const int c = msbfs_read_timeline(dg, max_entries, batch, level, kind, frontier_vertices, frontier_edges, t_ms);
+        const int c = dg.timeline == 1
+                          ? bc_read_timeline(dg, max_entries, batch, level, kind, frontier_vertices, frontier_edges, t_ms)
+                          : msbfs_read_timeline(dg, max_entries, batch, level, kind, frontier_vertices, frontier_edges, t_ms);
         if (count) *count = c;
     });
 }

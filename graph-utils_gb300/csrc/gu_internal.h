@@ -138,6 +138,7 @@ struct DeviceGraph {
     cudaEvent_t ev_start = nullptr, ev_stop = nullptr;
     cudaStream_t copy_st = nullptr;  // host-form calls copy rows out on it while later sources run
     bool timed = false;
+    int timeline = 0;  // engine whose phase timeline the workspace holds: 0 batched BFS, 1 BC
     void mark_start(cudaStream_t s);
     void mark_stop(cudaStream_t s);
     ~DeviceGraph();
@@ -189,6 +190,8 @@ void launch_bc(DeviceGraph &g, const int32_t *sources, int32_t k, const BcOption
 size_t bc_workspace_bytes(const DeviceGraph &g, int32_t k, int batch, bool backward);
 size_t msbfs_workspace_bytes(const DeviceGraph &g, int32_t k);
 void bc_read_status(DeviceGraph &g, int *dev_err, int *max_level);
+int bc_read_timeline(DeviceGraph &g, int max_entries, int32_t *batch, int32_t *level, int32_t *kind,
+                     int64_t *frontier_vertices, int64_t *frontier_edges, double *t_ms);
 size_t lbs_scratch_bytes(int32_t N);
 void launch_lbs(const int32_t *counts, int32_t N, int32_t *scanned, int32_t *result, int64_t result_capacity,
                 int32_t *total_dev, int64_t *total_host, void *scratch_ptr, size_t scratch_bytes, cudaStream_t st);

@@ -1756,6 +1756,7 @@ void launch_msbfs(DeviceGraph &g, const int32_t *sources, int32_t k, int32_t *di
     GU_CUDA_CHECK(cudaMemsetAsync(a.ctl, 0, CTL_REGION, stream));
     const int sms = g.sm_count;
     const int mb = opt.max_blocks;
+    g.timeline = 0;
     if (opt.timed) g.mark_start(stream);
     switch (opt.variant) {
     case GU_BFS_AUTO: launch_words<GU_BFS_AUTO>(a, W, sms, stream, mb); break;

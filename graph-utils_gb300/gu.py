@@ -260,7 +260,7 @@ class Graph:
         return t.value, td.value, bu.value, ml.value
 
     def level_profile(self, max_entries=1024):
-        """Per-phase timeline of the last batched search: list of dicts."""
+        """Per-phase timeline of the last batched search or BC / sigma pass: list of dicts."""
         b, lv, kd = (np.zeros(max_entries, np.int32) for _ in range(3))
         fv, fe = np.zeros(max_entries, np.int64), np.zeros(max_entries, np.int64)
         t = np.zeros(max_entries, np.float64)
@@ -268,7 +268,8 @@ class Graph:
         check(lib().gu_graph_level_profile(self._h, max_entries, _ptr(b), _ptr(lv), _ptr(kd),
                                            fv.ctypes.data_as(_i64p), fe.ctypes.data_as(_i64p),
                                            t.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), ctypes.byref(cnt)))
-        kinds = {0: "top-down", 1: "bottom-up", 2: "rows", 4: "init", 5: "bu-final", 6: "bu-light", 7: "bu-scan"}
+        kinds = {0: "top-down", 1: "bottom-up", 2: "rows", 4: "init", 5: "bu-final", 6: "bu-light", 7: "bu-scan",
+                 8: "bc-forward", 9: "bc-backward", 10: "bc-combine", 11: "bc-finish", 12: "bc-clear"}
         return [dict(batch=int(b[i]), level=int(lv[i]), kind=kinds.get(int(kd[i]), "?"),
                      frontier_vertices=int(fv[i]), frontier_edges=int(fe[i]), t_ms=float(t[i]))
                 for i in range(cnt.value)]

@@ -155,14 +155,17 @@ gu_status gu_graph_arrays(gu_graph g, const int32_t **R_dev, const int32_t **C_d
  * (e.g. shuffle_based.cu:42-44). */
 gu_status gu_graph_last_launch(gu_graph g, double *kernel_seconds, int *td_levels, int *bu_levels, int *max_level);
 
-/* Profiling hook: the per-phase timeline of the last batched search on g (up to
- * max_entries phases).  Entry i: batch, level j of the phase, kind (0 top-down,
- * 1 bottom-up, 2 distance write-out, 4 batch initialised; inside a bottom-up
- * phase 5 marks the end of the finalise step, 6 the end of the light class's
- * scan as seen by warp 0 of each CTA, 7 the end of the scans before the rare
- * sources' top-down expansion), vertices and out-edges of the frontier it
- * expanded, and the time the slowest CTA finished it, in ms from the end of
- * entry 0.  No reference counterpart (the reference times whole calls only). */
+/* Profiling hook: the per-phase timeline of the last batched search or BC /
+ * sigma pass on g (up to max_entries phases).  Entry i: batch, level j of the
+ * phase, kind (0 top-down, 1 bottom-up, 2 distance write-out, 4 batch
+ * initialised; inside a bottom-up phase 5 marks the end of the finalise step, 6
+ * the end of the light class's scan as seen by warp 0 of each CTA, 7 the end of
+ * the scans before the rare sources' top-down expansion; BC and sigma passes: 8
+ * forward level, 9 backward level, 10 split vertices' sums of a backward level,
+ * 11 bc accumulation and per-source rows, 12 a forward level's bitmap cleared),
+ * vertices and out-edges of the frontier it expanded (batched search only; 0 for
+ * BC), and the time the slowest CTA finished it, in ms from the end of entry 0.
+ * No reference counterpart (the reference times whole calls only). */
 gu_status gu_graph_level_profile(gu_graph g, int max_entries, int32_t *batch, int32_t *level, int32_t *kind,
                                  int64_t *frontier_vertices, int64_t *frontier_edges, double *t_ms, int *count);
 

@@ -132,3 +132,29 @@ def test_diameter(golden_graphs, engine, monkeypatch):
     g = gu.Graph(hg)
     srcs = gu.sources(hg.n, 100, seed=2)
     assert g.diameter(dev(srcs)) == oracle.diameter(hg.R, hg.C, hg.n, srcs, nthreads=8)
+
+
+def test_phase_timeline():
+    """The profiling hook's BC timeline: per batch, forward levels 1..L+1 then
+    backward levels L..1, each ending after the one before."""
+    hg = gu.HostGraph.rmat(12, 8, seed=5)
+    g = gu.Graph(hg)
+    srcs = gu.sources(hg.n, 192, seed=3)
+    run_bc(g, srcs, batch=128)
+    tl = g.level_profile()
+    assert tl and all(e["kind"] in ("init", "bc-forward", "bc-backward", "bc-combine", "bc-finish", "bc-clear")
+                      for e in tl)
+    t = [e["t_ms"] for e in tl]
+    assert t == sorted(t)
+    for b in (0, 1):
+        fw = [e["level"] for e in tl if e["batch"] == b and e["kind"] == "bc-forward"]
+        bw = [e["level"] for e in tl if e["batch"] == b and e["kind"] == "bc-backward"]
+        assert fw == list(range(1, len(fw) + 1)) and bw == list(range(len(fw) - 1, 0, -1))
+    assert sum(e["kind"] == "bc-finish" for e in tl) == 2
+    # a BFS afterwards replaces it with the batched search's own timeline
+    s = dev(np.asarray(srcs, np.int32))
+    d = torch.empty((len(srcs), hg.n), dtype=torch.int32, device="cuda")
+    g.bfs(s, d, variant="warp")  # a batched-engine variant (AUTO picks the per-source engine here)
+    torch.cuda.synchronize()
+    assert all(e["kind"] in ("init", "top-down", "bottom-up", "rows", "bu-final", "bu-light", "bu-scan")
+               for e in g.level_profile())
