@@ -118,6 +118,35 @@ def wl_c1(args):
            "note": "tiny graphs: launch- and barrier-latency bound, GTEPS is not the point"})
 
 
+def _hbm_peak():
+    """Measured HBM copy bandwidth (GB/s) of this machine's GPUs, or the fallback figure."""
+    try:
+        with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"])
+    except (OSError, KeyError, ValueError):
+        return 6800.0
+
+
+def wl_c3_pass(args):
+    """Profiling case: one Brandes pass over 256 of the C3 sources (batch 256), three
+    times, on the C3 graph; prints the kernel times and the pass's phase timeline."""
+    import gu
+    torch = _torch()
+    hg = gu.HostGraph.rmat(18, 16, 0.57, 0.19, 0.19, seed=1, permute=True)
+    g = gu.Graph(hg)
+    s = torch.as_tensor(gu.sources(hg.n, 8192, seed=2)[:256], device="cuda")
+    bc = torch.empty(hg.n, dtype=torch.float64, device="cuda")
+    times = []
+    for _ in range(3):
+        g.bc(s, bc, batch=256)
+        times.append(g.last_launch()[0] * 1e3)
+    tl = g.level_profile()
+    _emit({"workload": "c3_pass_rmat18_256src_bc", "metric": "kernel time of one 256-source BC pass",
+           "unit": "ms", "kernel_ms": times,
+           "phases_us": [[e["kind"], e["level"], round(1e3 * (e["t_ms"] - tl[i - 1]["t_ms"]), 1)]
+                         for i, e in enumerate(tl) if i > 0]})
+
+
 def wl_c3(args):
     import gu
     import oracle
@@ -148,7 +177,8 @@ def wl_c3(args):
     dst = torch.empty((ks, hg.n), dtype=torch.int32, device="cuda")
     res["sigma_1024src_kernel_ms"] = _median_kernel_ms(g, lambda: g.sigma(s1, sig, dist_dev=dst), reps=3)
     del sig, dst
-    # BC algorithmic bytes, 28n + 32 V_s + 40 E_s per source (SURVEY 8(d) model)
+    # BC algorithmic bytes per source: 28n + 32 V_s + 40 E_s (dist, sigma, delta rows and bc; forward
+    # and backward reads of the adjacency, levels, sigma and delta per reached vertex and edge)
     alg = len(srcs) * 28.0 * hg.n + 32.0 * V + 40.0 * E
     best = min(res[f"bc_batch{b}_kernel_ms"] for b in (64, 128, 256, 512, 1024))
     sub1, subN = srcs[:4], srcs[:4 * cores]
@@ -158,7 +188,10 @@ def wl_c3(args):
            "unit": "GTEPS", "value": edges / best / 1e6, "n": hg.n, "m_csr": hg.m, "sources": len(srcs),
            "edges": edges, "results": res,
            "roofline": {"bound": "hbm", "alg_bytes": alg, "achieved_gbs": alg / best / 1e6,
-                        "model": "per-source 28n + 32 V_s + 40 E_s (effective: a pass shares reads)"},
+                        "peak_gbs": _hbm_peak(), "effective_frac": alg / best / 1e6 / _hbm_peak(),
+                        "model": "per-source 28n + 32 V_s + 40 E_s (effective: a pass shares reads)",
+                        "physical": "ncu of one 256-source pass: 9.87 GB DRAM in 6.32 ms, 1.56 TB/s, 0.23 of "
+                                    "the measured HBM peak (profiles/bc_grid_kernel_rmat18.md)"},
            "cpu_bc_f64": {"per_source_ms_1thread": c1 * 1e3 / len(sub1),
                           f"per_source_ms_{cores}threads": cN * 1e3 / len(subN),
                           "extrapolated_8192_s_all_threads": cN / len(subN) * 8192,
@@ -226,7 +259,7 @@ def wl_c5(args):
     cpu_ms = []
     import queue
     import threading
-    for rate in (100.0, 400.0, 1600.0, 3200.0):
+    for rate in (100.0, 400.0, 1600.0, 3200.0, 6400.0):
         srv = gu.Server(hbm_budget_bytes=64 << 30, slots=4, max_batch=1024)
         plan, t = [], 0.0
         dur = 2.0
@@ -383,4 +416,4 @@ def wl_dag(args):
 
 
 def run(workload, args):
-    {"c1": wl_c1, "c3": wl_c3, "c4": wl_c4, "c5": wl_c5, "io": wl_io, "dag": wl_dag}[workload](args)
+    {"c1": wl_c1, "c3": wl_c3, "c3-pass": wl_c3_pass, "c4": wl_c4, "c5": wl_c5, "io": wl_io, "dag": wl_dag}[workload](args)

@@ -30,6 +30,7 @@
 #include <memory>
 #include <thread>
 #include <unordered_map>
+#include <unistd.h>
 
 namespace gu {
 
@@ -82,6 +83,13 @@ struct Slot {
     char *dres = nullptr;  // device results of the running batch, request after request
     bool copying = false;  // kernels done, results being copied out by the copier thread
     cudaError_t done_status = cudaSuccess;
+    int touch_pending = 0;  // page-touch jobs of the batch's host buffers not yet done (tmu_)
+};
+
+struct TouchJob {
+    char *p;
+    size_t bytes;
+    Slot *slot;
 };
 
 class Server {
@@ -97,6 +105,11 @@ public:
             GU_CUDA_CHECK(cudaStreamCreateWithFlags(&s.st, cudaStreamNonBlocking));
             GU_CUDA_CHECK(cudaEventCreateWithFlags(&s.ev, cudaEventDisableTiming));
         }
+        page_ = (size_t)sysconf(_SC_PAGESIZE);
+        if (page_ < 4096) page_ = 4096;
+        const unsigned hw = std::thread::hardware_concurrency();
+        const int nt = (int)std::max(1u, std::min(8u, hw / 2));
+        for (int i = 0; i < nt; ++i) touchers_.emplace_back([this] { touch_loop(); });
         worker_ = std::thread([this] { loop(); });
         copier_ = std::thread([this] { copy_loop(); });
     }
@@ -115,6 +128,12 @@ public:
         }
         cv_copy_.notify_all();
         if (copier_.joinable()) copier_.join();
+        {
+            std::lock_guard<std::mutex> lk(tmu_);
+            stop_touch_ = true;
+        }
+        cv_touch_.notify_all();
+        for (std::thread &t : touchers_) t.join();
         cudaSetDevice(device_);
         for (Slot &s : slots_) {
             if (s.st) cudaStreamSynchronize(s.st);
@@ -320,6 +339,21 @@ private:
         }
         s.dres = dres;
         GU_CUDA_CHECK(cudaEventRecord(s.ev, s.st));
+        {
+            // touch the requests' host buffers while the batch runs, in pieces of
+            // at least 4 MiB so every helper gets work on a large result
+            std::lock_guard<std::mutex> tlk(tmu_);
+            const size_t piece = std::max<size_t>((size_t)4 << 20, out_bytes / touchers_.size() + 1);
+            for (SRequest *r : batch) {
+                char *p = static_cast<char *>(r->out);
+                const size_t b = row_bytes(r);
+                for (size_t off = 0; off < b; off += piece) {
+                    touch_q_.push_back({p + off, std::min(piece, b - off), &s});
+                    ++s.touch_pending;
+                }
+            }
+        }
+        cv_touch_.notify_all();
         s.busy = true;
         s.kind = kind;
         s.g = &g;
@@ -369,6 +403,10 @@ private:
                     err = "device reported error code " + std::to_string(e);
                 }
             }
+            {
+                std::unique_lock<std::mutex> tlk(tmu_);
+                cv_touched_.wait(tlk, [&] { return s.touch_pending == 0; });
+            }
             if (st == GU_OK) {
                 size_t off = 0;
                 cudaError_t ce = cudaSuccess;
@@ -390,6 +428,25 @@ private:
             s.busy = false;
             cv_done_.notify_all();
             cv_work_.notify_all();
+        }
+    }
+
+    // Helper thread: writes one byte of every page of a job's range (inside the
+    // request's own output buffer, which the result copy overwrites later).
+    void touch_loop()
+    {
+        std::unique_lock<std::mutex> lk(tmu_);
+        while (true) {
+            cv_touch_.wait(lk, [&] { return !touch_q_.empty() || stop_touch_; });
+            if (touch_q_.empty()) return;
+            const TouchJob j = touch_q_.front();
+            touch_q_.pop_front();
+            lk.unlock();
+            volatile char *p = j.p;
+            for (size_t off = 0; off < j.bytes; off += page_) p[off] = 0;
+            if (j.bytes) p[j.bytes - 1] = 0;
+            lk.lock();
+            if (--j.slot->touch_pending == 0) cv_touched_.notify_all();
         }
     }
 
@@ -430,6 +487,13 @@ private:
     std::condition_variable cv_copy_;
     std::deque<Slot *> done_q_;
     bool stop_copier_ = false;
+    // page touching of the running batches' host buffers
+    size_t page_ = 4096;
+    std::vector<std::thread> touchers_;
+    std::mutex tmu_;
+    std::condition_variable cv_touch_, cv_touched_;
+    std::deque<TouchJob> touch_q_;
+    bool stop_touch_ = false;
 };
 
 Server *server_create(size_t budget, int nslots, int max_batch) { return new Server(budget, nslots, max_batch); }
