@@ -119,6 +119,8 @@ struct DeviceGraph {
     int32_t *RT = nullptr, *CT = nullptr;
     int32_t *F = nullptr;
     int32_t max_degree = 0;
+    int32_t *ell = nullptr;  // low-degree graphs: neighbours padded to ell_width per vertex (-1), built on first use
+    int ell_width = 0;
     // bottom-up degree classes by in-degree, each ascending: light (1 ..
     // BU_LIGHT_DEGREE), mid (.. BU_MID_DEGREE), wide (.. BU_HEAVY_DEGREE),
     // heavy (above)

@@ -17,9 +17,18 @@
 // engine.  Rows mode claims vertices in the distance row itself; the counting
 // modes (diameter, reachability) claim them in a per-CTA visited bitmap and
 // write no rows.
+//
+// The adjacency is read from a padded copy (ELL: the neighbours of v in CSR
+// order at v * width, width 4, 8 or 16, padded with -1), built on the graph's
+// first per-source search: one 16-byte load brings a grid vertex's whole list,
+// where the CSR form needs the offsets first and then a second, dependent load.
+// With a few hundred sources' frontiers spread over the graph the adjacency does
+// not stay in L2, so the halved sector count matters as much as the shorter
+// chain.
 #include "device_utils.cuh"
 #include "gu_internal.h"
 
+#include <algorithm>
 #include <climits>
 #include <cstdlib>
 
@@ -32,8 +41,7 @@ constexpr int PLAIN_MAX_VERTICES = 4096;  // ... and the one-CTA-per-source form
 constexpr size_t LOCAL_SMEM = 2 * LOCAL_QCAP * sizeof(int32_t);
 
 struct LocalArgs {
-    const int32_t *__restrict__ R;
-    const int32_t *__restrict__ C;
+    const int4 *__restrict__ ell;  // [n][width / 4]
     int32_t n;
     const int32_t *sources;
     int32_t k;
@@ -47,7 +55,18 @@ struct LocalArgs {
     int qcap;                   // vertices per shared level queue: min(n, LOCAL_QCAP)
 };
 
-template <bool ROWS>
+__global__ void build_ell_kernel(const int32_t *__restrict__ R, const int32_t *__restrict__ C, int32_t n, int width,
+                                 int32_t *__restrict__ ell)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < (int64_t)n * width;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t v = (int32_t)(i / width), t = (int32_t)(i % width);
+        const int32_t e = __ldg(R + v) + t;
+        ell[i] = e < __ldg(R + v + 1) ? __ldg(C + e) : -1;
+    }
+}
+
+template <bool ROWS, int WIDTH>
 __global__ void __launch_bounds__(LOCAL_THREADS, 2) local_bfs_kernel(LocalArgs a)
 {
     extern __shared__ int32_t sq[];  // [2][qcap]
@@ -83,13 +102,13 @@ __global__ void __launch_bounds__(LOCAL_THREADS, 2) local_bfs_kernel(LocalArgs a
             int32_t *Q2 = sq + (cur ^ 1) * a.qcap;
             int *nlen = &s_len[cur ^ 1];
             for (int i = threadIdx.x; i < qlen; i += blockDim.x) {
-                const int32_t v = Q[i];
-                const int32_t e1 = __ldg(a.R + v + 1);
-                for (int32_t e = __ldg(a.R + v); e < e1; e += 4) {
-                    int32_t w[4];
-                    bool ok[4];
+                const int4 *row = a.ell + (size_t)Q[i] * (WIDTH / 4);
 #pragma unroll
-                    for (int t = 0; t < 4; ++t) w[t] = e + t < e1 ? __ldg(a.C + e + t) : -1;
+                for (int c = 0; c < WIDTH / 4; ++c) {
+                    const int4 q4 = __ldg(row + c);
+                    const int32_t w[4] = {q4.x, q4.y, q4.z, q4.w};
+                    if (w[0] < 0) break;  // padding: the list ended
+                    bool ok[4];
 #pragma unroll
                     for (int t = 0; t < 4; ++t) {  // four claims in flight
                         if (w[t] < 0) {
@@ -155,13 +174,30 @@ AutoEngine auto_engine(const DeviceGraph &g, bool rows)
 bool launch_local_bfs(DeviceGraph &g, const int32_t *sources, int32_t k, int32_t *dist, int64_t ld,
                       unsigned long long *reach, int *max_level_host, cudaStream_t stream)
 {
-    static bool attr_set[2] = {false, false};
+    if (!g.ell) {  // the padded adjacency, once per graph
+        const int width = g.max_degree <= 4 ? 4 : g.max_degree <= 8 ? 8 : 16;
+        if (g.max_degree > 16) throw gu_error(GU_ERR_INTERNAL, "per-source engine on a graph of out-degree > 16");
+        const size_t bytes = (size_t)(g.n > 0 ? g.n : 1) * width * sizeof(int32_t);
+        GU_CUDA_CHECK(cudaMalloc(&g.ell, bytes));
+        g.extra_allocs.push_back(g.ell);
+        g.bytes += bytes;
+        g.ell_width = width;
+        const int64_t total = (int64_t)g.n * width;
+        const int blocks = (int)std::min<int64_t>((total + 255) / 256, (int64_t)g.sm_count * 8);
+        if (total > 0) build_ell_kernel<<<blocks > 0 ? blocks : 1, 256, 0, stream>>>(g.R, g.C, g.n, width, g.ell);
+        GU_CUDA_CHECK(cudaGetLastError());
+    }
+    static bool attr_set[2][3] = {{false, false, false}, {false, false, false}};
     const bool rows = dist != nullptr;
-    auto kern = rows ? local_bfs_kernel<true> : local_bfs_kernel<false>;
-    if (!attr_set[rows]) {
+    const int wi = g.ell_width == 4 ? 0 : g.ell_width == 8 ? 1 : 2;
+    void (*const kerns[2][3])(LocalArgs) = {
+        {local_bfs_kernel<false, 4>, local_bfs_kernel<false, 8>, local_bfs_kernel<false, 16>},
+        {local_bfs_kernel<true, 4>, local_bfs_kernel<true, 8>, local_bfs_kernel<true, 16>}};
+    auto kern = kerns[rows][wi];
+    if (!attr_set[rows][wi]) {
         GU_CUDA_CHECK(cudaFuncSetAttribute((const void *)kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)LOCAL_SMEM));
-        attr_set[rows] = true;
+        attr_set[rows][wi] = true;
     }
     const int qcap = g.n < LOCAL_QCAP ? (g.n > 0 ? g.n : 1) : LOCAL_QCAP;
     const size_t smem = 2 * (size_t)qcap * sizeof(int32_t);
@@ -175,8 +211,7 @@ bool launch_local_bfs(DeviceGraph &g, const int32_t *sources, int32_t k, int32_t
     char *ws = (char *)g.ws.get(need);
     GU_CUDA_CHECK(cudaMemsetAsync(ws, 0, 64, stream));
     LocalArgs a;
-    a.R = g.R;
-    a.C = g.C;
+    a.ell = reinterpret_cast<const int4 *>(g.ell);
     a.n = g.n;
     a.sources = sources;
     a.k = k;
