@@ -108,10 +108,14 @@ __global__ void __launch_bounds__(LOCAL_THREADS, 2) local_bfs_kernel(LocalArgs a
                     const int4 q4 = __ldg(row + c);
                     const int32_t w[4] = {q4.x, q4.y, q4.z, q4.w};
                     if (w[0] < 0) break;  // padding: the list ended
-                    bool ok[4];
+                    bool ok[4], seen[4];
+#pragma unroll
+                    for (int t = 0; t < 4; ++t)  // rows: plain reads first (the row lives in DRAM;
+                        // a claimed entry never reverts, so a stale read only costs the CAS)
+                        seen[t] = w[t] < 0 || (ROWS && d[w[t]] != INT_MAX);
 #pragma unroll
                     for (int t = 0; t < 4; ++t) {  // four claims in flight
-                        if (w[t] < 0) {
+                        if (seen[t]) {
                             ok[t] = false;
                         } else if (ROWS) {
                             ok[t] = atomicCAS(d + w[t], INT_MAX, level + 1) == INT_MAX;
