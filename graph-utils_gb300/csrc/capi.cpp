@@ -381,7 +381,24 @@ static void bfs_device(DeviceGraph &g, int variant, const int32_t *sources_dev, 
         GU_CUDA_CHECK(cudaGetLastError());
         return;
     }
-    if (variant == GU_BFS_AUTO) {
+    MsOptions opt;
+    opt.variant = variant;
+    if (variant == GU_BFS_AUTO && g.tune.set) {  // the measured choice (gu_graph_autotune)
+        if (g.tune.engine == GU_ENGINE_PER_SOURCE &&
+            launch_local_bfs(g, sources_dev, k, dist_dev, ld, nullptr, nullptr, stream))
+            return;
+        if (g.tune.engine == GU_ENGINE_ONE_CTA) {
+            launch_plain_bfs(g, sources_dev, k, dist_dev, ld, stream);
+            GU_CUDA_CHECK(cudaStreamSynchronize(stream));
+            GU_CUDA_CHECK(cudaGetLastError());
+            return;
+        }
+        if (g.tune.engine == GU_ENGINE_BATCHED) {
+            opt.alpha = g.tune.alpha;
+            opt.beta = g.tune.beta;
+            opt.batch_words = g.tune.words;
+        }
+    } else if (variant == GU_BFS_AUTO) {
         const AutoEngine eng = auto_engine(g, true);
         if (eng == AutoEngine::LOCAL && launch_local_bfs(g, sources_dev, k, dist_dev, ld, nullptr, nullptr, stream))
             return;
@@ -392,10 +409,131 @@ static void bfs_device(DeviceGraph &g, int variant, const int32_t *sources_dev, 
             return;
         }
     }
-    MsOptions opt;
-    opt.variant = variant;
     launch_msbfs(g, sources_dev, k, dist_dev, ld, opt, stream, nullptr);
     check_dev_status(g, stream);
+}
+
+// ---- autotuning AUTO ------------------------------------------------------------------
+static double last_kernel_seconds(DeviceGraph &g)
+{
+    GU_CUDA_CHECK(cudaEventSynchronize(g.ev_stop));
+    float ms = 0;
+    GU_CUDA_CHECK(cudaEventElapsedTime(&ms, g.ev_start, g.ev_stop));
+    return ms / 1000.0;
+}
+
+gu_status gu_graph_autotune(gu_graph g, const int32_t *sources_dev, int32_t k, gu_tuning *best, gu_tuning *trials,
+                            int max_trials, int *ntrials)
+{
+    return guarded([&] {
+        if (!g || !sources_dev || k <= 0 || max_trials < 0 || (max_trials > 0 && !trials))
+            throw gu_error(GU_ERR_INVALID_ARGUMENT, "bad arguments");
+        DeviceGraph &dg = *g->g;
+        std::lock_guard<std::mutex> lk(dg.mu);
+        DeviceScope ds(dg.device);
+        std::vector<int32_t> hs((size_t)k);
+        GU_CUDA_CHECK(cudaMemcpy(hs.data(), sources_dev, sizeof(int32_t) * k, cudaMemcpyDeviceToHost));
+        validate_sources_host(hs.data(), k, dg.n);
+        const size_t row_bytes = (size_t)k * (size_t)dg.n * sizeof(int32_t);
+        if (row_bytes > ((size_t)4 << 30)) throw gu_error(GU_ERR_INVALID_ARGUMENT, "sample too large: k x n x 4 > 4 GiB");
+        int32_t *rows = nullptr;
+        GU_CUDA_CHECK(cudaMalloc(reinterpret_cast<void **>(&rows), row_bytes ? row_bytes : 4));
+        cudaStream_t st = nullptr;
+        GU_CUDA_CHECK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+        std::vector<gu_tuning> cand;
+        auto add = [&](int engine, float alpha, float beta, int words) {
+            gu_tuning t;
+            t.engine = engine;
+            t.alpha = alpha;
+            t.beta = beta;
+            t.words = words;
+            t.seconds = 0;
+            cand.push_back(t);
+        };
+        if (dg.max_degree <= 16) add(GU_ENGINE_PER_SOURCE, 0, 0, 0);
+        if (dg.n <= 65536) add(GU_ENGINE_ONE_CTA, 0, 0, 0);
+        const int wd = msbfs_words_for(k);
+        const float grid[][2] = {{2.f, 24.f}, {1.f, 24.f}, {4.f, 24.f}, {8.f, 24.f}, {2.f, 12.f}, {2.f, 48.f}};
+        for (int w = wd; w >= 1 && w >= wd / 2; w /= 2)
+            for (const auto &ab : grid) add(GU_ENGINE_BATCHED, ab[0], ab[1], w);
+        const DeviceGraph::Tuning saved = dg.tune;
+        gu_tuning pick{};
+        pick.seconds = -1;
+        int nt = 0;
+        try {
+            for (gu_tuning &t : cand) {
+                dg.tune.set = true;
+                dg.tune.engine = t.engine;
+                dg.tune.alpha = t.alpha;
+                dg.tune.beta = t.beta;
+                dg.tune.words = t.words;
+                bool fell_back = false;
+                double best_t = 1e30;
+                for (int rep = 0; rep < 3; ++rep) {
+                    if (t.engine == GU_ENGINE_PER_SOURCE &&
+                        !launch_local_bfs(dg, sources_dev, k, rows, dg.n, nullptr, nullptr, st)) {
+                        fell_back = true;  // a frontier overflowed the shared queues: not a candidate here
+                        break;
+                    }
+                    if (t.engine != GU_ENGINE_PER_SOURCE) bfs_device(dg, GU_BFS_AUTO, sources_dev, k, rows, dg.n, st);
+                    const double sec = last_kernel_seconds(dg);
+                    if (rep > 0 || sec > 0.02) best_t = std::min(best_t, sec);  // first run warms up, unless slow
+                    if (pick.seconds >= 0 && sec > 3 * pick.seconds) {            // far behind: one run is enough
+                        best_t = std::min(best_t, sec);
+                        break;
+                    }
+                }
+                if (fell_back) continue;
+                t.seconds = best_t;
+                if (nt < max_trials) trials[nt] = t;
+                ++nt;
+                if (pick.seconds < 0 || t.seconds < pick.seconds) pick = t;
+            }
+        } catch (...) {
+            dg.tune = saved;
+            cudaStreamDestroy(st);
+            cudaFree(rows);
+            throw;
+        }
+        GU_CUDA_CHECK(cudaStreamDestroy(st));
+        GU_CUDA_CHECK(cudaFree(rows));
+        if (pick.seconds < 0) {
+            dg.tune = saved;
+            throw gu_error(GU_ERR_INTERNAL, "no candidate completed");
+        }
+        dg.tune.set = true;
+        dg.tune.engine = pick.engine;
+        dg.tune.alpha = pick.alpha;
+        dg.tune.beta = pick.beta;
+        dg.tune.words = pick.words;
+        if (best) *best = pick;
+        if (ntrials) *ntrials = std::min(nt, max_trials);
+    });
+}
+
+gu_status gu_graph_set_tuning(gu_graph g, const gu_tuning *t)
+{
+    return guarded([&] {
+        if (!g) throw gu_error(GU_ERR_INVALID_ARGUMENT, "null graph");
+        DeviceGraph &dg = *g->g;
+        std::lock_guard<std::mutex> lk(dg.mu);
+        if (!t) {
+            dg.tune = DeviceGraph::Tuning();
+            return;
+        }
+        if (t->engine < GU_ENGINE_BATCHED || t->engine > GU_ENGINE_ONE_CTA)
+            throw gu_error(GU_ERR_INVALID_ARGUMENT, "unknown engine");
+        if (t->engine == GU_ENGINE_PER_SOURCE && dg.max_degree > 16)
+            throw gu_error(GU_ERR_INVALID_ARGUMENT, "the per-source engine needs out-degree <= 16");
+        if (t->engine == GU_ENGINE_BATCHED &&
+            (!(t->alpha > 0) || !(t->beta > 0) || (t->words != 0 && t->words != 1 && t->words != 2 && t->words != 4)))
+            throw gu_error(GU_ERR_INVALID_ARGUMENT, "batched engine needs alpha, beta > 0 and words 0, 1, 2 or 4");
+        dg.tune.set = true;
+        dg.tune.engine = t->engine;
+        dg.tune.alpha = t->alpha;
+        dg.tune.beta = t->beta;
+        dg.tune.words = t->words;
+    });
 }
 
 static void check_bfs_args(gu_graph g, int variant, int32_t k, int64_t ld)

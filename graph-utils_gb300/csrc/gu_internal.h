@@ -119,6 +119,13 @@ struct DeviceGraph {
     int32_t *RT = nullptr, *CT = nullptr;
     int32_t *F = nullptr;
     int32_t max_degree = 0;
+    // AUTO's measured choice (gu_graph_autotune / gu_graph_set_tuning); unset: by shape
+    struct Tuning {
+        bool set = false;
+        int engine = 0;  // gu_engine
+        float alpha = 2.f, beta = 24.f;
+        int words = 0;
+    } tune;
     int32_t *ell = nullptr;  // low-degree graphs: neighbours padded to ell_width per vertex (-1), built on first use
     int ell_width = 0;
     // bottom-up degree classes by in-degree, each ascending: light (1 ..
@@ -149,7 +156,7 @@ struct DeviceGraph {
 // Per-call options of the batched multi-source engine.
 struct MsOptions {
     int variant = GU_BFS_AUTO;
-    int batch_words = 1;  // 64-source words per batch
+    int batch_words = 0;  // 64-source words per batch (0: by the number of sources)
     float alpha = 2.f;    // top-down -> bottom-up when frontier out-edges > m / alpha
     float beta = 24.f;    // bottom-up -> top-down when frontier vertices < n / beta
     float gamma = 4.f;    // ... or when frontier out-edges < n / gamma
@@ -182,6 +189,7 @@ void launch_plain_bfs(DeviceGraph &g, const int32_t *sources, int32_t k, int32_t
 // if a frontier overflowed its shared queues (rerun on the batched engine).
 // Reachable-set sizes of every vertex of a DAG (self excluded) and their sum.
 void dag_reach(DeviceGraph &g, int64_t *counts, int64_t *total_host, cudaStream_t st);
+int msbfs_words_for(int32_t k);  // 64-source words per batch for k sources
 enum class AutoEngine { LOCAL, PLAIN, BATCHED };
 AutoEngine auto_engine(const DeviceGraph &g, bool rows);
 bool launch_local_bfs(DeviceGraph &g, const int32_t *sources, int32_t k, int32_t *dist, int64_t ld,

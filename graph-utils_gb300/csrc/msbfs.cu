@@ -1694,7 +1694,8 @@ void launch_msbfs(DeviceGraph &g, const int32_t *sources, int32_t k, int32_t *di
 {
     (void)dev_err_out;
     if (opt.variant == GU_BFS_EDGE) ensure_coo(g, stream);
-    const int W = msbfs_words_for(k);
+    const int W = (opt.batch_words == 1 || opt.batch_words == 2 || opt.batch_words == 4) ? opt.batch_words
+                                                                                         : msbfs_words_for(k);
     const size_t n = (size_t)g.n;
     const int nplanes = msbfs_planes(n);
     auto up = [](size_t b) { return ((b + 255) / 256) * 256; };

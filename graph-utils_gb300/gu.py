@@ -29,6 +29,20 @@ _i64p = ctypes.POINTER(ctypes.c_int64)
 _vp = ctypes.c_void_p
 
 
+class GuTuning(ctypes.Structure):
+    """gu_tuning: AUTO's engine choice and its measured kernel time."""
+    _fields_ = [("engine", ctypes.c_int32), ("alpha", ctypes.c_float), ("beta", ctypes.c_float),
+                ("words", ctypes.c_int32), ("seconds", ctypes.c_double)]
+
+
+ENGINES = {0: "batched", 1: "per-source", 2: "one-cta"}
+
+
+def _tuning_dict(t):
+    return {"engine": ENGINES[t.engine], "alpha": float(t.alpha), "beta": float(t.beta), "words": int(t.words),
+            "seconds": float(t.seconds)}
+
+
 class GuError(RuntimeError):
     def __init__(self, status, msg):
         super().__init__(f"{STATUS.get(status, status)}: {msg}")
@@ -80,6 +94,9 @@ def lib():
                              ctypes.POINTER(_vp)], ctypes.c_int),
         "gu_graph_last_launch": ([_vp, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int),
                                   ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
+        "gu_graph_autotune": ([_vp, _vp, ctypes.c_int32, ctypes.POINTER(GuTuning), ctypes.POINTER(GuTuning),
+                               ctypes.c_int, ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
+        "gu_graph_set_tuning": ([_vp, ctypes.POINTER(GuTuning)], ctypes.c_int),
         "gu_graph_level_profile": ([_vp, ctypes.c_int, _i32p, _i32p, _i32p, _i64p, _i64p,
                                     ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
         "gu_bfs": ([_vp, ctypes.c_int, _vp, ctypes.c_int32, _vp, ctypes.c_int64, _vp], ctypes.c_int),
@@ -250,6 +267,25 @@ class Graph:
         b = ctypes.c_size_t()
         check(lib().gu_graph_info(self._h, None, None, None, ctypes.byref(b)))
         return b.value
+
+    def autotune(self, sources_dev, max_trials=32):
+        """Times AUTO's candidate engines and settings on a sample of sources and makes the
+        fastest this graph's AUTO choice.  Returns (best, trials) as dicts."""
+        best = GuTuning()
+        trials = (GuTuning * max_trials)()
+        nt = ctypes.c_int()
+        check(lib().gu_graph_autotune(self._h, sources_dev.data_ptr(), int(sources_dev.numel()), ctypes.byref(best),
+                                      trials, max_trials, ctypes.byref(nt)))
+        return _tuning_dict(best), [_tuning_dict(trials[i]) for i in range(nt.value)]
+
+    def set_tuning(self, tuning):
+        """Sets AUTO's choice explicitly (a dict as autotune returns; None: the built-in choice)."""
+        if tuning is None:
+            check(lib().gu_graph_set_tuning(self._h, None))
+            return
+        eng = {v: k for k, v in ENGINES.items()}[tuning["engine"]]
+        t = GuTuning(eng, float(tuning.get("alpha", 2.0)), float(tuning.get("beta", 24.0)), int(tuning.get("words", 0)), 0.0)
+        check(lib().gu_graph_set_tuning(self._h, ctypes.byref(t)))
 
     def last_launch(self):
         """(kernel seconds, top-down levels, bottom-up levels, max level) of the last launch."""

@@ -169,6 +169,39 @@ gu_status gu_graph_last_launch(gu_graph g, double *kernel_seconds, int *td_level
 gu_status gu_graph_level_profile(gu_graph g, int max_entries, int32_t *batch, int32_t *level, int32_t *kind,
                                  int64_t *frontier_vertices, int64_t *frontier_edges, double *t_ms, int *count);
 
+/* ---- autotuning AUTO --------------------------------------------------------- */
+/* AUTO's built-in choice goes by graph shape (out-degree, size) and fixed
+ * direction thresholds.  gu_graph_autotune measures instead: it runs the
+ * candidate engines and settings on a sample of sources (distance rows into a
+ * scratch buffer it allocates, k x n int32: keep the sample modest), times each
+ * by its kernel, and makes the fastest the graph's AUTO choice for later gu_bfs
+ * / gu_bfs_host calls (the server and the counting calls keep the built-in
+ * choice).  Candidates: the per-source engine (out-degree <= 16), the
+ * one-CTA-per-source form (n <= 65536), and the batched engine over a grid of
+ * direction thresholds (alpha: top-down -> bottom-up when the frontier's
+ * out-edges exceed m / alpha; beta: back when the frontier holds fewer than
+ * n / beta vertices) and source words per batch; slow candidates are cut after
+ * one run.  trials (optional, room for max_trials) receives every measured
+ * candidate in order; best receives the choice.  Distances do not depend on the
+ * choice.  No reference counterpart (its examples pick the kernel by hand). */
+typedef enum gu_engine {
+    GU_ENGINE_BATCHED = 0,    /* bit-matrix engine, 64 x words sources per batch */
+    GU_ENGINE_PER_SOURCE = 1, /* one CTA per source, shared-memory level queues */
+    GU_ENGINE_ONE_CTA = 2     /* PLAIN: one CTA per source, distance row as visited set */
+} gu_engine;
+
+typedef struct gu_tuning {
+    int32_t engine;     /* gu_engine */
+    float alpha, beta;  /* batched engine's direction thresholds */
+    int32_t words;      /* batched engine: 64-source words per batch (1, 2 or 4) */
+    double seconds;     /* measured kernel time on the sample (autotune output) */
+} gu_tuning;
+
+gu_status gu_graph_autotune(gu_graph g, const int32_t *sources_dev, int32_t k, gu_tuning *best, gu_tuning *trials,
+                            int max_trials, int *ntrials);
+/* Sets the graph's AUTO choice explicitly (t = NULL: back to the built-in choice). */
+gu_status gu_graph_set_tuning(gu_graph g, const gu_tuning *t);
+
 /* ---- multi-source BFS ------------------------------------------------------ */
 /* Row i of dist (row stride ld >= n elements) receives the distances from
  * sources[i]; GU_DIST_UNREACHABLE where unreachable.  Replaces

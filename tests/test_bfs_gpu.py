@@ -198,3 +198,28 @@ def test_rmat20_full_size_certificates():
     sample = [0, 1, 63, 64, 200, 511]
     ref, _ = oracle.bfs_multi(hg.R, hg.C, hg.n, srcs[sample], nthreads=8)
     np.testing.assert_array_equal(dist[sample].cpu().numpy(), ref)
+
+
+@pytest.mark.parametrize("shape", ["rmat", "grid"])
+def test_autotune_keeps_distances(shape):
+    """gu_graph_autotune times the candidates on a sample and makes the fastest AUTO's
+    choice; distances after tuning (and under every explicitly set choice) equal the
+    oracle's, and clearing the tuning restores the built-in choice."""
+    hg = gu.HostGraph.rmat(13, 16, seed=9) if shape == "rmat" else gu.HostGraph.grid(96, 64, 0.05, seed=4)
+    g = gu.Graph(hg)
+    srcs = gu.sources(hg.n, 96, seed=6)
+    ref, _ = oracle.bfs_multi(hg.R, hg.C, hg.n, srcs, nthreads=8)
+    best, trials = g.autotune(torch.as_tensor(srcs, device="cuda"))
+    engines = {t["engine"] for t in trials}
+    assert "batched" in engines and best in trials
+    assert ("per-source" in engines) == (shape == "grid")  # out-degree <= 16 only on the grid
+    assert best["seconds"] == min(t["seconds"] for t in trials) > 0
+    assert all(0 < t["seconds"] < 10 for t in trials)
+    np.testing.assert_array_equal(run_bfs(g, srcs, "auto")[0], ref)
+    for t in trials[:4]:
+        g.set_tuning(t)
+        np.testing.assert_array_equal(run_bfs(g, srcs, "auto")[0], ref, err_msg=str(t))
+    with pytest.raises(gu.GuError):
+        g.set_tuning({"engine": "batched", "alpha": 2.0, "beta": 24.0, "words": 3})
+    g.set_tuning(None)
+    np.testing.assert_array_equal(run_bfs(g, srcs, "auto")[0], ref)
