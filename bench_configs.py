@@ -165,6 +165,12 @@ def wl_c3(args):
         t = _median_kernel_ms(g, lambda: g.bc(s, bc, batch=batch), reps=3)
         res[f"bc_batch{batch}_kernel_ms"] = t
         res[f"bc_batch{batch}_gteps"] = edges / t / 1e6
+    # the plain form: one launch per source (32 sources, extrapolated to the 8192)
+    t1 = []
+    for i in range(32):
+        g.bc(s[i:i + 1], bc)
+        t1.append(g.last_launch()[0] * 1e3)
+    res["bc_one_source_per_launch_ms_extrapolated"] = float(np.mean(t1[1:])) * len(srcs)
     # per-phase timeline of one 256-source pass (the library's profiling hook)
     g.bc(s[:256], bc, batch=256)
     torch.cuda.synchronize()
@@ -255,6 +261,19 @@ def wl_c5(args):
         hg = gu.HostGraph.dag(n, 8 * n, seed=200 + i)
         dags.append((f"dag{n}_s{200 + i}", hg, gu.Graph(hg)))
     torch.cuda.synchronize()
+    # edges a search from s traverses on an undirected graph: its component's CSR entries
+    # (each undirected edge once per direction); GTEPS counts them once, as the other lines do
+    import scipy.sparse
+    import scipy.sparse.csgraph
+    comp_edges = {}
+    for name, hg, g in rmats:
+        A = scipy.sparse.csr_matrix((np.ones(hg.m, np.int8), hg.C, hg.R), shape=(hg.n, hg.n))
+        _, lab = scipy.sparse.csgraph.connected_components(A, directed=False)
+        per = np.bincount(lab, weights=np.diff(hg.R).astype(np.float64))
+        comp_edges[id(hg)] = per[lab] / 2.0
+
+    def req_edges(q, hg, srcs):
+        return float(comp_edges[id(hg)][srcs].sum()) if q != gu.QUERY_REACH else 0.0
     results = []
     cpu_ms = []
     import queue
@@ -310,11 +329,34 @@ def wl_c5(args):
         st = srv.stats()
         srv.close()
         lat.sort()
+        edges = sum(req_edges(q, hg, srcs) for (_, q, hg, _, srcs) in plan)
         results.append({"offered_rate_per_s": rate, "requests": len(plan), "wall_s": wall,
-                        "served_per_s": len(plan) / wall,
+                        "served_per_s": len(plan) / wall, "served_gteps_bfs_bc": edges / wall / 1e9,
                         "p50_ms": 1e3 * lat[len(lat) // 2], "p99_ms": 1e3 * lat[min(len(lat) - 1, int(0.99 * len(lat)))],
                         "server_p50_ms": st["p50_s"] * 1e3, "server_p99_ms": st["p99_s"] * 1e3,
                         "batches": st["batches"], "mean_requests_per_batch": st["mean_requests_per_batch"]})
+    # the same request stream one call per request, no batching or overlap (the plain form):
+    # host sources in, host results out, as the server's requests
+    sample = plan[:2000]
+    t0 = time.perf_counter()
+    for (_, q, hg, g, srcs) in sample:
+        if q == gu.QUERY_BFS:
+            g.bfs_host(srcs, variant="auto")
+        else:
+            sd = torch.as_tensor(srcs, device="cuda")
+            if q == gu.QUERY_BC:
+                o = torch.empty(hg.n, dtype=torch.float64, device="cuda")
+                g.bc(sd, o)
+            else:
+                o = torch.zeros(len(srcs), dtype=torch.int64, device="cuda")
+                g.reach(sd, o)
+            o.cpu()
+    torch.cuda.synchronize()
+    one_wall = time.perf_counter() - t0
+    one_edges = sum(req_edges(q, hg, srcs) for (_, q, hg, _, srcs) in sample)
+    one_by_one = {"requests": len(sample), "wall_s": one_wall, "requests_per_s": len(sample) / one_wall,
+                  "gteps_bfs_bc": one_edges / one_wall / 1e9,
+                  "note": "the first 2000 requests of the last rate's stream, one synchronous call per request"}
     # CPU: per-request oracle time on a sample of requests of each kind
     for (t_, q, hg, g, srcs) in plan[:24]:
         if q == gu.QUERY_BC:
@@ -326,7 +368,7 @@ def wl_c5(args):
             _, c = _cpu(oracle.bfs_multi, hg.R, hg.C, hg.n, srcs, nthreads=os.cpu_count() or 1)
         cpu_ms.append(c * 1e3)
     _emit({"workload": "c5_serving_mix", "metric": "request latency p50 / p99", "unit": "ms",
-           "graphs": [n for n, _, _ in rmats + dags], "results": results,
+           "graphs": [n for n, _, _ in rmats + dags], "results": results, "one_call_per_request": one_by_one,
            "mix": "60% BFS rows (1-256 sources), 20% BC (64-256 sources), 20% DAG reachable counts (1-256)",
            "cpu_per_request_ms_median": statistics.median(cpu_ms),
            "cpu_sample": "first 24 requests of the last rate, oracle on all host threads (BC extrapolated "
