@@ -137,3 +137,26 @@ def test_bad_request_rejected(graphs):
     with pytest.raises(gu.GuError):
         srv.submit(g, gu.QUERY_BFS, np.array([g.n], np.int32), np.empty((1, g.n), np.int32))
     srv.close()
+
+
+def test_page_touching_stays_inside_the_buffers(graphs):
+    """The helper threads touch each request's host buffer while its batch runs; on
+    buffers that start and end inside pages shared with other data, the bytes around
+    them must keep their values (results land exactly in the buffers)."""
+    g = graphs["rmat13"]
+    srv = gu.Server(hbm_budget_bytes=16 << 30, slots=2, max_batch=256)
+    rng = np.random.default_rng(3)
+    reqs = []
+    for i in range(6):
+        k = int(rng.integers(1, 9))
+        srcs = rng.choice(g.n, size=k, replace=False).astype(np.int32)
+        words = k * g.n
+        arena = np.full(words + 4096 + 3, -123, np.int32)  # guard words on both sides
+        off = 1 + int(rng.integers(0, 1000))                 # start inside a page
+        out = arena[off:off + words].reshape(k, g.n)
+        reqs.append((srv.submit(g, gu.QUERY_BFS, srcs, out), srcs, out, arena, off, words))
+    for rid, srcs, out, arena, off, words in reqs:
+        srv.wait(rid)
+        np.testing.assert_array_equal(out, lone_bfs(g, srcs))
+        assert (arena[:off] == -123).all() and (arena[off + words:] == -123).all()
+    srv.close()
