@@ -147,6 +147,22 @@ def wl_c3_pass(args):
                          for i, e in enumerate(tl) if i > 0]})
 
 
+def wl_c4_pass(args):
+    """Profiling case: the per-source engine in counting mode (diameter over the 256 C4
+    sources, no rows), three times, on the C4 grid."""
+    import gu
+    torch = _torch()
+    hg = gu.HostGraph.grid(2048, 2048, 0.05, seed=7)
+    g = gu.Graph(hg)
+    s = torch.as_tensor(gu.sources(hg.n, 256, seed=2), device="cuda")
+    times, diam = [], None
+    for _ in range(3):
+        diam = g.diameter(s)
+        times.append(g.last_launch()[0] * 1e3)
+    _emit({"workload": "c4_pass_grid2048_256src_diameter", "metric": "kernel time of the per-source engine, counting mode",
+           "unit": "ms", "kernel_ms": times, "diameter": diam})
+
+
 def wl_c3(args):
     import gu
     import oracle
@@ -458,4 +474,4 @@ def wl_dag(args):
 
 
 def run(workload, args):
-    {"c1": wl_c1, "c3": wl_c3, "c3-pass": wl_c3_pass, "c4": wl_c4, "c5": wl_c5, "io": wl_io, "dag": wl_dag}[workload](args)
+    {"c1": wl_c1, "c3": wl_c3, "c3-pass": wl_c3_pass, "c4": wl_c4, "c4-pass": wl_c4_pass, "c5": wl_c5, "io": wl_io, "dag": wl_dag}[workload](args)
