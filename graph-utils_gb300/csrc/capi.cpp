@@ -689,7 +689,7 @@ gu_status gu_lbs(const int32_t *counts_dev, int32_t N, int32_t *scanned_dev, int
         int dev = 0;
         GU_CUDA_CHECK(cudaGetDevice(&dev));
         Workspace &ws = device_scratch(dev);
-        const size_t need = lbs_scratch_bytes(N);
+        const size_t need = lbs_scratch_bytes(N, result_capacity);
         void *p = ws.get(need);
         launch_lbs(counts_dev, N, scanned_dev, result_dev, result_capacity, total_dev, total_host, p, ws.bytes,
                    (cudaStream_t)stream);

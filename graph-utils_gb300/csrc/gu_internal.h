@@ -202,7 +202,7 @@ size_t msbfs_workspace_bytes(const DeviceGraph &g, int32_t k);
 void bc_read_status(DeviceGraph &g, int *dev_err, int *max_level);
 int bc_read_timeline(DeviceGraph &g, int max_entries, int32_t *batch, int32_t *level, int32_t *kind,
                      int64_t *frontier_vertices, int64_t *frontier_edges, double *t_ms);
-size_t lbs_scratch_bytes(int32_t N);
+size_t lbs_scratch_bytes(int32_t N, int64_t result_capacity);
 void launch_lbs(const int32_t *counts, int32_t N, int32_t *scanned, int32_t *result, int64_t result_capacity,
                 int32_t *total_dev, int64_t *total_host, void *scratch_ptr, size_t scratch_bytes, cudaStream_t st);
 void launch_race_and_resolve(const int32_t *pred, int32_t nwarps, int32_t *winner, cudaStream_t st);

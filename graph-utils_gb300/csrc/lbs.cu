@@ -9,10 +9,11 @@
 //   1. scan: CTAs reduce tiles of 4096 counts (int64, warp shuffles), one CTA
 //      scans the tile sums, CTAs rescan their tiles with the tile offset;
 //   2. search: merge-path partition (the merge of slot keys 0..total-1 with the
-//      scanned offsets, ties to the offsets) into equal diagonals of 4096; a CTA
-//      finds its two path endpoints by binary search, stages its offsets in
-//      shared memory, every thread merges 8 steps from its own diagonal, and
-//      the CTA writes its run of owners contiguously.
+//      scanned offsets, ties to the offsets) into equal diagonals of 4096; the
+//      tiles' path endpoints are found by binary search in one pass (a thread
+//      per endpoint), then a CTA per tile stages its offsets in shared memory,
+//      every thread merges 8 steps from its own diagonal, and the CTA writes its
+//      run of owners contiguously.
 // race_and_resolve (race_and_resolve.cuh:13-25) is exposed as a warp-level
 // kernel over an array of predicates for testing the device primitive.
 #include "device_utils.cuh"
@@ -148,18 +149,27 @@ __device__ __forceinline__ int32_t merge_path(const int32_t *B, int32_t N, long 
     return (int32_t)lo;
 }
 
+// Path endpoints of every search tile, all in parallel: one thread per tile
+// boundary d = t * LBS_TILE (the last one at total + N).  Done inside each
+// search CTA, the 20-odd dependent global loads of the binary search were most
+// of the kernel's time.
+__global__ void lbs_partition(const int32_t *__restrict__ scanned, int32_t N, long long total, int32_t ntile,
+                              int32_t *__restrict__ kpart)
+{
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t > ntile) return;
+    kpart[t] = merge_path(scanned, N, total, min(t * LBS_TILE, total + N));
+}
+
 __global__ void __launch_bounds__(LBS_THREADS) lbs_search(const int32_t *__restrict__ scanned, int32_t N,
-                                                          long long total, int32_t *__restrict__ result)
+                                                          long long total, const int32_t *__restrict__ kpart,
+                                                          int32_t *__restrict__ result)
 {
     __shared__ int32_t s_b[LBS_TILE + 1];
     __shared__ int32_t s_out[LBS_TILE];
-    __shared__ int32_t s_k[2];
     const long long d0 = (long long)blockIdx.x * LBS_TILE;
     const long long d1 = min(d0 + LBS_TILE, total + N);
-    if (threadIdx.x == 0) s_k[0] = merge_path(scanned, N, total, d0);
-    if (threadIdx.x == 32) s_k[1] = merge_path(scanned, N, total, d1);
-    __syncthreads();
-    const int32_t k0 = s_k[0], k1 = s_k[1];
+    const int32_t k0 = __ldg(kpart + blockIdx.x), k1 = __ldg(kpart + blockIdx.x + 1);
     const long long i0 = d0 - k0, i1 = d1 - k1;  // slots [i0, i1) of this tile
     const int nb = k1 - k0;
     for (int t = threadIdx.x; t < nb; t += blockDim.x) s_b[t] = scanned[k0 + t];
@@ -196,10 +206,15 @@ __global__ void race_and_resolve_kernel(const int32_t *__restrict__ pred, int32_
     winner[i] = race_and_resolve_warp(pred[i] != 0);
 }
 
-size_t lbs_scratch_bytes(int32_t N)
+// Scan tile sums and flags, then the search tiles' path endpoints (as many as a
+// total of result_capacity slots can need).
+size_t lbs_scratch_bytes(int32_t N, int64_t result_capacity)
 {
-    const size_t ntiles = (size_t)(((long long)(N > 0 ? N : 0) + LBS_TILE - 1) / LBS_TILE);
-    return (ntiles + 2) * sizeof(long long) + 256;
+    const long long n = N > 0 ? N : 0;
+    const size_t ntiles = (size_t)((n + LBS_TILE - 1) / LBS_TILE);
+    const long long cap = result_capacity < 0 ? 0 : (result_capacity > INT32_MAX ? INT32_MAX : result_capacity);
+    const size_t nsearch = (size_t)((cap + n + LBS_TILE - 1) / LBS_TILE);
+    return (ntiles + 2) * sizeof(long long) + 256 + (nsearch + 2) * sizeof(int32_t);
 }
 
 void launch_lbs(const int32_t *counts, int32_t N, int32_t *scanned, int32_t *result, int64_t result_capacity,
@@ -208,10 +223,11 @@ void launch_lbs(const int32_t *counts, int32_t N, int32_t *scanned, int32_t *res
     if (N < 0) throw gu_error(GU_ERR_INVALID_ARGUMENT, "N must be >= 0");
     if (N > 0 && (!counts || !scanned)) throw gu_error(GU_ERR_INVALID_ARGUMENT, "null counts or scanned");
     const int32_t ntiles = (int32_t)(((long long)N + LBS_TILE - 1) / LBS_TILE);
-    if (scratch_bytes < lbs_scratch_bytes(N)) throw gu_error(GU_ERR_INTERNAL, "lbs scratch too small");
+    if (scratch_bytes < lbs_scratch_bytes(N, result_capacity)) throw gu_error(GU_ERR_INTERNAL, "lbs scratch too small");
     long long *tile = reinterpret_cast<long long *>(scratch_ptr);
     long long *tot_d = tile + ntiles;
     int *neg_d = reinterpret_cast<int *>(tot_d + 1);
+    int32_t *kpart = reinterpret_cast<int32_t *>(reinterpret_cast<char *>(tile) + (ntiles + 2) * sizeof(long long) + 256);
     long long tot = 0;
     int neg = 0;
     if (N > 0) {
@@ -234,7 +250,10 @@ void launch_lbs(const int32_t *counts, int32_t N, int32_t *scanned, int32_t *res
         lbs_scan_write<<<ntiles, LBS_THREADS, 0, st>>>(counts, N, tile, scanned);
         const long long ndiag = tot + N;
         const int32_t nsearch = (int32_t)((ndiag + LBS_TILE - 1) / LBS_TILE);
-        if (tot > 0) lbs_search<<<nsearch, LBS_THREADS, 0, st>>>(scanned, N, tot, result);
+        if (tot > 0) {
+            lbs_partition<<<(nsearch + 1 + 255) / 256, 256, 0, st>>>(scanned, N, tot, nsearch, kpart);
+            lbs_search<<<nsearch, LBS_THREADS, 0, st>>>(scanned, N, tot, kpart, result);
+        }
         GU_CUDA_CHECK(cudaGetLastError());
     }
     if (total_dev) {
