@@ -166,7 +166,9 @@ __global__ void __launch_bounds__(LBS_THREADS) lbs_search(const int32_t *__restr
                                                           int32_t *__restrict__ result)
 {
     __shared__ int32_t s_b[LBS_TILE + 1];
-    __shared__ int32_t s_out[LBS_TILE];
+    // owners by slot, one padding word per 32: thread t writes slots 8t.. (a stride of 8
+    // words across the warp), which unpadded would hit 4 banks
+    __shared__ int32_t s_out[LBS_TILE + LBS_TILE / 32];
     const long long d0 = (long long)blockIdx.x * LBS_TILE;
     const long long d1 = min(d0 + LBS_TILE, total + N);
     const int32_t k0 = __ldg(kpart + blockIdx.x), k1 = __ldg(kpart + blockIdx.x + 1);
@@ -188,14 +190,15 @@ __global__ void __launch_bounds__(LBS_THREADS) lbs_search(const int32_t *__restr
         const bool take_slot = kk >= nb || ii < (long long)s_b[kk];
         if (take_slot) {
             if (ii >= i1) break;
-            s_out[ii - i0] = k0 + kk - 1;
+            const int o = (int)(ii - i0);
+            s_out[o + (o >> 5)] = k0 + kk - 1;
             ++ii;
         } else {
             ++kk;
         }
     }
     __syncthreads();
-    for (long long i = threadIdx.x; i < i1 - i0; i += blockDim.x) result[i0 + i] = s_out[i];
+    for (int i = threadIdx.x; i < (int)(i1 - i0); i += blockDim.x) result[i0 + i] = s_out[i + (i >> 5)];
 }
 
 // Winner lane per warp of 32 predicates (race_and_resolve_warp).
