@@ -152,6 +152,7 @@ struct Lvl {
     int32_t tag;  // stamp of level j (j + 1)
     u64 active[MAXW];  // bottom-up levels: without the rare sources
     bool rare_td;      // bottom-up level with rare sources expanded top-down
+    bool scanq;        // top-down level whose next queue is built by a scan of F_j afterwards
 };
 
 struct GridG {
@@ -415,6 +416,12 @@ __device__ __forceinline__ void td_visit(const MsArgs &a, const Lvl &L, const u6
                                          const Q &qu = Q())
 {
     const size_t o = (size_t)w * W;
+    if (L.scanq) {  // OR every frontier bit into F_j; the scan after the level removes the known ones
+#pragma unroll
+        for (int q = 0; q < W; ++q)
+            if (f[q]) red_or(L.fnxt + o + q, f[q]);
+        return;
+    }
     u64 s[W], nb[W];
     ldw<W>(a.seen + o, s);
 #pragma unroll
@@ -431,6 +438,14 @@ __device__ __forceinline__ void td_visit2(const MsArgs &a, const Lvl &L, const u
                                           const u64 (&f2)[W], int32_t w2, const Q &qu = Q())
 {
     const size_t o = (size_t)w * W, o2 = (size_t)(w2 < 0 ? w : w2) * W;
+    if (L.scanq) {
+#pragma unroll
+        for (int q = 0; q < W; ++q) {
+            if (f[q]) red_or(L.fnxt + o + q, f[q]);
+            if (w2 >= 0 && f2[q]) red_or(L.fnxt + o2 + q, f2[q]);
+        }
+        return;
+    }
     u64 s[W], s2[W];
     ldw<W>(a.seen + o, s);
     ldw<W>(a.seen + o2, s2);
@@ -1523,6 +1538,7 @@ __global__ void __launch_bounds__(MS_THREADS, MS_MIN_BLOCKS) ms_grid_kernel(MsAr
             }
             if (rank < COVER_SLOT) a.cover[((j + 1) & 3) * COVER_SLOT + rank] = 0;
             L.rare_td = false;
+            L.scanq = false;
             // plane b is first written in phase 2^b + 1; clear it one phase earlier
             if ((j & (j - 1)) == 0) {
                 const int pb = __ffs(j) - 1;
@@ -1593,6 +1609,12 @@ __global__ void __launch_bounds__(MS_THREADS, MS_MIN_BLOCKS) ms_grid_kernel(MsAr
                     gather_mp<W, GridG, true>(a, LC, s_rare);
                 }
             } else {
+                // A top-down expansion over more edges than the graph has vertices
+                // discovers a large F_j, most vertices many times: then a visit is
+                // only an OR of the frontier word into F_j (no read of seen, no
+                // first-discovery stamp), and one scan after the level keeps the
+                // bits not seen before, updates seen and builds the next queue.
+                L.scanq = VARIANT == GU_BFS_AUTO && (double)L.qedges > (double)a.n;
                 td_update<W, GridG>(a, L);
                 if (VARIANT == GU_BFS_EDGE) gather_edge<W, GridG>(a, L);
                 else if (VARIANT == GU_BFS_WARP) gather_warp<W, GridG>(a, L);
@@ -1601,6 +1623,30 @@ __global__ void __launch_bounds__(MS_THREADS, MS_MIN_BLOCKS) ms_grid_kernel(MsAr
                 else if (VARIANT == GU_BFS_SHUFFLE) gather_shuffle<W, GridG>(a, L);
                 else if (VARIANT == GU_BFS_LINEAR) gather_linear<W, GridG>(a, L);
                 else gather_mp<W, GridG>(a, L);  // AUTO, BOTTOM_UP level 1
+                if (L.scanq) {
+                    if (!barrier()) return;  // every claim of the level is in F_j
+                    const CtaQ cq{reinterpret_cast<int32_t *>(ms_smem()), cq_count(), MS_SMEM_BYTES / 4};
+                    for (long long v = rank; v < a.n; v += size) {
+                        const size_t o = (size_t)v * W;
+                        u64 f[W];
+                        ldw<W>(L.fnxt + o, f);
+                        if (!anyw<W>(f)) continue;
+                        u64 sn[W], nb[W];
+                        ldw<W>(a.seen + o, sn);
+#pragma unroll
+                        for (int q = 0; q < W; ++q) {
+                            nb[q] = f[q] & ~sn[q];
+                            sn[q] |= nb[q];
+                        }
+                        stw<W>(L.fnxt + o, nb);  // F_j: the new bits only (zero if none)
+                        if (anyw<W>(nb)) {
+                            stw<W>(a.seen + o, sn);
+                            cq.push(a, L, (int32_t)v);
+                        }
+                    }
+                    __syncthreads();
+                    if (*cq.n > 0) cta_flush(a, L, cq);
+                }
             }
             __syncthreads();
             if (threadIdx.x < W) {
