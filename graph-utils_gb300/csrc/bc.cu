@@ -691,7 +691,9 @@ __global__ void __launch_bounds__(BC_THREADS, 2) bc_grid_kernel(BcArgs a, int do
             if (!barrier(BC_PHASE_CLEAR, j)) return;
             // work units of all word groups, taken dynamically (unit x = group x / nunits)
             const long long nfw = (long long)(W / NQ) * a.cin.nunits;
-            for (;;) {
+            // warps beyond the unit count have nothing to take (on a small graph most
+            // of the grid): they skip the shared counter instead of queueing on it
+            for (; gwarp() < nfw;) {
                 long long x = 0;
                 if (lane_id() == 0) x = atomicAdd(&ctl->fwork, 1u);
                 x = __shfl_sync(FULL_MASK, x, 0);
@@ -717,7 +719,7 @@ __global__ void __launch_bounds__(BC_THREADS, 2) bc_grid_kernel(BcArgs a, int do
             for (int l = L; l >= 1; --l) {
                 if (rank == 0) ctl->work[(l - 1) & 1] = 0;  // level l-1's counter (last used by level l+1)
                 const long long nbw = (long long)(W / NQ) * a.cout.nunits;
-                for (;;) {
+                for (; gwarp() < nbw;) {
                     long long x = 0;
                     if (lane_id() == 0) x = atomicAdd(&ctl->work[l & 1], 1u);
                     x = __shfl_sync(FULL_MASK, x, 0);
@@ -773,16 +775,23 @@ static void build_chunks(DeviceGraph &g, const std::vector<int32_t> &R, ChunkMap
     };
     // work units: items by descending edge count (heavy items are taken first,
     // light ones fill the gaps), cut into runs of at most 32 items and about
-    // BC_UNIT_COST edges (an item counts its edges plus a fixed overhead)
+    // BC_UNIT_COST edges (an item counts its edges plus a fixed overhead) -- or
+    // less on a small graph, so that there are at least four units per warp of
+    // the grid (down to one item per unit) and no level runs on a few warps
     std::vector<int32_t> order(v.size()), ustart;
     for (size_t i = 0; i < order.size(); ++i) order[i] = (int32_t)i;
     std::stable_sort(order.begin(), order.end(),
                      [&](int32_t x, int32_t y) { return e1[x] - e0[x] > e1[y] - e0[y]; });
-    int cost = 0, cnt = 0;
+    long long total_cost = 0;
+    for (size_t i = 0; i < v.size(); ++i) total_cost += e1[i] - e0[i] + BC_ITEM_OVERHEAD;
+    const long long warps = (long long)std::max(g.sm_count, 1) * 2 * (BC_THREADS / 32);
+    const long long unit_cost = std::max<long long>(1, std::min<long long>(BC_UNIT_COST, total_cost / (4 * warps)));
+    long long cost = 0;
+    int cnt = 0;
     for (size_t i = 0; i < order.size(); ++i) {
         if (cnt == 0) ustart.push_back((int32_t)i);
         cost += e1[order[i]] - e0[order[i]] + BC_ITEM_OVERHEAD;
-        if (++cnt == 32 || cost >= BC_UNIT_COST) cost = cnt = 0;
+        if (++cnt == 32 || cost >= unit_cost) cost = cnt = 0;
     }
     ustart.push_back((int32_t)order.size());
     up(order, cm.order);
