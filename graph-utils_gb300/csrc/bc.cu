@@ -17,14 +17,19 @@
 //   lvl[L+1][n][W]      lvl[j] = bitmap of the sources whose BFS level of v is j
 //   sigma[n][B] uint64  shortest-path counts, sources of the batch contiguous
 //   delta[n][B] double  dependencies
+//   beta[n][B] double   (1 + delta) / sigma, the backward terms
 //   part[slots][W][64]  backward partial sums of vertices split into several items
 //   bc[n] double        accumulated over batches (output)
 // Work items (graph-static, ChunkMap): one per <= 256 edges of a vertex's in-
 // (forward) or out-adjacency (backward), times the word groups of the batch (up
-// to four source words, 256 sources, per group); a warp per item, lane l owning
-// sources 64q+l and 64q+32+l of each word q of the group, so an adjacency range
-// is read once for 256 sources.  One grid barrier per level (two for backward
-// levels with split vertices).
+// to four source words, 256 sources, per group), so an adjacency range is read
+// once for 256 sources.  Items are grouped into work units (heaviest first, <= 32
+// items and about 512 edges; smaller on small graphs) that warps take from a
+// per-level counter; a warp triages a unit's items a lane each and then runs the
+// items with work.  Forward, lane l owns sources 64q+l and 64q+32+l of each word
+// q of the group; backward, the FP64 terms are compacted to dense source lists
+// (see bc_backward_item).  One grid barrier per level (two for backward levels
+// with split vertices), plus the level bitmap's clear.
 #include "device_utils.cuh"
 #include "gu_internal.h"
 
