@@ -25,10 +25,12 @@
 //     bits when they were discovered)
 //   * clear F_{j-2}
 //   * discover F_j top-down (gather the adjacency of the F_{j-1} queue and claim
-//     the bits missing from seen with 64-bit OR reductions into seen and F_j) or
-//     bottom-up (each vertex still missing some active source ORs its
-//     in-neighbours' F_{j-1} words, stopping as soon as every missing active
-//     source is found).
+//     the bits missing from seen with 64-bit OR reductions into seen and F_j; on
+//     an expansion over more edges than the graph has vertices, OR the frontier
+//     words into F_j unread and let one scan after the level drop the bits seen
+//     before, update seen and build the queue) or bottom-up (each vertex still
+//     missing some active source ORs its in-neighbours' F_{j-1} words, stopping
+//     as soon as every missing active source is found).
 // A source is active while its frontier is non-empty; the active mask of F_j is
 // OR-reduced per CTA in shared memory during phase j.  Direction: top-down ->
 // bottom-up when the frontier's out-edges exceed m / alpha, back when it holds
