@@ -64,6 +64,23 @@ def dist_env():
     return ws, rank, local
 
 
+def max_over_ranks(x, ws, device=None):
+    """The largest of the ranks' values (every rank gets it); x itself on one rank.
+    The job's time is its slowest rank's, as the timing contract asks."""
+    if ws <= 1:
+        return float(x)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_gteps(ws, edges_per_rank_step, steps, seconds):
+    """Whole-job GTEPS: every rank (a replica) processes the same edges per step."""
+    return ws * edges_per_rank_step * steps / seconds / 1e9
+
+
 def peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(path):
@@ -276,12 +293,8 @@ def run_ours(args):
         if psampler:
             psampler.__exit__(None, None, None)
     clocks = clk.summary()
-    t_total = ev0.elapsed_time(ev1) / 1e3
-    if ws > 1:
-        t = torch.tensor([t_total], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        t_total = float(t.item())
-    value = ws * gteps_edges * args.steps / t_total / 1e9
+    t_total = max_over_ranks(ev0.elapsed_time(ev1) / 1e3, ws, dev)
+    value = job_gteps(ws, gteps_edges, args.steps, t_total)
     if psampler:
         power = {"avg_w": psampler.watts, "samples": psampler.samples,
                  "gteps_per_w": value / ws / psampler.watts if psampler.watts else None,
@@ -299,13 +312,9 @@ def run_ours(args):
         for _ in range(args.steps):
             g.bfs_host(src_np, args.variant, out=out_np, stream=stream)
         barrier()
-        t_e2e = time.perf_counter() - t0
-        if ws > 1:
-            t = torch.tensor([t_e2e], device=dev)
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            t_e2e = float(t.item())
+        t_e2e = max_over_ranks(time.perf_counter() - t0, ws, dev)
         ok = np.array_equal(out_np[:4], dist_buf[:4].cpu().numpy())
-        e2e = {"value": ws * gteps_edges * args.steps / t_e2e / 1e9, "unit": "GTEPS",
+        e2e = {"value": job_gteps(ws, gteps_edges, args.steps, t_e2e), "unit": "GTEPS",
                "h2d_bytes_per_step": int(srcs.nbytes), "d2h_bytes_per_step": int(len(srcs) * hg.n * 4),
                "ms_per_step": 1e3 * t_e2e / args.steps, "host_rows_match_device": bool(ok)}
 
