@@ -223,3 +223,21 @@ def test_autotune_keeps_distances(shape):
         g.set_tuning({"engine": "batched", "alpha": 2.0, "beta": 24.0, "words": 3})
     g.set_tuning(None)
     np.testing.assert_array_equal(run_bfs(g, srcs, "auto")[0], ref)
+
+
+@pytest.mark.parametrize("k", [40, 100, 256, 600])
+def test_scan_built_queues_every_width(k, monkeypatch):
+    """Top-down levels over more edges than vertices build their queue by a scan of
+    F_j (R-MAT's hub levels): distances stay exact at every batch width (1, 2 and 4
+    words) and across batches.  With the bottom-up switch pushed out of reach
+    (alpha 0.25), every level is top-down and the scan is certainly taken."""
+    hg = gu.HostGraph.rmat(15, 16, seed=13)
+    g = gu.Graph(hg)
+    srcs = gu.sources(hg.n, k, seed=8)
+    ref, _ = oracle.bfs_multi(hg.R, hg.C, hg.n, srcs, nthreads=8)
+    np.testing.assert_array_equal(run_bfs(g, srcs, "auto_batched")[0], ref)
+    monkeypatch.setenv("GU_MS_ALPHA", "0.25")
+    np.testing.assert_array_equal(run_bfs(g, srcs, "auto_batched")[0], ref)
+    tl = g.level_profile()
+    assert all(e["kind"] in ("init", "top-down", "rows") for e in tl)
+    assert any(e["kind"] == "top-down" and e["frontier_edges"] > hg.n for e in tl)
