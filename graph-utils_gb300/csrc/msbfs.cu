@@ -1465,19 +1465,33 @@ __global__ void __launch_bounds__(MS_THREADS, MS_MIN_BLOCKS) ms_grid_kernel(MsAr
     if (threadIdx.x == 0) *cq_count() = 0;
     const int bsz = 64 * W;
     const int nbatch = (a.k + bsz - 1) / bsz;
+    // First-discovery stamps carry level tags that grow across the launch's batches
+    // (a batch's tags start above every tag of the batches before it), so the
+    // stamps are cleared once per launch, not per batch.
+    int tag_base = 0;
     for (int b = 0; b < nbatch; ++b) {
         const int row0 = b * bsz;
         const int nb = min(bsz, a.k - row0);
         const int eager = min(EAGER_PLANES, a.nplanes);
+        if (tag_base > INT_MAX / 2) tag_base = 0;  // (then the stamps are cleared again below)
         {
-            // seen, f[0..2] and the eager planes are one contiguous region
-            // (256-byte aligned start): zero it with consecutive 16-byte stores
-            const size_t cnt = (size_t)((a.plane + eager * pstride) - a.seen);
-            ulonglong2 *v2 = reinterpret_cast<ulonglong2 *>(a.seen);
+            // seen, f[0..2] and the eager planes are one contiguous region (256-byte
+            // aligned start), cleared with consecutive 16-byte stores.  After the
+            // first batch the frontier arrays are already clear (each batch clears
+            // its last frontier through its queue), so only seen and the planes are.
             const ulonglong2 z2 = make_ulonglong2(0ull, 0ull);
-            for (long long i = rank; i < (long long)(cnt >> 1); i += size) v2[i] = z2;
-            if ((cnt & 1) && rank == 0) a.seen[cnt - 1] = 0ull;
-            if (W > 1)
+            auto clear = [&](u64 *p0, size_t cnt) {
+                ulonglong2 *v2 = reinterpret_cast<ulonglong2 *>(p0);
+                for (long long i = rank; i < (long long)(cnt >> 1); i += size) v2[i] = z2;
+                if ((cnt & 1) && rank == 0) p0[cnt - 1] = 0ull;
+            };
+            if (b == 0) {
+                clear(a.seen, (size_t)((a.plane + eager * pstride) - a.seen));
+            } else {
+                clear(a.seen, (size_t)(a.fr[0] - a.seen));
+                clear(a.plane, (size_t)eager * pstride);
+            }
+            if (W > 1 && tag_base == 0)
                 for (long long w = rank; w < a.n; w += size) a.stamp[w] = 0;
         }
         if (rank < 4) {
@@ -1497,7 +1511,7 @@ __global__ void __launch_bounds__(MS_THREADS, MS_MIN_BLOCKS) ms_grid_kernel(MsAr
             atomicOr(&ctl->active[0][q], bit);
             bool first;
             if (W == 1) first = old == 0;
-            else first = atomicMax(a.stamp + s, 1) < 1;
+            else first = atomicMax(a.stamp + s, tag_base + 1) < tag_base + 1;
             if (first) append_vertex(a, 0, a.q[0], a.qoff[0], s);
         }
         if (threadIdx.x == 0) record_event(ctl, ev_idx, rank == 0, b, 0, 4, nb, 0);  // batch initialised, seeded
@@ -1530,7 +1544,7 @@ __global__ void __launch_bounds__(MS_THREADS, MS_MIN_BLOCKS) ms_grid_kernel(MsAr
             L.fprv = a.fr[L.prv];
             L.sact = s_act;
             L.lev = j - 1;
-            L.tag = j + 1;
+            L.tag = tag_base + j + 1;
             if (rank == 0) {
                 const int z = (j + 1) & 3;
                 ctl->qpack[z] = 0;
@@ -1666,7 +1680,16 @@ __global__ void __launch_bounds__(MS_THREADS, MS_MIN_BLOCKS) ms_grid_kernel(MsAr
             prev_bu = bu;
             if (!barrier()) return;
         }
-        // F_{j-1} is empty: levels of this batch are 0..j-2
+        // F_{j-1} is empty: levels of this batch are 0..j-2.  F_{j-2} is the only
+        // frontier array with bits left: clear it through its queue, so that the
+        // next batch starts from clear frontier arrays.
+        {
+            const int nq = (int)(s_ctl.qpack[(j - 2) & 3] >> QPACK_SHIFT);
+            const int32_t *qq = a.q[(j - 2) % 3];
+            u64 *ff = a.fr[(j - 2) % 3];
+            for (long long i = rank; i < nq; i += size) zerow<W>(ff + (size_t)__ldcg(qq + i) * W);
+        }
+        tag_base += j + 1;
         int used = 0;
         while (used < 31 && ((j - 2) >> used) != 0) ++used;
         if (a.dist) write_distances<W, GridG>(a, row0, nb, used);  // no rows: diameter, reach queries
