@@ -61,6 +61,7 @@ static void check_dev_status(DeviceGraph &g, cudaStream_t stream)
     int err = 0;
     msbfs_read_status(g, &err, nullptr, nullptr, nullptr);
     if (err == DEV_ERR_BARRIER_TIMEOUT) throw gu_error(GU_ERR_TIMEOUT, "a device-side wait exceeded its limit");
+    if (err == DEV_ERR_BAD_SOURCE) throw gu_error(GU_ERR_INVALID_ARGUMENT, "source vertex out of range");
     if (err != 0) throw gu_error(GU_ERR_INTERNAL, "device reported error code " + std::to_string(err));
 }
 
@@ -335,6 +336,26 @@ gu_status gu_graph_last_launch(gu_graph g, double *kernel_seconds, int *td_level
     });
 }
 
+gu_status gu_graph_launch_times(gu_graph g, int max_entries, double *kernel_seconds, int *count)
+{
+    return guarded([&] {
+        if (!g || max_entries < 0 || (max_entries > 0 && !kernel_seconds))
+            throw gu_error(GU_ERR_INVALID_ARGUMENT, "bad arguments");
+        DeviceGraph &dg = *g->g;
+        std::lock_guard<std::mutex> lk(dg.mu);
+        DeviceScope ds(dg.device);
+        const int n = std::min(dg.ring_count, max_entries);
+        for (int i = 0; i < n; ++i) {  // oldest first
+            const int slot = (dg.ring_next - n + i + 2 * DeviceGraph::LAUNCH_RING) % DeviceGraph::LAUNCH_RING;
+            GU_CUDA_CHECK(cudaEventSynchronize(dg.ring_stop[slot]));
+            float ms = 0;
+            GU_CUDA_CHECK(cudaEventElapsedTime(&ms, dg.ring_start[slot], dg.ring_stop[slot]));
+            kernel_seconds[i] = ms / 1000.0;
+        }
+        if (count) *count = n;
+    });
+}
+
 gu_status gu_graph_level_profile(gu_graph g, int max_entries, int32_t *batch, int32_t *level, int32_t *kind,
                                  int64_t *frontier_vertices, int64_t *frontier_edges, double *t_ms, int *count)
 {
@@ -553,14 +574,21 @@ gu_status gu_bfs(gu_graph g, int variant, const int32_t *sources_dev, int32_t k,
         DeviceGraph &dg = *g->g;
         std::lock_guard<std::mutex> lk(dg.mu);
         DeviceScope ds(dg.device);
-        // validate sources on the host side of the boundary (a bad id would index out of bounds)
-        std::vector<int32_t> hs((size_t)k);
-        if (k > 0) {
+        // Source ids are checked before they index anything: by the batched kernel
+        // itself where it is the engine that runs (it skips a bad id and reports it
+        // as GU_ERR_INVALID_ARGUMENT), else here on the host, which costs a copy and a
+        // synchronisation per call.
+        const bool batched = variant != GU_BFS_PLAIN &&
+                             (variant != GU_BFS_AUTO ||
+                              (dg.tune.set ? dg.tune.engine == GU_ENGINE_BATCHED
+                                           : auto_engine(dg, true) == AutoEngine::BATCHED));
+        if (!batched && k > 0) {
+            std::vector<int32_t> hs((size_t)k);
             GU_CUDA_CHECK(cudaMemcpyAsync(hs.data(), sources_dev, sizeof(int32_t) * (size_t)k, cudaMemcpyDeviceToHost,
                                           (cudaStream_t)stream));
             GU_CUDA_CHECK(cudaStreamSynchronize((cudaStream_t)stream));
+            validate_sources_host(hs.data(), k, dg.n);
         }
-        validate_sources_host(hs.data(), k, dg.n);
         bfs_device(dg, variant, sources_dev, k, dist_dev, ld, (cudaStream_t)stream);
     });
 }

@@ -55,10 +55,13 @@ void Workspace::release()
 
 void DeviceGraph::mark_start(cudaStream_t s)
 {
-    if (!ev_start) {
-        GU_CUDA_CHECK(cudaEventCreate(&ev_start));
-        GU_CUDA_CHECK(cudaEventCreate(&ev_stop));
+    const int slot = ring_next;
+    if (!ring_start[slot]) {
+        GU_CUDA_CHECK(cudaEventCreate(&ring_start[slot]));
+        GU_CUDA_CHECK(cudaEventCreate(&ring_stop[slot]));
     }
+    ev_start = ring_start[slot];
+    ev_stop = ring_stop[slot];
     GU_CUDA_CHECK(cudaEventRecord(ev_start, s));
 }
 
@@ -66,6 +69,8 @@ void DeviceGraph::mark_stop(cudaStream_t s)
 {
     GU_CUDA_CHECK(cudaEventRecord(ev_stop, s));
     timed = true;
+    ring_next = (ring_next + 1) % LAUNCH_RING;
+    if (ring_count < LAUNCH_RING) ++ring_count;
 }
 
 DeviceGraph::~DeviceGraph()
@@ -73,8 +78,10 @@ DeviceGraph::~DeviceGraph()
     int prev = -1;
     cudaGetDevice(&prev);
     cudaSetDevice(device);
-    if (ev_start) cudaEventDestroy(ev_start);
-    if (ev_stop) cudaEventDestroy(ev_stop);
+    for (int i = 0; i < LAUNCH_RING; ++i) {
+        if (ring_start[i]) cudaEventDestroy(ring_start[i]);
+        if (ring_stop[i]) cudaEventDestroy(ring_stop[i]);
+    }
     if (copy_st) cudaStreamDestroy(copy_st);
     ws.release();
     io.release();

@@ -35,6 +35,7 @@ enum DevErr : int {
     DEV_OK = 0,
     DEV_ERR_BARRIER_TIMEOUT = 1,
     DEV_ERR_QUEUE_OVERFLOW = 2,
+    DEV_ERR_BAD_SOURCE = 4,  // batched search: a source id outside [0, n) (skipped, not searched)
 };
 
 struct gu_error : std::runtime_error {
@@ -143,7 +144,11 @@ struct DeviceGraph {
     ChunkMap bc_in, bc_out;
     std::vector<int32_t> host_R, host_RT;  // offsets kept on the host for building work items
     std::vector<void *> extra_allocs;  // freed with the graph
-    // events bracketing the last main kernel launch (kernel-only timing)
+    // events bracketing the last main kernel launch (kernel-only timing): the
+    // current slot of a ring that keeps the last LAUNCH_RING launches' events
+    static constexpr int LAUNCH_RING = 64;
+    cudaEvent_t ring_start[LAUNCH_RING] = {}, ring_stop[LAUNCH_RING] = {};
+    int ring_next = 0, ring_count = 0;
     cudaEvent_t ev_start = nullptr, ev_stop = nullptr;
     cudaStream_t copy_st = nullptr;  // host-form calls copy rows out on it while later sources run
     bool timed = false;

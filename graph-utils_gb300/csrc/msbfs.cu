@@ -1504,6 +1504,10 @@ __global__ void __launch_bounds__(MS_THREADS, MS_MIN_BLOCKS) ms_grid_kernel(MsAr
         if (!barrier()) return;
         if (rank < nb) {
             const int32_t s = __ldg(a.sources + row0 + rank);
+            if ((unsigned)s >= (unsigned)a.n) {  // reported by the call; its row is never seeded
+                atomicCAS(&ctl->err, 0, (int)DEV_ERR_BAD_SOURCE);
+                goto seeded;
+            }
             const int q = (int)rank >> 6;
             const u64 bit = 1ull << (rank & 63);
             const u64 old = atomicOr(a.fr[0] + (size_t)s * W + q, bit);
@@ -1514,6 +1518,7 @@ __global__ void __launch_bounds__(MS_THREADS, MS_MIN_BLOCKS) ms_grid_kernel(MsAr
             else first = atomicMax(a.stamp + s, tag_base + 1) < tag_base + 1;
             if (first) append_vertex(a, 0, a.q[0], a.qoff[0], s);
         }
+    seeded:
         if (threadIdx.x == 0) record_event(ctl, ev_idx, rank == 0, b, 0, 4, nb, 0);  // batch initialised, seeded
         ++ev_idx;
         if (!barrier()) return;
@@ -1571,7 +1576,10 @@ __global__ void __launch_bounds__(MS_THREADS, MS_MIN_BLOCKS) ms_grid_kernel(MsAr
             }
             if (bu) {
                 // part A; F_0 may hold sources without in-edges, which no class list has
-                if (j == 2 && rank < nb) zerow<W>(L.fprv + (size_t)__ldg(a.sources + row0 + rank) * W);
+                if (j == 2 && rank < nb) {
+                    const int32_t s0 = __ldg(a.sources + row0 + rank);
+                    if ((unsigned)s0 < (unsigned)a.n) zerow<W>(L.fprv + (size_t)s0 * W);
+                }
                 if (rank == 0) ctl->rpack = 0;
                 bu_finalise_all<W, GridG>(a, L);
                 __syncthreads();

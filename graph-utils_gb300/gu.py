@@ -94,6 +94,8 @@ def lib():
                              ctypes.POINTER(_vp)], ctypes.c_int),
         "gu_graph_last_launch": ([_vp, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int),
                                   ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
+        "gu_graph_launch_times": ([_vp, ctypes.c_int, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int)],
+                                  ctypes.c_int),
         "gu_graph_autotune": ([_vp, _vp, ctypes.c_int32, ctypes.POINTER(GuTuning), ctypes.POINTER(GuTuning),
                                ctypes.c_int, ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
         "gu_graph_set_tuning": ([_vp, ctypes.POINTER(GuTuning)], ctypes.c_int),
@@ -267,6 +269,14 @@ class Graph:
         b = ctypes.c_size_t()
         check(lib().gu_graph_info(self._h, None, None, None, ctypes.byref(b)))
         return b.value
+
+    def launch_times(self, max_entries=64):
+        """Kernel seconds of the graph's last launches (up to 64), oldest first."""
+        out = np.zeros(max_entries, np.float64)
+        cnt = ctypes.c_int()
+        check(lib().gu_graph_launch_times(self._h, max_entries, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                          ctypes.byref(cnt)))
+        return [float(x) for x in out[: cnt.value]]
 
     def autotune(self, sources_dev, max_trials=32):
         """Times AUTO's candidate engines and settings on a sample of sources and makes the

@@ -155,6 +155,11 @@ gu_status gu_graph_arrays(gu_graph g, const int32_t **R_dev, const int32_t **C_d
  * (e.g. shuffle_based.cu:42-44). */
 gu_status gu_graph_last_launch(gu_graph g, double *kernel_seconds, int *td_levels, int *bu_levels, int *max_level);
 
+/* Kernel durations of the graph's last launches (up to 64, oldest first; CUDA
+ * events on each call's stream around its main kernel): a caller timing many
+ * calls reads them once afterwards instead of querying after every call. */
+gu_status gu_graph_launch_times(gu_graph g, int max_entries, double *kernel_seconds, int *count);
+
 /* Profiling hook: the per-phase timeline of the last batched search or BC /
  * sigma pass on g (up to max_entries phases).  Entry i: batch, level j of the
  * phase, kind (0 top-down, 1 bottom-up, 2 distance write-out, 4 batch

@@ -102,12 +102,19 @@ def test_edge_cases():
     s = torch.zeros(0, dtype=torch.int32, device="cuda")
     out = torch.zeros((1, hg.n), dtype=torch.int32, device="cuda")
     g.bfs(s, out)
-    # out-of-range source is rejected before any launch
-    s = torch.tensor([0, hg.n], dtype=torch.int32, device="cuda")
-    out = torch.zeros((2, hg.n), dtype=torch.int32, device="cuda")
-    with pytest.raises(gu.GuError) as e:
-        g.bfs(s, out)
-    assert e.value.status == 1
+    # an out-of-range source is rejected: on the host before the launch for the
+    # one-CTA-per-source and per-source engines, by the batched kernel itself
+    # (which skips it) for the batched variants
+    for v in ("auto", "plain", "warp", "shuffle", "bottom_up"):
+        for bad in (hg.n, -1):
+            s = torch.tensor([0, bad, 3], dtype=torch.int32, device="cuda")
+            out = torch.zeros((3, hg.n), dtype=torch.int32, device="cuda")
+            with pytest.raises(gu.GuError) as e:
+                g.bfs(s, out, variant=v)
+            assert e.value.status == 1, v
+        # the graph handle stays usable
+        got, _ = run_bfs(g, srcs, v)
+        np.testing.assert_array_equal(got, ref, err_msg=v)
 
 
 @pytest.mark.parametrize("engine", ["auto", "batched"])
@@ -241,3 +248,17 @@ def test_scan_built_queues_every_width(k, monkeypatch):
     tl = g.level_profile()
     assert all(e["kind"] in ("init", "top-down", "rows") for e in tl)
     assert any(e["kind"] == "top-down" and e["frontier_edges"] > hg.n for e in tl)
+
+
+def test_launch_times_ring():
+    """gu_graph_launch_times: the kernel time of each of the last launches, oldest
+    first; the newest is the one gu_graph_last_launch reports."""
+    hg = gu.HostGraph.rmat(13, 16, seed=4)
+    g = gu.Graph(hg)
+    srcs = gu.sources(hg.n, 64, seed=1)
+    for _ in range(70):
+        run_bfs(g, srcs, "auto")
+    t = g.launch_times()
+    assert len(t) == 64 and all(x > 0 for x in t)
+    assert t[-1] == pytest.approx(g.last_launch()[0])
+    assert len(g.launch_times(5)) == 5
