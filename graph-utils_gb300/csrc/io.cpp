@@ -21,13 +21,18 @@
 // Where the reference has undefined behaviour (more METIS lines or entries than
 // the header announces, SNAP ids that are not dense, a line with one field) the
 // reader reports GU_ERR_INVALID_ARGUMENT instead.  Files are read whole and
-// parsed in place: no per-character string appends.
+// parsed in place (no per-character string appends) by several threads, each
+// over a range of whole lines, the ranges joined in file order -- the result is
+// the sequential one.
 #include "gu_internal.h"
 
 #include <algorithm>
+#include <atomic>
 #include <cstdio>
 #include <cstring>
+#include <exception>
 #include <string>
+#include <thread>
 #include <utility>
 #include <vector>
 
@@ -132,17 +137,78 @@ void check_columns(const std::vector<int32_t> &C, int32_t n)
         if (c < 0 || c >= n) throw gu_error(GU_ERR_INVALID_ARGUMENT, "vertex id out of range");
 }
 
+// Splits [b, e) into up to `parts` ranges that end at line ends (each range but
+// the last ends just after a '\n'), at least `min_bytes` each.
+std::vector<std::pair<const char *, const char *>> line_ranges(const char *b, const char *e, unsigned parts,
+                                                              size_t min_bytes)
+{
+    std::vector<std::pair<const char *, const char *>> r;
+    const size_t len = (size_t)(e - b);
+    parts = std::max(1u, std::min<unsigned>(parts, (unsigned)(len / std::max<size_t>(min_bytes, 1) + 1)));
+    const char *s = b;
+    for (unsigned i = 1; i <= parts && s < e; ++i) {
+        const char *t = i == parts ? e : b + len * i / parts;
+        if (t < s) t = s;
+        if (t < e) {
+            const char *nl = static_cast<const char *>(std::memchr(t, '\n', (size_t)(e - t)));
+            t = nl ? nl + 1 : e;
+        }
+        r.emplace_back(s, t);
+        s = t;
+    }
+    return r;
+}
+
+// Runs fn(i) for i in [0, n) on up to n threads; rethrows the first failure in
+// index order after all have finished.
+template <class Fn>
+void parallel_for(size_t n, Fn fn)
+{
+    std::vector<std::exception_ptr> err(n);
+    std::vector<std::thread> th;
+    for (size_t i = 1; i < n; ++i)
+        th.emplace_back([&, i] {
+            try {
+                fn(i);
+            } catch (...) {
+                err[i] = std::current_exception();
+            }
+        });
+    if (n > 0) {
+        try {
+            fn(0);
+        } catch (...) {
+            err[0] = std::current_exception();
+        }
+    }
+    for (auto &t : th) t.join();
+    for (auto &x : err)
+        if (x) std::rethrow_exception(x);
+}
+
+unsigned reader_threads()
+{
+    const unsigned hw = std::thread::hardware_concurrency();
+    return std::max(1u, std::min(hw ? hw : 1u, 32u));
+}
+
+// METIS: the header is read first; the vertex lines are then parsed by several
+// threads, each over a range of whole lines (its lines' entry counts and
+// entries, in order), and joined in line order.  Same result as a sequential
+// pass: line i of the body is vertex i whichever thread read it.
 HostGraph parse_metis(const std::vector<char> &buf)
 {
     HostGraph g;
     g.directed = false;
     Fields fl;
-    bool first = true;
-    int64_t m2 = 0, vertex = 0;
-    for_lines(buf, [&](const char *b, const char *e) {
-        if (b < e && *b == '%') return;
-        fl.split(b, e);
-        if (first) {
+    int64_t m2 = 0;
+    const char *p = buf.data(), *end = buf.data() + buf.size();
+    bool have_header = false;
+    while (p < end && !have_header) {
+        const char *nl = static_cast<const char *>(std::memchr(p, '\n', (size_t)(end - p)));
+        const char *le = nl ? nl : end;
+        if (!(p < le && *p == '%')) {
+            fl.split(p, le);
             if (fl.f.size() < 2) throw gu_error(GU_ERR_INVALID_ARGUMENT, "METIS header needs n and m");
             const long long n = to_int(fl.f[0].first, fl.f[0].second, "METIS header");
             m2 = 2 * to_int(fl.f[1].first, fl.f[1].second, "METIS header");
@@ -151,104 +217,204 @@ HostGraph parse_metis(const std::vector<char> &buf)
                 throw gu_error(GU_ERR_UNSUPPORTED, "weighted graphs are not supported");
             if (n < 0 || m2 < 0) throw gu_error(GU_ERR_INVALID_ARGUMENT, "negative size in METIS header");
             g.n = (int32_t)n;
-            g.R.assign((size_t)n + 1, 0);
-            g.C.reserve((size_t)m2);
-            first = false;
-            return;
+            have_header = true;
         }
-        if (vertex >= g.n) {  // lines past the last vertex: blank ones are ignored
-            for (const auto &t : fl.f)
-                if (all_digits(t.first, t.second))
-                    throw gu_error(GU_ERR_INVALID_ARGUMENT, "more METIS vertex lines than the header's n");
-            return;
+        p = nl ? nl + 1 : end;
+    }
+    if (!have_header) throw gu_error(GU_ERR_INVALID_ARGUMENT, "METIS file has no header");
+    struct Part {
+        std::vector<int32_t> cnt;  // entries of each vertex line
+        std::vector<int32_t> c;    // the entries, 0-based
+    };
+    const auto ranges = line_ranges(p, end, reader_threads(), (size_t)1 << 20);
+    std::vector<Part> parts(ranges.size());
+    parallel_for(ranges.size(), [&](size_t i) {
+        Part &pt = parts[i];
+        Fields f;
+        const char *q = ranges[i].first, *qe = ranges[i].second;
+        while (q < qe) {
+            const char *nl = static_cast<const char *>(std::memchr(q, '\n', (size_t)(qe - q)));
+            const char *le = nl ? nl : qe;
+            if (!(q < le && *q == '%')) {
+                f.split(q, le);
+                int32_t k = 0;
+                for (const auto &t : f.f) {
+                    if (!all_digits(t.first, t.second)) continue;  // dropped, as the reference drops it
+                    pt.c.push_back((int32_t)(to_int(t.first, t.second, "METIS adjacency") - 1));
+                    ++k;
+                }
+                pt.cnt.push_back(k);
+            }
+            q = nl ? nl + 1 : qe;
         }
-        for (const auto &t : fl.f) {
-            if (!all_digits(t.first, t.second)) continue;  // dropped, as the reference drops it
-            g.C.push_back((int32_t)(to_int(t.first, t.second, "METIS adjacency") - 1));
-        }
-        g.R[(size_t)++vertex] = (int32_t)g.C.size();
     });
-    if (first) throw gu_error(GU_ERR_INVALID_ARGUMENT, "METIS file has no header");
-    for (int64_t v = vertex; v < g.n; ++v) g.R[(size_t)v + 1] = (int32_t)g.C.size();  // missing lines: no neighbours
-    if ((int64_t)g.C.size() > m2) throw gu_error(GU_ERR_INVALID_ARGUMENT, "more METIS entries than twice the header's m");
-    check_columns(g.C, g.n);
+    // join in line order: the first n lines are the vertices; later lines must be empty
+    g.R.assign((size_t)g.n + 1, 0);
+    int64_t line = 0, total = 0;
+    std::vector<int64_t> c_off(parts.size() + 1, 0);  // where each part's kept entries go
+    std::vector<int64_t> keep(parts.size(), 0);       // entries of each part on vertex lines
+    for (size_t i = 0; i < parts.size(); ++i) {
+        c_off[i] = total;
+        for (const int32_t k : parts[i].cnt) {
+            if (line < g.n) {
+                total += k;
+                keep[i] += k;
+                g.R[(size_t)++line] = (int32_t)std::min<int64_t>(total, 2147483647LL);
+            } else if (k > 0) {
+                throw gu_error(GU_ERR_INVALID_ARGUMENT, "more METIS vertex lines than the header's n");
+            } else {
+                ++line;  // blank line past the last vertex: ignored
+            }
+        }
+    }
+    for (int64_t v = std::min<int64_t>(line, g.n); v < g.n; ++v) g.R[(size_t)v + 1] = (int32_t)total;  // missing lines
+    if (total > m2) throw gu_error(GU_ERR_INVALID_ARGUMENT, "more METIS entries than twice the header's m");
+    g.C.resize((size_t)total);
+    parallel_for(parts.size(), [&](size_t i) {
+        std::memcpy(g.C.data() + c_off[i], parts[i].c.data(), sizeof(int32_t) * (size_t)keep[i]);
+        for (int64_t j = 0; j < keep[i]; ++j) {
+            const int32_t c = parts[i].c[(size_t)j];
+            if (c < 0 || c >= g.n) throw gu_error(GU_ERR_INVALID_ARGUMENT, "vertex id out of range");
+        }
+    });
     return g;
 }
 
+// SNAP: lines parsed by several threads over ranges of whole lines (each keeps
+// its edges in file order), the distinct ids marked in one shared bitset, the
+// ranges' edges joined in file order.
 HostGraph parse_snap(const std::vector<char> &buf)
 {
     HostGraph g;
     g.directed = true;
-    Fields fl;
-    std::vector<int32_t> F;
-    std::vector<uint64_t> seen;  // bitset of the ids met (dense 0..n-1 in valid files)
-    int64_t distinct = 0;
-    for_lines(buf, [&](const char *b, const char *e) {
-        if (b < e && *b == '#') return;
-        fl.split(b, e);
-        if (fl.f.empty()) return;
-        if (fl.f.size() < 2) throw gu_error(GU_ERR_INVALID_ARGUMENT, "edge list line with one field");
-        const long long u = to_int(fl.f[0].first, fl.f[0].second, "edge list");
-        const long long v = to_int(fl.f[1].first, fl.f[1].second, "edge list");
-        if (u < 0 || v < 0) throw gu_error(GU_ERR_INVALID_ARGUMENT, "negative vertex id");
-        for (long long x : {u, v}) {
-            const size_t w = (size_t)x >> 6;
-            if (w >= seen.size()) seen.resize(std::max(w + 1, seen.size() * 2), 0);
-            const uint64_t bit = 1ull << (x & 63);
-            if (!(seen[w] & bit)) {
-                seen[w] |= bit;
-                ++distinct;
+    struct Part {
+        std::vector<int32_t> u, v;
+        int32_t max_id = -1;
+    };
+    const auto ranges = line_ranges(buf.data(), buf.data() + buf.size(), reader_threads(), (size_t)1 << 20);
+    std::vector<Part> parts(ranges.size());
+    parallel_for(ranges.size(), [&](size_t i) {
+        Part &pt = parts[i];
+        Fields fl;
+        const char *q = ranges[i].first, *qe = ranges[i].second;
+        while (q < qe) {
+            const char *nl = static_cast<const char *>(std::memchr(q, '\n', (size_t)(qe - q)));
+            const char *le = nl ? nl : qe;
+            if (!(q < le && *q == '#')) {
+                fl.split(q, le);
+                if (!fl.f.empty()) {
+                    if (fl.f.size() < 2) throw gu_error(GU_ERR_INVALID_ARGUMENT, "edge list line with one field");
+                    const long long u = to_int(fl.f[0].first, fl.f[0].second, "edge list");
+                    const long long v = to_int(fl.f[1].first, fl.f[1].second, "edge list");
+                    if (u < 0 || v < 0) throw gu_error(GU_ERR_INVALID_ARGUMENT, "negative vertex id");
+                    pt.u.push_back((int32_t)u);
+                    pt.v.push_back((int32_t)v);
+                    pt.max_id = std::max(pt.max_id, (int32_t)std::max(u, v));
+                }
             }
+            q = nl ? nl + 1 : qe;
         }
-        F.push_back((int32_t)u);
-        g.C.push_back((int32_t)v);
     });
+    int32_t max_id = -1;
+    std::vector<size_t> off(parts.size() + 1, 0);
+    for (size_t i = 0; i < parts.size(); ++i) {
+        max_id = std::max(max_id, parts[i].max_id);
+        off[i + 1] = off[i] + parts[i].u.size();
+    }
+    // n = number of distinct ids (dense 0..n-1 in a valid file)
+    const size_t words = (size_t)(((int64_t)max_id + 64) / 64);
+    std::vector<std::atomic<uint64_t>> seen(words);
+    for (auto &w : seen) w.store(0, std::memory_order_relaxed);
+    parallel_for(parts.size(), [&](size_t i) {
+        for (const auto *a : {&parts[i].u, &parts[i].v})
+            for (const int32_t x : *a) {
+                const uint64_t bit = 1ull << (x & 63);
+                if (!(seen[(size_t)x >> 6].load(std::memory_order_relaxed) & bit))
+                    seen[(size_t)x >> 6].fetch_or(bit, std::memory_order_relaxed);
+            }
+    });
+    int64_t distinct = 0;
+    for (const auto &w : seen) distinct += __builtin_popcountll(w.load(std::memory_order_relaxed));
     if (distinct > 2147483647LL) throw gu_error(GU_ERR_INVALID_ARGUMENT, "too many vertices");
     g.n = (int32_t)distinct;
+    std::vector<int32_t> F(off.back());
+    g.C.resize(off.back());
+    parallel_for(parts.size(), [&](size_t i) {
+        std::memcpy(F.data() + off[i], parts[i].u.data(), sizeof(int32_t) * parts[i].u.size());
+        std::memcpy(g.C.data() + off[i], parts[i].v.data(), sizeof(int32_t) * parts[i].v.size());
+    });
     induce_offsets(F, g.n, g.R);
     check_columns(g.C, g.n);
     return g;
 }
 
+// MatrixMarket: the size line first, then the entry lines parsed by several
+// threads over ranges of whole lines, joined in file order; both directions of
+// every entry, counting-sorted by row and each row's columns sorted.
 HostGraph parse_market(const std::vector<char> &buf)
 {
     HostGraph g;
     g.directed = false;
     Fields fl;
-    bool first = true;
-    std::vector<std::pair<int32_t, int32_t>> e2;
-    for_lines(buf, [&](const char *b, const char *e) {
-        if (b < e && *b == '%') return;
-        fl.split(b, e);
-        if (first) {
+    const char *p = buf.data(), *end = buf.data() + buf.size();
+    bool have_size = false;
+    while (p < end && !have_size) {
+        const char *nl = static_cast<const char *>(std::memchr(p, '\n', (size_t)(end - p)));
+        const char *le = nl ? nl : end;
+        if (!(p < le && *p == '%')) {
+            fl.split(p, le);
             if (fl.f.size() != 3) throw gu_error(GU_ERR_INVALID_ARGUMENT, "MatrixMarket size line must be: rows cols nnz");
             const long long n = to_int(fl.f[0].first, fl.f[0].second, "MatrixMarket size line");
             const long long nnz = to_int(fl.f[2].first, fl.f[2].second, "MatrixMarket size line");
             if (n < 0 || nnz < 0) throw gu_error(GU_ERR_INVALID_ARGUMENT, "negative size in MatrixMarket size line");
             g.n = (int32_t)n;
-            e2.reserve((size_t)nnz * 2);
-            first = false;
-            return;
+            have_size = true;
         }
-        if (fl.f.size() != 2) throw gu_error(GU_ERR_INVALID_ARGUMENT, "only pattern MatrixMarket entries (u v) are accepted");
-        const int32_t u = (int32_t)(to_int(fl.f[0].first, fl.f[0].second, "MatrixMarket entry") - 1);
-        const int32_t v = (int32_t)(to_int(fl.f[1].first, fl.f[1].second, "MatrixMarket entry") - 1);
-        e2.emplace_back(u, v);
-        e2.emplace_back(v, u);
+        p = nl ? nl + 1 : end;
+    }
+    if (!have_size) throw gu_error(GU_ERR_INVALID_ARGUMENT, "MatrixMarket file has no size line");
+    const auto ranges = line_ranges(p, end, reader_threads(), (size_t)1 << 20);
+    std::vector<std::vector<std::pair<int32_t, int32_t>>> parts(ranges.size());
+    parallel_for(ranges.size(), [&](size_t i) {
+        Fields f;
+        const char *q = ranges[i].first, *qe = ranges[i].second;
+        while (q < qe) {
+            const char *nl = static_cast<const char *>(std::memchr(q, '\n', (size_t)(qe - q)));
+            const char *le = nl ? nl : qe;
+            if (!(q < le && *q == '%')) {
+                f.split(q, le);
+                if (f.f.size() != 2)
+                    throw gu_error(GU_ERR_INVALID_ARGUMENT, "only pattern MatrixMarket entries (u v) are accepted");
+                const int32_t u = (int32_t)(to_int(f.f[0].first, f.f[0].second, "MatrixMarket entry") - 1);
+                const int32_t v = (int32_t)(to_int(f.f[1].first, f.f[1].second, "MatrixMarket entry") - 1);
+                if (u < 0 || u >= g.n || v < 0 || v >= g.n)
+                    throw gu_error(GU_ERR_INVALID_ARGUMENT, "vertex id out of range");
+                parts[i].emplace_back(u, v);
+            }
+            q = nl ? nl + 1 : qe;
+        }
     });
-    if (first) throw gu_error(GU_ERR_INVALID_ARGUMENT, "MatrixMarket file has no size line");
     // entries in (row, column) order, as the reference's sort of the pairs leaves
     // them: a counting sort by row, then each row's columns sorted
-    for (const auto &p : e2)
-        if (p.first < 0 || p.first >= g.n || p.second < 0 || p.second >= g.n)
-            throw gu_error(GU_ERR_INVALID_ARGUMENT, "vertex id out of range");
     g.R.assign((size_t)g.n + 1, 0);
-    for (const auto &p : e2) g.R[(size_t)p.first + 1]++;
+    for (const auto &pt : parts)
+        for (const auto &e : pt) {
+            g.R[(size_t)e.first + 1]++;
+            g.R[(size_t)e.second + 1]++;
+        }
     for (int32_t v = 0; v < g.n; ++v) g.R[(size_t)v + 1] += g.R[(size_t)v];
-    g.C.resize(e2.size());
+    g.C.resize((size_t)g.R[(size_t)g.n]);
     std::vector<int32_t> fill(g.R.begin(), g.R.end() - 1);
-    for (const auto &p : e2) g.C[(size_t)fill[(size_t)p.first]++] = p.second;
-    for (int32_t v = 0; v < g.n; ++v) std::sort(g.C.begin() + g.R[(size_t)v], g.C.begin() + g.R[(size_t)v + 1]);
+    for (const auto &pt : parts)
+        for (const auto &e : pt) {
+            g.C[(size_t)fill[(size_t)e.first]++] = e.second;
+            g.C[(size_t)fill[(size_t)e.second]++] = e.first;
+        }
+    const unsigned nt = reader_threads();
+    parallel_for(nt, [&](size_t t) {
+        for (int64_t v = (int64_t)t; v < g.n; v += nt)
+            std::sort(g.C.begin() + g.R[(size_t)v], g.C.begin() + g.R[(size_t)v + 1]);
+    });
     return g;
 }
 
