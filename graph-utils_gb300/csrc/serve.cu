@@ -108,7 +108,7 @@ public:
         page_ = (size_t)sysconf(_SC_PAGESIZE);
         if (page_ < 4096) page_ = 4096;
         const unsigned hw = std::thread::hardware_concurrency();
-        const int nt = (int)std::max(1u, std::min(8u, hw / 2));
+        const int nt = (int)std::max(1u, std::min(12u, hw > 4 ? hw - 4 : 1u));
         for (int i = 0; i < nt; ++i) touchers_.emplace_back([this] { touch_loop(); });
         worker_ = std::thread([this] { loop(); });
         copier_ = std::thread([this] { copy_loop(); });
