@@ -54,12 +54,14 @@ struct DeviceScope {
     }
 };
 
+// After launch_msbfs on the graph's workspace: waits for the launch and reads its
+// control block from the pinned copy the launch queued behind its kernel.
 static void check_dev_status(DeviceGraph &g, cudaStream_t stream)
 {
     GU_CUDA_CHECK(cudaStreamSynchronize(stream));
     GU_CUDA_CHECK(cudaGetLastError());
     int err = 0;
-    msbfs_read_status(g, &err, nullptr, nullptr, nullptr);
+    msbfs_status_after_sync(g, &err, nullptr, nullptr, nullptr);
     if (err == DEV_ERR_BARRIER_TIMEOUT) throw gu_error(GU_ERR_TIMEOUT, "a device-side wait exceeded its limit");
     if (err == DEV_ERR_BAD_SOURCE) throw gu_error(GU_ERR_INVALID_ARGUMENT, "source vertex out of range");
     if (err != 0) throw gu_error(GU_ERR_INTERNAL, "device reported error code " + std::to_string(err));

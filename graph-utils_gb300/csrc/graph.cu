@@ -82,6 +82,7 @@ DeviceGraph::~DeviceGraph()
         if (ring_start[i]) cudaEventDestroy(ring_start[i]);
         if (ring_stop[i]) cudaEventDestroy(ring_stop[i]);
     }
+    if (ctl_host) cudaFreeHost(ctl_host);
     if (copy_st) cudaStreamDestroy(copy_st);
     ws.release();
     io.release();

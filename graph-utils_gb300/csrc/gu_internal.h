@@ -127,6 +127,7 @@ struct DeviceGraph {
         float alpha = 2.f, beta = 24.f;
         int words = 0;
     } tune;
+    void *ctl_host = nullptr;  // pinned copy of the batched engine's control block, written after each launch
     int32_t *ell = nullptr;  // low-degree graphs: neighbours padded to ell_width per vertex (-1), built on first use
     int ell_width = 0;
     // bottom-up degree classes by in-degree, each ascending: light (1 ..
@@ -224,6 +225,9 @@ int64_t server_submit(Server *s, int kind, DeviceGraph *g, const int32_t *src, i
 gu_status server_wait(Server *s, int64_t id, double timeout, double *latency, std::string &err);
 void server_stats(Server *s, int64_t *completed, int64_t *batches, double *p50, double *p99, double *mean_batch);
 void msbfs_read_status(DeviceGraph &g, int *dev_err, int *td_levels, int *bu_levels, int *max_level);
+// The same, from the pinned copy launch_msbfs queued after its kernel (valid once
+// the launch's stream is synchronised; the launch used the graph's workspace).
+void msbfs_status_after_sync(DeviceGraph &g, int *dev_err, int *td_levels, int *bu_levels, int *max_level);
 void ensure_coo(DeviceGraph &g, cudaStream_t stream);
 int device_sm_count(int device);
 

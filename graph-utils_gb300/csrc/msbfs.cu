@@ -1850,6 +1850,23 @@ void launch_msbfs(DeviceGraph &g, const int32_t *sources, int32_t k, int32_t *di
     default: throw gu_error(GU_ERR_INVALID_ARGUMENT, "unknown BFS variant");
     }
     if (opt.timed) g.mark_stop(stream);
+    if (&wsp == &g.ws) {  // the control block comes back with the launch: one round trip per call
+        if (!g.ctl_host) GU_CUDA_CHECK(cudaHostAlloc(&g.ctl_host, sizeof(MsCtl), cudaHostAllocDefault));
+        GU_CUDA_CHECK(cudaMemcpyAsync(g.ctl_host, a.ctl, sizeof(MsCtl), cudaMemcpyDeviceToHost, stream));
+    }
+}
+
+void msbfs_status_after_sync(DeviceGraph &g, int *dev_err, int *td_levels, int *bu_levels, int *max_level)
+{
+    if (!g.ctl_host) {
+        msbfs_read_status(g, dev_err, td_levels, bu_levels, max_level);
+        return;
+    }
+    const MsCtl &c = *static_cast<const MsCtl *>(g.ctl_host);
+    if (dev_err) *dev_err = c.err;
+    if (td_levels) *td_levels = c.td_levels;
+    if (bu_levels) *bu_levels = c.bu_levels;
+    if (max_level) *max_level = c.max_level;
 }
 
 // Device error word of a launch that used workspace `ws` (after its stream is synchronised).
