@@ -24,6 +24,8 @@ namespace gu {
 constexpr int LBS_THREADS = 512;
 constexpr int LBS_ITEMS = 8;
 constexpr int LBS_TILE = LBS_THREADS * LBS_ITEMS;  // counts per scan tile / diagonals per search tile
+constexpr int LBS_STHREADS = 256;                  // search CTA: fewer threads, more CTAs resident per SM
+constexpr int LBS_SITEMS = LBS_TILE / LBS_STHREADS;  // merge steps per search thread
 
 __device__ __forceinline__ long long block_reduce_ll(long long x, long long *s_warp)
 {
@@ -161,13 +163,13 @@ __global__ void lbs_partition(const int32_t *__restrict__ scanned, int32_t N, lo
     kpart[t] = merge_path(scanned, N, total, min(t * LBS_TILE, total + N));
 }
 
-__global__ void __launch_bounds__(LBS_THREADS) lbs_search(const int32_t *__restrict__ scanned, int32_t N,
+__global__ void __launch_bounds__(LBS_STHREADS) lbs_search(const int32_t *__restrict__ scanned, int32_t N,
                                                           long long total, const int32_t *__restrict__ kpart,
                                                           int32_t *__restrict__ result)
 {
     __shared__ int32_t s_b[LBS_TILE + 1];
-    // owners by slot, one padding word per 32: thread t writes slots 8t.. (a stride of 8
-    // words across the warp), which unpadded would hit 4 banks
+    // owners by slot, one padding word per 32: thread t writes slots 16t.. (a stride of
+    // 16 words across the warp), which unpadded would hit 2 banks
     __shared__ int32_t s_out[LBS_TILE + LBS_TILE / 32];
     const long long d0 = (long long)blockIdx.x * LBS_TILE;
     const long long d1 = min(d0 + LBS_TILE, total + N);
@@ -176,8 +178,8 @@ __global__ void __launch_bounds__(LBS_THREADS) lbs_search(const int32_t *__restr
     const int nb = k1 - k0;
     for (int t = threadIdx.x; t < nb; t += blockDim.x) s_b[t] = scanned[k0 + t];
     __syncthreads();
-    // this thread's diagonal, then LBS_ITEMS merge steps
-    const long long dt = min(d0 + (long long)threadIdx.x * LBS_ITEMS, d1) - d0;
+    // this thread's diagonal, then LBS_SITEMS merge steps
+    const long long dt = min(d0 + (long long)threadIdx.x * LBS_SITEMS, d1) - d0;
     long long lo = dt > (i1 - i0) ? dt - (i1 - i0) : 0, hi = dt < nb ? dt : nb;
     while (lo < hi) {
         const long long k = (lo + hi) >> 1;
@@ -186,7 +188,7 @@ __global__ void __launch_bounds__(LBS_THREADS) lbs_search(const int32_t *__restr
     }
     int kk = (int)lo;
     long long ii = i0 + (dt - lo);
-    for (int step = 0; step < LBS_ITEMS && (ii - i0) + kk < (i1 - i0) + nb; ++step) {
+    for (int step = 0; step < LBS_SITEMS && (ii - i0) + kk < (i1 - i0) + nb; ++step) {
         const bool take_slot = kk >= nb || ii < (long long)s_b[kk];
         if (take_slot) {
             if (ii >= i1) break;
@@ -255,7 +257,7 @@ void launch_lbs(const int32_t *counts, int32_t N, int32_t *scanned, int32_t *res
         const int32_t nsearch = (int32_t)((ndiag + LBS_TILE - 1) / LBS_TILE);
         if (tot > 0) {
             lbs_partition<<<(nsearch + 1 + 255) / 256, 256, 0, st>>>(scanned, N, tot, nsearch, kpart);
-            lbs_search<<<nsearch, LBS_THREADS, 0, st>>>(scanned, N, tot, kpart, result);
+            lbs_search<<<nsearch, LBS_STHREADS, 0, st>>>(scanned, N, tot, kpart, result);
         }
         GU_CUDA_CHECK(cudaGetLastError());
     }
