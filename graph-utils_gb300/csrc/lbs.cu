@@ -11,13 +11,18 @@
 //   2. search: merge-path partition (the merge of slot keys 0..total-1 with the
 //      scanned offsets, ties to the offsets) into equal diagonals of 4096; the
 //      tiles' path endpoints are found by binary search in one pass (a thread
-//      per endpoint), then a CTA per tile stages its offsets in shared memory,
-//      every thread merges 8 steps from its own diagonal, and the CTA writes its
-//      run of owners contiguously.
+//      per endpoint), then each search CTA takes tiles in turn, stages their
+//      offsets in shared memory, every thread merges 16 steps from its own
+//      diagonal, and the CTA writes its run of owners contiguously.
+//   The scan of the tile sums also checks the call (negative counts, int32
+//   overflow, result capacity) on the device, so all kernels are queued at once
+//   and the host waits once, at the end.
 // race_and_resolve (race_and_resolve.cuh:13-25) is exposed as a warp-level
 // kernel over an array of predicates for testing the device primitive.
 #include "device_utils.cuh"
 #include "gu_internal.h"
+
+#include <algorithm>
 
 namespace gu {
 
@@ -94,9 +99,15 @@ __global__ void __launch_bounds__(LBS_THREADS) lbs_tile_sums(const int32_t *__re
     if (threadIdx.x == 0) tile_sum[blockIdx.x] = tot;
 }
 
-// one CTA: exclusive scan of the tile sums in chunks of blockDim; last entry = total
+// one CTA: exclusive scan of the tile sums in chunks of blockDim; last entry = total.
+// It also decides on the device whether the search may run (no negative count,
+// total within int32 and within the result capacity, a result buffer when the
+// total is positive) -- the later kernels read the verdict, so the call needs no
+// host round trip before them -- and writes the int32 total when it may.
 __global__ void __launch_bounds__(LBS_THREADS) lbs_scan_tiles(long long *__restrict__ tile_sum, int32_t ntiles,
-                                                              long long *__restrict__ total)
+                                                              long long *__restrict__ total, const int *neg,
+                                                              long long capacity, int has_result, int *ok,
+                                                              int32_t *total_out)
 {
     __shared__ long long s_warp[33];
     long long carry = 0;
@@ -108,7 +119,12 @@ __global__ void __launch_bounds__(LBS_THREADS) lbs_scan_tiles(long long *__restr
         if (i < ntiles) tile_sum[i] = carry + ex;
         carry += tot;
     }
-    if (threadIdx.x == 0) *total = carry;
+    if (threadIdx.x == 0) {
+        *total = carry;
+        const bool good = *neg == 0 && carry <= INT32_MAX && carry <= capacity && (carry == 0 || has_result);
+        *ok = good ? 1 : 0;
+        if (good && total_out) *total_out = (int32_t)carry;
+    }
 }
 
 // rescan each tile with its offset; counts are read in blocked order (thread t
@@ -155,52 +171,64 @@ __device__ __forceinline__ int32_t merge_path(const int32_t *B, int32_t N, long 
 // boundary d = t * LBS_TILE (the last one at total + N).  Done inside each
 // search CTA, the 20-odd dependent global loads of the binary search were most
 // of the kernel's time.
-__global__ void lbs_partition(const int32_t *__restrict__ scanned, int32_t N, long long total, int32_t ntile,
-                              int32_t *__restrict__ kpart)
+__global__ void lbs_partition(const int32_t *__restrict__ scanned, int32_t N, const long long *total_p,
+                              const int *ok, int32_t *__restrict__ kpart)
 {
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t > ntile) return;
-    kpart[t] = merge_path(scanned, N, total, min(t * LBS_TILE, total + N));
+    if (!*ok) return;
+    const long long total = *total_p;
+    if (total == 0) return;
+    const long long ntile = (total + N + LBS_TILE - 1) / LBS_TILE;
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t <= ntile;
+         t += (long long)gridDim.x * blockDim.x)
+        kpart[t] = merge_path(scanned, N, total, min(t * LBS_TILE, total + N));
 }
 
 __global__ void __launch_bounds__(LBS_STHREADS) lbs_search(const int32_t *__restrict__ scanned, int32_t N,
-                                                          long long total, const int32_t *__restrict__ kpart,
-                                                          int32_t *__restrict__ result)
+                                                           const long long *total_p, const int *ok,
+                                                           const int32_t *__restrict__ kpart,
+                                                           int32_t *__restrict__ result)
 {
     __shared__ int32_t s_b[LBS_TILE + 1];
     // owners by slot, one padding word per 32: thread t writes slots 16t.. (a stride of
     // 16 words across the warp), which unpadded would hit 2 banks
     __shared__ int32_t s_out[LBS_TILE + LBS_TILE / 32];
-    const long long d0 = (long long)blockIdx.x * LBS_TILE;
-    const long long d1 = min(d0 + LBS_TILE, total + N);
-    const int32_t k0 = __ldg(kpart + blockIdx.x), k1 = __ldg(kpart + blockIdx.x + 1);
-    const long long i0 = d0 - k0, i1 = d1 - k1;  // slots [i0, i1) of this tile
-    const int nb = k1 - k0;
-    for (int t = threadIdx.x; t < nb; t += blockDim.x) s_b[t] = scanned[k0 + t];
-    __syncthreads();
-    // this thread's diagonal, then LBS_SITEMS merge steps
-    const long long dt = min(d0 + (long long)threadIdx.x * LBS_SITEMS, d1) - d0;
-    long long lo = dt > (i1 - i0) ? dt - (i1 - i0) : 0, hi = dt < nb ? dt : nb;
-    while (lo < hi) {
-        const long long k = (lo + hi) >> 1;
-        if ((long long)s_b[k] <= i0 + (dt - k) - 1) lo = k + 1;
-        else hi = k;
-    }
-    int kk = (int)lo;
-    long long ii = i0 + (dt - lo);
-    for (int step = 0; step < LBS_SITEMS && (ii - i0) + kk < (i1 - i0) + nb; ++step) {
-        const bool take_slot = kk >= nb || ii < (long long)s_b[kk];
-        if (take_slot) {
-            if (ii >= i1) break;
-            const int o = (int)(ii - i0);
-            s_out[o + (o >> 5)] = k0 + kk - 1;
-            ++ii;
-        } else {
-            ++kk;
+    if (!*ok) return;
+    const long long total = *total_p;
+    if (total == 0) return;  // no slots; the path endpoints were not written
+    const long long ntile = (total + N + LBS_TILE - 1) / LBS_TILE;
+    for (long long tile = blockIdx.x; tile < ntile; tile += gridDim.x) {  // block-uniform
+        const long long d0 = tile * LBS_TILE;
+        const long long d1 = min(d0 + LBS_TILE, total + N);
+        const int32_t k0 = __ldg(kpart + tile), k1 = __ldg(kpart + tile + 1);
+        const long long i0 = d0 - k0, i1 = d1 - k1;  // slots [i0, i1) of this tile
+        const int nb = k1 - k0;
+        for (int t = threadIdx.x; t < nb; t += blockDim.x) s_b[t] = scanned[k0 + t];
+        __syncthreads();
+        // this thread's diagonal, then LBS_SITEMS merge steps
+        const long long dt = min(d0 + (long long)threadIdx.x * LBS_SITEMS, d1) - d0;
+        long long lo = dt > (i1 - i0) ? dt - (i1 - i0) : 0, hi = dt < nb ? dt : nb;
+        while (lo < hi) {
+            const long long k = (lo + hi) >> 1;
+            if ((long long)s_b[k] <= i0 + (dt - k) - 1) lo = k + 1;
+            else hi = k;
         }
+        int kk = (int)lo;
+        long long ii = i0 + (dt - lo);
+        for (int step = 0; step < LBS_SITEMS && (ii - i0) + kk < (i1 - i0) + nb; ++step) {
+            const bool take_slot = kk >= nb || ii < (long long)s_b[kk];
+            if (take_slot) {
+                if (ii >= i1) break;
+                const int o = (int)(ii - i0);
+                s_out[o + (o >> 5)] = k0 + kk - 1;
+                ++ii;
+            } else {
+                ++kk;
+            }
+        }
+        __syncthreads();
+        for (int i = threadIdx.x; i < (int)(i1 - i0); i += blockDim.x) result[i0 + i] = s_out[i + (i >> 5)];
+        __syncthreads();  // s_b and s_out are reused by the next tile
     }
-    __syncthreads();
-    for (int i = threadIdx.x; i < (int)(i1 - i0); i += blockDim.x) result[i0 + i] = s_out[i + (i >> 5)];
 }
 
 // Winner lane per warp of 32 predicates (race_and_resolve_warp).
@@ -232,18 +260,32 @@ void launch_lbs(const int32_t *counts, int32_t N, int32_t *scanned, int32_t *res
     long long *tile = reinterpret_cast<long long *>(scratch_ptr);
     long long *tot_d = tile + ntiles;
     int *neg_d = reinterpret_cast<int *>(tot_d + 1);
+    int *ok_d = neg_d + 1;
     int32_t *kpart = reinterpret_cast<int32_t *>(reinterpret_cast<char *>(tile) + (ntiles + 2) * sizeof(long long) + 256);
+    // every kernel is queued at once; the scan-of-tile-sums kernel decides whether
+    // the search may run, and the host checks the same conditions after one wait
     long long tot = 0;
     int neg = 0;
+    const long long cap = result_capacity < 0 ? 0 : (result_capacity > INT32_MAX ? INT32_MAX : result_capacity);
     if (N > 0) {
         GU_CUDA_CHECK(cudaMemsetAsync(neg_d, 0, sizeof(int), st));
         lbs_tile_sums<<<ntiles, LBS_THREADS, 0, st>>>(counts, N, tile, neg_d);
-        lbs_scan_tiles<<<1, LBS_THREADS, 0, st>>>(tile, ntiles, tot_d);
+        lbs_scan_tiles<<<1, LBS_THREADS, 0, st>>>(tile, ntiles, tot_d, neg_d, result_capacity, result ? 1 : 0, ok_d,
+                                                  total_dev);
+        lbs_scan_write<<<ntiles, LBS_THREADS, 0, st>>>(counts, N, tile, scanned);
+        // grids sized by the capacity bound, capped; both loop over the tiles the total needs
+        const long long nsearch_max = (cap + N + LBS_TILE - 1) / LBS_TILE;
+        const int gpart = (int)std::min<long long>((nsearch_max + 1 + 255) / 256, 1024);
+        const int gsearch = (int)std::min<long long>(std::max<long long>(nsearch_max, 1), 4096);
+        lbs_partition<<<gpart, 256, 0, st>>>(scanned, N, tot_d, ok_d, kpart);
+        lbs_search<<<gsearch, LBS_STHREADS, 0, st>>>(scanned, N, tot_d, ok_d, kpart, result);
         GU_CUDA_CHECK(cudaGetLastError());
         GU_CUDA_CHECK(cudaMemcpyAsync(&tot, tot_d, sizeof(long long), cudaMemcpyDeviceToHost, st));
         GU_CUDA_CHECK(cudaMemcpyAsync(&neg, neg_d, sizeof(int), cudaMemcpyDeviceToHost, st));
-        GU_CUDA_CHECK(cudaStreamSynchronize(st));
+    } else if (total_dev) {
+        GU_CUDA_CHECK(cudaMemsetAsync(total_dev, 0, sizeof(int32_t), st));
     }
+    GU_CUDA_CHECK(cudaStreamSynchronize(st));
     if (total_host) *total_host = tot;
     if (neg) throw gu_error(GU_ERR_INVALID_ARGUMENT, "work counts must be >= 0");
     if (tot > INT32_MAX) throw gu_error(GU_ERR_OVERFLOW, "total work exceeds INT32_MAX (int32 scanned offsets)");
@@ -251,21 +293,6 @@ void launch_lbs(const int32_t *counts, int32_t N, int32_t *scanned, int32_t *res
         throw gu_error(GU_ERR_CAPACITY, "result buffer holds " + std::to_string(result_capacity) + " slots, need " +
                                             std::to_string(tot));
     if (tot > 0 && !result) throw gu_error(GU_ERR_INVALID_ARGUMENT, "null result");
-    if (N > 0) {
-        lbs_scan_write<<<ntiles, LBS_THREADS, 0, st>>>(counts, N, tile, scanned);
-        const long long ndiag = tot + N;
-        const int32_t nsearch = (int32_t)((ndiag + LBS_TILE - 1) / LBS_TILE);
-        if (tot > 0) {
-            lbs_partition<<<(nsearch + 1 + 255) / 256, 256, 0, st>>>(scanned, N, tot, nsearch, kpart);
-            lbs_search<<<nsearch, LBS_STHREADS, 0, st>>>(scanned, N, tot, kpart, result);
-        }
-        GU_CUDA_CHECK(cudaGetLastError());
-    }
-    if (total_dev) {
-        const int32_t t32 = (int32_t)tot;
-        GU_CUDA_CHECK(cudaMemcpyAsync(total_dev, &t32, sizeof(int32_t), cudaMemcpyHostToDevice, st));
-    }
-    GU_CUDA_CHECK(cudaStreamSynchronize(st));
 }
 
 void launch_race_and_resolve(const int32_t *pred, int32_t nwarps, int32_t *winner, cudaStream_t st)
