@@ -420,6 +420,7 @@ static void bfs_device(DeviceGraph &g, int variant, const int32_t *sources_dev, 
             opt.alpha = g.tune.alpha;
             opt.beta = g.tune.beta;
             opt.batch_words = g.tune.words;
+            opt.tuned = true;
         }
     } else if (variant == GU_BFS_AUTO) {
         const AutoEngine eng = auto_engine(g, true);

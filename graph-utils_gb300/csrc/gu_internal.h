@@ -169,6 +169,7 @@ struct MsOptions {
     // bottom-up levels expand top-down the sources that fewer than this fraction
     // of the CTAs discovered in the previous level (0: none)
     float rare_frac = 1.f / 3.f;
+    bool tuned = false;  // alpha, beta, words come from the graph's tuning: the GU_MS_* variables do not apply
     Workspace *ws = nullptr;  // scratch to use (default: the graph's)
     int max_blocks = 0;       // cap on the persistent grid (0: the whole GPU)
     bool timed = true;        // record the graph's launch events

@@ -1826,8 +1826,8 @@ void launch_msbfs(DeviceGraph &g, const int32_t *sources, int32_t k, int32_t *di
         a.qoff[i] = reinterpret_cast<int32_t *>(p);
         p += i32_bytes;
     }
-    a.alpha = env_float("GU_MS_ALPHA", opt.alpha);
-    a.beta = env_float("GU_MS_BETA", opt.beta);
+    a.alpha = opt.tuned ? opt.alpha : env_float("GU_MS_ALPHA", opt.alpha);
+    a.beta = opt.tuned ? opt.beta : env_float("GU_MS_BETA", opt.beta);
     a.gamma = env_float("GU_MS_GAMMA", opt.gamma);
     a.rare_frac = env_float("GU_MS_RARE", opt.rare_frac);
     int degbits = 1;
