@@ -16,6 +16,8 @@
 //
 // Binary files are little-endian raw arrays; a CSR prefix P names P.R (int32
 // n+1), P.C (int32 m) and P.meta (text: "n m directed").
+#include <chrono>
+#include <climits>
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
@@ -94,7 +96,8 @@ int main(int argc, char **argv)
                 "usage: ref_oracle parse <file> <format> <out_prefix>\n"
                 "       ref_oracle run <csr_prefix> <sources.i32> <out_prefix>\n"
                 "       ref_oracle lbs <counts.i32> <out_prefix>\n"
-                "       ref_oracle dag <csr_prefix> <out_prefix>\n");
+                "       ref_oracle dag <csr_prefix> <out_prefix>\n"
+                "       ref_oracle time_bfs <csr_prefix> <sources.i32>\n");
         return 2;
     }
     std::string mode = argv[1];
@@ -139,6 +142,25 @@ int main(int argc, char **argv)
         write_vec(out + ".delta_f32", delta);
         std::vector<int> dv(1, diam);
         write_vec(out + ".diameter", dv);
+        return 0;
+    }
+    if (mode == "time_bfs" && argc == 4) {
+        // The reference's BFS checker, one source after another on one thread;
+        // prints the seconds spent inside it and the CSR entries its searches
+        // scanned (the adjacency of every reached vertex).
+        host_graph g = read_csr(argv[2]);
+        std::vector<int> sources = read_vec<int>(argv[3]);
+        double secs = 0;
+        long long scanned = 0;
+        for (int src : sources) {
+            std::vector<int> d;
+            const auto t0 = std::chrono::steady_clock::now();
+            ms_sequential(g, src, d);
+            secs += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+            for (int v = 0; v < g.n; ++v)
+                if (d[v] != INT_MAX) scanned += g.R[v + 1] - g.R[v];
+        }
+        printf("%.6f %lld\n", secs, scanned);
         return 0;
     }
     if (mode == "lbs" && argc == 4) {
