@@ -265,8 +265,9 @@ gu_status gu_dag_reach(gu_graph g, int64_t *counts_dev, int64_t *total_pairs, vo
  * result_dev[j] for every work slot j < total = the item that owns it
  * (upper_bound(scanned, j) - 1).  The total is returned in *total_host and/or
  * *total_dev (either may be NULL).  GU_ERR_OVERFLOW if the total exceeds
- * INT32_MAX, GU_ERR_CAPACITY if it exceeds result_capacity (nothing written to
- * result then).  Replaces extract_edges_{warp,block} / load_balance_search_{warp,
+ * INT32_MAX, GU_ERR_CAPACITY if it exceeds result_capacity, GU_ERR_INVALID_ARGUMENT
+ * for a negative count: result_dev and *total_dev are not written then (the
+ * checks run on the device, so scanned_dev may hold the prefix sums).  Replaces extract_edges_{warp,block} / load_balance_search_{warp,
  * block} (load_balanced_search.cuh:10-13, load_balanced_search.cu:63-202). */
 gu_status gu_lbs(const int32_t *counts_dev, int32_t N, int32_t *scanned_dev, int32_t *result_dev,
                  int64_t result_capacity, int32_t *total_dev, int64_t *total_host, void *stream);
