@@ -70,6 +70,15 @@ def test_lbs_errors():
     with pytest.raises(gu.GuError) as e:
         run_lbs(np.array([3, -1, 4], np.int32), capacity=6)
     assert e.value.status == 1
+    # a rejected call leaves the result slots and the device total as they were
+    for counts, cap in ((np.full(10, 5, np.int32), 20), (np.array([3, -1, 4], np.int32), 6)):
+        c = torch.as_tensor(counts, device="cuda")
+        sc = torch.empty_like(c)
+        res = torch.full((cap,), -7, dtype=torch.int32, device="cuda")
+        tot = torch.full((1,), -9, dtype=torch.int32, device="cuda")
+        with pytest.raises(gu.GuError):
+            gu.lbs(c, sc, res, total_dev=tot)
+        assert bool((res == -7).all()) and int(tot.item()) == -9
     # no items
     c = torch.zeros(0, dtype=torch.int32, device="cuda")
     assert gu.lbs(c, torch.zeros(1, dtype=torch.int32, device="cuda"), torch.zeros(0, dtype=torch.int32,
