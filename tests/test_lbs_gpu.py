@@ -85,6 +85,40 @@ def test_lbs_errors():
                                                                                       device="cuda")) == 0
 
 
+def test_lbs_total_at_int32_max():
+    """The largest total the int32 offsets hold: 4096 items owning 2^31 - 1 slots
+    (an 8 GiB result).  Checked through size-independent properties: the scan is
+    exact, owners never decrease, each item owns exactly its count of slots and
+    its first slot sits at its offset.  One slot more overflows."""
+    N, per = 4096, 1 << 19
+    counts = np.full(N, per, np.int32)
+    c = torch.as_tensor(counts, device="cuda")
+    sc = torch.empty_like(c)
+    small = torch.full((16,), -7, dtype=torch.int32, device="cuda")
+    with pytest.raises(gu.GuError) as e:
+        gu.lbs(c, sc, small)  # total 2^31
+    assert e.value.status == 5 and bool((small == -7).all())
+    counts[-1] -= 1
+    c = torch.as_tensor(counts, device="cuda")
+    total = (1 << 31) - 1
+    res = torch.empty(total, dtype=torch.int32, device="cuda")
+    tdev = torch.zeros(1, dtype=torch.int32, device="cuda")
+    assert gu.lbs(c, sc, res, total_dev=tdev) == total
+    assert int(tdev.item()) == total
+    offs = torch.arange(N, device="cuda", dtype=torch.int64) * per
+    assert torch.equal(sc.to(torch.int64), offs)
+    assert torch.equal(res[offs].to(torch.int64), torch.arange(N, device="cuda", dtype=torch.int64))
+    owned = torch.zeros(N, dtype=torch.int64, device="cuda")
+    chunk = 1 << 28
+    for s0 in range(0, total, chunk):
+        part = res[s0:min(total, s0 + chunk + 1)]  # one slot of overlap for the order check
+        assert bool((part[1:] >= part[:-1]).all())
+        owned += torch.bincount(res[s0:min(total, s0 + chunk)].to(torch.int64), minlength=N)
+    assert torch.equal(owned, c.to(torch.int64))
+    del res
+    torch.cuda.empty_cache()
+
+
 def test_race_and_resolve_vs_oracle():
     rng = np.random.default_rng(5)
     nw = 4096
