@@ -207,6 +207,29 @@ def test_rmat20_full_size_certificates():
     np.testing.assert_array_equal(dist[sample].cpu().numpy(), ref)
 
 
+def test_rows_beyond_2_31_elements():
+    """2304 sources on R-MAT scale 20 (nine 256-source batches in one launch):
+    the distance rows hold 2.4 G elements (9.7 GB), so row offsets pass 2^31
+    elements.  Rows on both sides of that point, and the last row, equal the
+    oracle's; every source is at level 0 of its own row."""
+    hg = gu.HostGraph.rmat(20, 16, seed=1)
+    g = gu.Graph(hg)
+    k = 2304
+    assert k * hg.n > 2 ** 31
+    srcs = gu.sources(hg.n, k, seed=3)
+    dev = torch.device("cuda:0")
+    s = torch.as_tensor(srcs, device=dev)
+    dist = torch.empty((k, hg.n), dtype=torch.int32, device=dev)
+    g.bfs(s, dist, variant="auto")
+    assert bool((dist[torch.arange(k, device=dev), s.long()] == 0).all())
+    first_past = (2 ** 31) // hg.n  # the first row that starts beyond element 2^31
+    sample = [0, 255, 256, first_past - 1, first_past, first_past + 1, k - 1]
+    ref, _ = oracle.bfs_multi(hg.R, hg.C, hg.n, srcs[sample], nthreads=os.cpu_count() or 1)
+    np.testing.assert_array_equal(dist[sample].cpu().numpy(), ref)
+    del dist
+    torch.cuda.empty_cache()
+
+
 @pytest.mark.parametrize("shape", ["rmat", "grid"])
 def test_autotune_keeps_distances(shape):
     """gu_graph_autotune times the candidates on a sample and makes the fastest AUTO's
