@@ -5,6 +5,8 @@ the reference graph-utils checkers compiled from their sources (see
 tests/golden/make_golden.py).  These tests pin oracle/gu_oracle.c to them
 bit-for-bit before it is trusted as the parity checker of the CUDA path.
 """
+import os
+
 import numpy as np
 import pytest
 
@@ -154,3 +156,19 @@ def test_bc_threads_deterministic_and_close():
     c = oracle.bc(g["R"], g["C"], n, np.arange(n), nthreads=4)
     np.testing.assert_array_equal(b, c)
     np.testing.assert_allclose(a, b, rtol=1e-14)
+
+
+def test_port_speed_script_against_reference_checker():
+    """oracle/compare_speed.py, where the reference checkers were built here: the
+    port and the reference's own BFS checker scan the same CSR entries on the
+    benchmark graph's generator (small scale), and both rates are reported."""
+    import json
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    if not os.path.exists(os.path.join(root, "oracle", "_ref", "ref_oracle")):
+        pytest.skip("reference checkers not built (no reference tree)")
+    out = subprocess.run([sys.executable, os.path.join(root, "oracle", "compare_speed.py"), "--scale", "12",
+                          "--sources", "4"], check=True, capture_output=True, text=True).stdout
+    r = json.loads(out.strip().splitlines()[-1])
+    assert r["sources"] == 4 and r["reference_gteps"] > 0 and r["port_gteps"] > 0
