@@ -460,10 +460,19 @@ gu_status gu_graph_autotune(gu_graph g, const int32_t *sources_dev, int32_t k, g
         validate_sources_host(hs.data(), k, dg.n);
         const size_t row_bytes = (size_t)k * (size_t)dg.n * sizeof(int32_t);
         if (row_bytes > ((size_t)4 << 30)) throw gu_error(GU_ERR_INVALID_ARGUMENT, "sample too large: k x n x 4 > 4 GiB");
-        int32_t *rows = nullptr;
-        GU_CUDA_CHECK(cudaMalloc(reinterpret_cast<void **>(&rows), row_bytes ? row_bytes : 4));
-        cudaStream_t st = nullptr;
-        GU_CUDA_CHECK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+        struct Scratch {  // released on every exit, errors included
+            int32_t *rows = nullptr;
+            cudaStream_t st = nullptr;
+            ~Scratch()
+            {
+                if (st) cudaStreamDestroy(st);
+                if (rows) cudaFree(rows);
+            }
+        } scratch;
+        GU_CUDA_CHECK(cudaMalloc(reinterpret_cast<void **>(&scratch.rows), row_bytes ? row_bytes : 4));
+        GU_CUDA_CHECK(cudaStreamCreateWithFlags(&scratch.st, cudaStreamNonBlocking));
+        int32_t *const rows = scratch.rows;
+        const cudaStream_t st = scratch.st;
         std::vector<gu_tuning> cand;
         auto add = [&](int engine, float alpha, float beta, int words) {
             gu_tuning t;
@@ -515,12 +524,9 @@ gu_status gu_graph_autotune(gu_graph g, const int32_t *sources_dev, int32_t k, g
             }
         } catch (...) {
             dg.tune = saved;
-            cudaStreamDestroy(st);
-            cudaFree(rows);
             throw;
         }
-        GU_CUDA_CHECK(cudaStreamDestroy(st));
-        GU_CUDA_CHECK(cudaFree(rows));
+        GU_CUDA_CHECK(cudaStreamSynchronize(st));
         if (pick.seconds < 0) {
             dg.tune = saved;
             throw gu_error(GU_ERR_INTERNAL, "no candidate completed");
