@@ -33,7 +33,12 @@ sys.path.insert(0, os.path.join(ROOT, "graph-utils_gb300"))
 import numpy as np  # noqa: E402
 
 SCALE, EDGE_FACTOR, GRAPH_SEED, K_SOURCES, SOURCE_SEED = 20, 16, 1, 512, 2
-WORKLOAD = "rmat20_ef16_512src_bfs"
+WORKLOAD = "rmat20_ef16_512src_bfs"  # the default workload's name
+
+
+def workload_name(scale, k):
+    """rmat<scale>_ef16_<k>src_bfs: the default names the headline workload."""
+    return f"rmat{scale}_ef{EDGE_FACTOR}_{k}src_bfs"
 FALLBACK_HBM_GBS = 6800.0
 
 
@@ -233,9 +238,10 @@ def run_reference(args):
     line = {"impl": "reference", "metric": "multi-source BFS GTEPS", "value": value, "unit": "GTEPS",
             "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * T / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
-            "data": "synthetic", "config": {"workload": WORKLOAD, "scale": args.scale, "edge_factor": EDGE_FACTOR,
-                                            "sources": args.sources, "graph_seed": GRAPH_SEED,
-                                            "source_seed": SOURCE_SEED},
+            "data": "synthetic",
+            "config": {"workload": workload_name(args.scale, args.sources), "scale": args.scale,
+                       "edge_factor": EDGE_FACTOR, "sources": args.sources, "graph_seed": GRAPH_SEED,
+                       "source_seed": SOURCE_SEED},
             "cpu_baseline": {"value": value, "unit": "GTEPS", "cores": cores, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": "GTEPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -345,8 +351,8 @@ def run_ours(args):
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_total / args.steps,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
                 "data": "synthetic",
-                "config": {"workload": WORKLOAD, "scale": args.scale, "edge_factor": EDGE_FACTOR,
-                           "n": hg.n, "m_csr": hg.m, "sources": len(srcs), "graph_seed": GRAPH_SEED,
+                "config": {"workload": workload_name(args.scale, args.sources), "scale": args.scale,
+                           "edge_factor": EDGE_FACTOR, "n": hg.n, "m_csr": hg.m, "sources": len(srcs), "graph_seed": GRAPH_SEED,
                            "source_seed": SOURCE_SEED, "variant": args.variant,
                            "l2": "inputs larger than L2 (CSR 134 MB + 2 GiB distance rows per step)",
                            "edges_per_step": gteps_edges, "levels_td_bu_max": levels},
