@@ -172,3 +172,64 @@ def test_port_speed_script_against_reference_checker():
                           "--sources", "4"], check=True, capture_output=True, text=True).stdout
     r = json.loads(out.strip().splitlines()[-1])
     assert r["sources"] == 4 and r["reference_gteps"] > 0 and r["port_gteps"] > 0
+
+
+def _random_csr(rng, n, m, directed):
+    """Random simple graph as CSR (no self-loops, no duplicates; undirected graphs
+    symmetrised), neighbour order shuffled as a file parser may leave it."""
+    if n < 2 or m == 0:
+        return np.zeros(n + 1, np.int32), np.zeros(0, np.int32)
+    u = rng.integers(0, n, m)
+    v = rng.integers(0, n, m)
+    keep = u != v
+    u, v = u[keep], v[keep]
+    if not directed:
+        u, v = np.concatenate([u, v]), np.concatenate([v, u])
+    key = np.unique(u.astype(np.int64) * n + v)
+    u, v = (key // n).astype(np.int32), (key % n).astype(np.int32)
+    perm = rng.permutation(len(u))
+    order = np.argsort(u[perm], kind="stable")
+    u, v = u[perm][order], v[perm][order]
+    R = np.zeros(n + 1, np.int32)
+    np.add.at(R, u + 1, 1)
+    return np.cumsum(R).astype(np.int32), v
+
+
+def test_oracle_vs_reference_checkers_on_random_graphs(tmp_path):
+    """Where the reference checkers were built here: distances, sigma, FP32 deltas
+    and the diameter of the oracle equal the reference's own checkers
+    (multi_search_test.cu:17-38, shortest_paths.cu:11-39, bc.cu:11-57,
+    diameter_sampling_test.cu:9-38) bit for bit on seeded random graphs, directed
+    and undirected, from one vertex to a few hundred."""
+    import subprocess
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    ref = os.path.join(root, "oracle", "_ref", "ref_oracle")
+    if not os.path.exists(ref):
+        pytest.skip("reference checkers not built (no reference tree)")
+    rng = np.random.default_rng(20)
+    for case in range(16):
+        n = int(rng.choice([1, 2, 7, 40, 150, 300]))
+        directed = bool(case % 2)
+        m = int(rng.integers(0, 4 * n + 1))
+        R, C = _random_csr(rng, n, m, directed)
+        k = min(n, 6)
+        src = rng.choice(n, k, replace=False).astype(np.int32)
+        pre = str(tmp_path / f"g{case}")
+        R.tofile(pre + ".R")
+        C.tofile(pre + ".C")
+        with open(pre + ".meta", "w") as f:
+            f.write(f"{n} {len(C)} {int(directed)}\n")
+        src.tofile(pre + ".src")
+        subprocess.run([ref, "run", pre, pre + ".src", pre + ".out"], check=True)
+        dist = np.fromfile(pre + ".out.dist", np.int32).reshape(k, n)
+        sigma = np.fromfile(pre + ".out.sigma", np.uint64).reshape(k, n)
+        delta = np.fromfile(pre + ".out.delta_f32", np.float32).reshape(k, n)
+        diam = int(np.fromfile(pre + ".out.diameter", np.int32)[0])
+        d, _ = oracle.bfs_multi(R, C, n, src)
+        np.testing.assert_array_equal(d, dist, err_msg=f"case {case}")
+        _, sg = oracle.sigma_multi(R, C, n, src)
+        np.testing.assert_array_equal(sg, sigma, err_msg=f"case {case}")
+        for i, s in enumerate(src):
+            _, _, de = oracle.brandes(R, C, n, int(s), kind="f32")
+            np.testing.assert_array_equal(de.view(np.uint32), delta[i].view(np.uint32), err_msg=f"case {case}")
+        assert oracle.diameter(R, C, n, src) == diam, f"case {case}"
