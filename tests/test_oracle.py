@@ -233,3 +233,53 @@ def test_oracle_vs_reference_checkers_on_random_graphs(tmp_path):
             _, _, de = oracle.brandes(R, C, n, int(s), kind="f32")
             np.testing.assert_array_equal(de.view(np.uint32), delta[i].view(np.uint32), err_msg=f"case {case}")
         assert oracle.diameter(R, C, n, src) == diam, f"case {case}"
+
+
+def test_oracle_dag_and_lbs_vs_reference_on_random_inputs(tmp_path):
+    """Where the reference checkers were built here: reachable pairs of seeded random
+    DAGs equal get_reachability_dag's (dag_reachability.cpp:36-65), and the LBS
+    scan and owners of random ragged counts (zeros included) equal the reference
+    example's (examples/load_balanced_search/lbs.cu:18-31), bit for bit."""
+    import subprocess
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    ref = os.path.join(root, "oracle", "_ref", "ref_oracle")
+    if not os.path.exists(ref):
+        pytest.skip("reference checkers not built (no reference tree)")
+    rng = np.random.default_rng(21)
+    for case in range(10):
+        n = int(rng.choice([1, 3, 30, 200, 400]))
+        m = int(rng.integers(0, 3 * n + 1))
+        topo = rng.permutation(n)  # vertex topo[i] comes i-th in the order
+        a, b = rng.integers(0, n, m), rng.integers(0, n, m)
+        keep = a != b
+        lo, hi = np.minimum(a, b)[keep], np.maximum(a, b)[keep]
+        u, v = topo[lo], topo[hi]
+        if len(u):
+            key = np.unique(u.astype(np.int64) * n + v)
+            u, v = (key // n).astype(np.int32), (key % n).astype(np.int32)
+        R = np.zeros(n + 1, np.int32)
+        np.add.at(R, np.asarray(u, np.int64) + 1, 1)
+        R = np.cumsum(R).astype(np.int32)
+        C = np.asarray(v, np.int32)
+        pre = str(tmp_path / f"d{case}")
+        R.tofile(pre + ".R")
+        C.tofile(pre + ".C")
+        with open(pre + ".meta", "w") as f:
+            f.write(f"{n} {len(C)} 1\n")
+        subprocess.run([ref, "dag", pre, pre + ".out"], check=True)
+        pairs = int(np.fromfile(pre + ".out.pairs", np.int64)[0])
+        assert oracle.dag_reach_pairs(R, C, n) == pairs, f"dag case {case}"
+        assert oracle.dag_reach_counts(R, C, n)[1] == pairs, f"dag case {case}"
+    for case in range(8):
+        N = int(rng.choice([1, 5, 64, 700]))
+        counts = rng.integers(0, 11, N).astype(np.int32)
+        counts[rng.random(N) < 0.4] = 0
+        pre = str(tmp_path / f"l{case}")
+        counts.tofile(pre + ".counts")
+        subprocess.run([ref, "lbs", pre + ".counts", pre + ".out"], check=True)
+        scanned = np.fromfile(pre + ".out.scanned", np.int32)
+        result = np.fromfile(pre + ".out.result", np.int32)
+        s, r, t = oracle.lbs(counts)
+        assert t == int(counts.sum()) == len(result), f"lbs case {case}"
+        np.testing.assert_array_equal(s[:N], scanned, err_msg=f"lbs case {case}")
+        np.testing.assert_array_equal(r[:t], result, err_msg=f"lbs case {case}")
