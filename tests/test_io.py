@@ -130,3 +130,33 @@ def test_convert_tool(tmp_path, capsys):
     np.testing.assert_array_equal(h.R, ref["R"])
     np.testing.assert_array_equal(h.C, ref["C"])
     assert convert.main(["-i", src, "-f", "dimacs"]) == 1
+
+
+def test_multi_range_files_vs_reference_parser(tmp_path):
+    """Where the reference checkers were built here: files of several MB, which the
+    readers split into line ranges parsed by many threads, give the CSR the
+    reference parser gives (parse.cpp:115-441), in every format, with the METIS
+    quirks (double spaces, tabs, trailing blanks, '\\r') and unsorted SNAP lines."""
+    import subprocess
+    import make_golden as M
+    if not os.path.exists(M.REF_ORACLE):
+        pytest.skip("reference checkers not built (no reference tree)")
+    rng = np.random.default_rng(31)
+    g = gu.HostGraph.rmat(15, 16, seed=37)
+    d = gu.HostGraph.dag(1 << 17, 1 << 20, seed=41)
+    cases = [("metis", "graph", "dimacs", lambda p: M.write_metis(p, g.R, g.C, g.n, rng)),
+             ("snap", "txt", "edgelist", lambda p: M.write_snap(p, d.R, d.C, d.n, rng, True)),
+             ("market", "mtx", "market", lambda p: M.write_market(p, g.R, g.C, g.n, rng))]
+    for name, ext, fmt, writer in cases:
+        path = str(tmp_path / f"{name}.{ext}")
+        writer(path)
+        assert os.path.getsize(path) > (3 << 20), name  # several line ranges
+        pre = str(tmp_path / f"ref_{name}")
+        subprocess.run([M.REF_ORACLE, "parse", path, fmt, pre], check=True)
+        R, C, n, directed = M.read_csr(pre)
+        ours = gu.HostGraph.parse(path, fmt)
+        assert ours.n == n, name
+        np.testing.assert_array_equal(ours.R, R, err_msg=name)
+        np.testing.assert_array_equal(ours.C, C[: R[n]], err_msg=name)
+        if fmt != "market":
+            assert ours.directed == directed, name
