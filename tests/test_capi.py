@@ -124,3 +124,20 @@ def test_from_edges_matches_oracle_semantics():
     assert g.m == 2 * 4  # (0,1),(1,2),(2,0),(3,4); self loop and duplicates dropped
     d = oracle.bfs(g.R, g.C, g.n, 0)
     assert d.tolist() == [0, 1, 1, oracle.INF, oracle.INF, oracle.INF]
+
+
+def test_drop_in_header_compiles_and_links(tmp_path):
+    """include/graph_utils.hpp (the reference's signatures) compiles and links
+    against the library with g++, as a reference caller would build it; the GPU
+    tests run the resulting program."""
+    import subprocess
+    lib_dir = os.path.join(ROOT, "graph-utils_gb300", "lib")
+    if not os.path.exists(os.path.join(lib_dir, "libgu_gb300.so")):
+        pytest.skip("library not built")
+    cmd = ["g++", "-std=c++17", "-O1", "-Wall", "-I" + os.path.join(ROOT, "include"),
+           "-I" + os.path.join(ROOT, "oracle"), "-I/usr/local/cuda/include",
+           os.path.join(ROOT, "tests", "cpp", "shim_check.cpp"), "-x", "c", os.path.join(ROOT, "oracle", "gu_oracle.c"),
+           "-x", "none", "-L" + lib_dir, "-lgu_gb300", "-L/usr/local/cuda/lib64", "-lcudart", "-lpthread",
+           "-o", str(tmp_path / "shim_check")]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
