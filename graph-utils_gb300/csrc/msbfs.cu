@@ -1956,25 +1956,19 @@ __global__ void noalloc_validate_kernel(const int32_t *R, const int32_t *C, int3
     }
 }
 
-// Device address of the scratch array for the current device.  The host-side
-// name g_noalloc_scratch is only a stand-in: the address is looked up once per
-// device (with that device current) and cached.
+// Device address of the scratch array on the current device.  The host-side name
+// g_noalloc_scratch is only a stand-in, so the address is looked up with the
+// device current, on every call: a cached address would outlive a
+// cudaDeviceReset (which reloads the module and may place the array elsewhere).
+// The first call on a device loads the library's module there; make it before
+// any stream capture.  Later lookups are a host-side table search.
 static char *noalloc_scratch_for_current_device()
 {
-    static std::mutex mu;
-    static void *addr[128] = {};
-    int dev = 0;
-    GU_CUDA_CHECK(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= 128) throw gu_error(GU_ERR_UNSUPPORTED, "device ordinal out of range");
-    std::lock_guard<std::mutex> lk(mu);
-    if (!addr[dev]) {
-        void *p = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess || !p)
-            throw gu_error(GU_ERR_CUDA, std::string("cudaGetSymbolAddress(g_noalloc_scratch): ") + cudaGetErrorString(e));
-        addr[dev] = p;
-    }
-    return static_cast<char *>(addr[dev]);
+    void *p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p)
+        throw gu_error(GU_ERR_CUDA, std::string("cudaGetSymbolAddress(g_noalloc_scratch): ") + cudaGetErrorString(e));
+    return static_cast<char *>(p);
 }
 
 static void bfs_noalloc(const int32_t *R, const int32_t *C, int32_t n, int64_t m, const int32_t *sources, int32_t k,

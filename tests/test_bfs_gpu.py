@@ -171,8 +171,8 @@ def test_host_form_matches_device_form():
 
 
 def test_rmat20_full_size_certificates():
-    """R-MAT scale 20, 512 sources: per-edge BFS certificates on the GPU plus
-    exact agreement with the oracle on a sample of rows."""
+    """R-MAT scale 20, 512 sources: per-edge BFS certificates on the GPU (they hold
+    at any size and need no oracle)."""
     hg = gu.HostGraph.rmat(20, 16, seed=1)
     g = gu.Graph(hg)
     srcs = gu.sources(hg.n, 512, seed=2)
@@ -199,12 +199,13 @@ def test_rmat20_full_size_certificates():
         parent = torch.zeros_like(d).scatter_reduce_(1, C.unsqueeze(0).expand(B, -1), has, reduce="amax")
         need = (d != INF) & (d > 0)
         assert bool(((parent > 0) | ~need).all())
+        # no negative level, and level 0 exactly once per row: at the row's source
+        assert bool((d >= 0).all())
         rows = torch.arange(b, b + B, device=dev)
         assert bool((d[torch.arange(B, device=dev), s[rows].long()] == 0).all())
+        assert bool(((d == 0).sum(1) == 1).all())
         del du, dv, fin_u, fin_v, diff, has, parent
-    sample = [0, 1, 63, 64, 200, 511]
-    ref, _ = oracle.bfs_multi(hg.R, hg.C, hg.n, srcs[sample], nthreads=8)
-    np.testing.assert_array_equal(dist[sample].cpu().numpy(), ref)
+    # every row against the oracle: tests/test_parity_configs.py::test_rmat20_all_512_rows
 
 
 def test_rows_beyond_2_31_elements():

@@ -8,8 +8,9 @@ array compiled into the library and works on the caller's own device CSR.
 The test calls it through the C ABI, twice in a row on the same device (the
 second call finds the first call's leftovers in the shared scratch), and checks
 each result against the existing entry point gu_bfs, which allocates its own
-workspace.  Distances are integers: the comparison is exact.  This file is
-collected last on purpose.
+workspace, and against the oracle (the C restatement of the reference's CPU
+BFS, examples/multi_search/multi_search_test.cu:17-38).  Distances are
+integers: the comparisons are exact.  This file is collected last on purpose.
 """
 import ctypes
 
@@ -17,6 +18,7 @@ import numpy as np
 import pytest
 
 import gu
+import oracle
 
 torch = pytest.importorskip("torch")
 pytestmark = pytest.mark.gpu
@@ -58,6 +60,8 @@ def test_noalloc_matches_gu_bfs_twice(kind):
         torch.cuda.synchronize()
         got = dist.cpu().numpy()
         np.testing.assert_array_equal(got[:, :hg.n], _reference_rows(hg, srcs), err_msg=f"call {call}")
+        ref, _ = oracle.bfs_multi(hg.R, hg.C, hg.n, srcs, nthreads=8)
+        np.testing.assert_array_equal(got[:, :hg.n], ref, err_msg=f"call {call} vs oracle")
         assert np.all(got[:, hg.n:] == -3)
 
 
