@@ -128,6 +128,7 @@ struct BcArgs {
     double *delta_rows;   // optional k x ld
     int64_t ld;
     BcCtl *ctl;
+    unsigned long long wait_ns;  // bound of every grid-barrier wait (gu_set_wait_limit)
 };
 
 // Takes the next (up to) K set lanes of a ballot in ascending lane order; a
@@ -644,7 +645,8 @@ __global__ void __launch_bounds__(BC_THREADS, 2) bc_grid_kernel(BcArgs a, int do
     auto barrier = [&](int kind, int level) {
         if (threadIdx.x == 0) record_bc_event(ctl, phase, blockIdx.x == 0, batch, level, kind);
         ++phase;
-        return grid_barrier(&ctl->bar, &ctl->err, epoch, reinterpret_cast<const u64 *>(ctl), reinterpret_cast<u64 *>(&s_ctl),
+        return grid_barrier(&ctl->bar, &ctl->err, epoch, a.wait_ns, reinterpret_cast<const u64 *>(ctl),
+                            reinterpret_cast<u64 *>(&s_ctl),
                             (int)(sizeof(BcCtl) / sizeof(u64)));
     };
     const long long rank = (long long)blockIdx.x * blockDim.x + threadIdx.x, size = (long long)gridDim.x * blockDim.x;
@@ -773,7 +775,7 @@ static void build_chunks(DeviceGraph &g, const std::vector<int32_t> &R, ChunkMap
     }
     auto up = [&](const std::vector<int32_t> &src, int32_t *&dst) {
         if (src.empty()) return;
-        GU_CUDA_CHECK(cudaMalloc(&dst, sizeof(int32_t) * src.size()));
+        GU_CUDA_CHECK(dev_malloc((void **)&dst, sizeof(int32_t) * src.size()));
         g.extra_allocs.push_back(dst);
         GU_CUDA_CHECK(cudaMemcpy(dst, src.data(), sizeof(int32_t) * src.size(), cudaMemcpyHostToDevice));
         g.bytes += sizeof(int32_t) * src.size();
@@ -914,6 +916,7 @@ void launch_bc(DeviceGraph &g, const int32_t *sources, int32_t k, const BcOption
     a.k = k;
     char *p = ws;
     a.ctl = reinterpret_cast<BcCtl *>(p);
+    a.wait_ns = wait_limit_ns();
     p += WS_CONTROL_BYTES;
     a.seen = reinterpret_cast<u64 *>(p);
     p += words;

@@ -134,6 +134,41 @@ gu_status gu_choose_device(int requested, int *chosen)
     });
 }
 
+gu_status gu_set_wait_limit(double seconds)
+{
+    return guarded([&] {
+        if (!(seconds >= 1e-4 && seconds <= 3600.0))
+            throw gu_error(GU_ERR_INVALID_ARGUMENT, "wait limit must be in [1e-4, 3600] seconds");
+        set_wait_limit_ns((unsigned long long)(seconds * 1e9));
+    });
+}
+
+gu_status gu_get_wait_limit(double *seconds)
+{
+    return guarded([&] {
+        if (!seconds) throw gu_error(GU_ERR_INVALID_ARGUMENT, "null output");
+        *seconds = (double)wait_limit_ns() * 1e-9;
+    });
+}
+
+gu_status gu_check_grid_barrier(int absent_block, double limit_seconds, void *stream, double *elapsed_seconds)
+{
+    return guarded([&] {
+        if (!(limit_seconds >= 1e-4 && limit_seconds <= 60.0))
+            throw gu_error(GU_ERR_INVALID_ARGUMENT, "limit must be in [1e-4, 60] seconds");
+        check_grid_barrier(absent_block, (unsigned long long)(limit_seconds * 1e9), (cudaStream_t)stream,
+                           elapsed_seconds);
+    });
+}
+
+gu_status gu_debug_fail_allocations(int64_t after, int64_t count)
+{
+    return guarded([&] {
+        if (after < 0 || count < 0) throw gu_error(GU_ERR_INVALID_ARGUMENT, "after and count must be >= 0");
+        set_alloc_failures(after, count);
+    });
+}
+
 gu_status gu_timer_start(void *stream, gu_timer *out)
 {
     return guarded([&] {
@@ -469,7 +504,7 @@ gu_status gu_graph_autotune(gu_graph g, const int32_t *sources_dev, int32_t k, g
                 if (rows) cudaFree(rows);
             }
         } scratch;
-        GU_CUDA_CHECK(cudaMalloc(reinterpret_cast<void **>(&scratch.rows), row_bytes ? row_bytes : 4));
+        GU_CUDA_CHECK(dev_malloc(reinterpret_cast<void **>(&scratch.rows), row_bytes ? row_bytes : 4));
         GU_CUDA_CHECK(cudaStreamCreateWithFlags(&scratch.st, cudaStreamNonBlocking));
         int32_t *const rows = scratch.rows;
         const cudaStream_t st = scratch.st;

@@ -60,19 +60,19 @@ __device__ __forceinline__ void red_release_add_u32(unsigned *p, unsigned v)
 __device__ __forceinline__ int ld_volatile_i32(const int *p) { return *(const volatile int *)p; }
 __device__ __forceinline__ u64 ld_volatile_u64(const u64 *p) { return *(const volatile u64 *)p; }
 
-// Upper bound on any single wait in these kernels.  A wait that runs out
-// records DEV_ERR_BARRIER_TIMEOUT in *err and returns; every block then leaves
-// the kernel and the host reports GU_ERR_TIMEOUT.  No wait is unbounded.
-constexpr u64 WAIT_LIMIT_NS = 4ull * 1000ull * 1000ull * 1000ull;
-
 // Grid-wide barrier for a cooperative launch (all CTAs co-resident).  `bar` is a
 // monotonically increasing arrival counter zeroed before the launch; `epoch`
 // counts this CTA's barriers.  Returns false if any CTA reported an error.
 // Thread 0 alone reads the global words every thread needs after the barrier
 // (the error flag, and n 64-bit words from src into the shared dst): one
 // request per CTA instead of one per warp, all at the same address.
-__device__ __forceinline__ bool grid_barrier(unsigned *bar, int *err, unsigned &epoch, const u64 *src = nullptr,
-                                             u64 *dst = nullptr, int n = 0)
+//
+// The wait is bounded by limit_ns (a launch argument, gu_set_wait_limit; 4 s by
+// default): a wait that runs out records DEV_ERR_BARRIER_TIMEOUT in *err and
+// returns false; every block then leaves the kernel and the host reports
+// GU_ERR_TIMEOUT.  No wait is unbounded.
+__device__ __forceinline__ bool grid_barrier(unsigned *bar, int *err, unsigned &epoch, u64 limit_ns,
+                                             const u64 *src = nullptr, u64 *dst = nullptr, int n = 0)
 {
     __shared__ int s_ok;
     __syncthreads();
@@ -90,7 +90,7 @@ __device__ __forceinline__ bool grid_barrier(unsigned *bar, int *err, unsigned &
             if ((++spins & 63u) == 0) {
                 u64 now = global_timer_ns();
                 if (t0 == 0) t0 = now;
-                else if (now - t0 > WAIT_LIMIT_NS) {
+                else if (now - t0 > limit_ns) {
                     atomicCAS(err, 0, (int)DEV_ERR_BARRIER_TIMEOUT);
                     break;
                 }

@@ -9,9 +9,118 @@
 #include "device_utils.cuh"
 #include "gu_internal.h"
 
+#include <atomic>
 #include <memory>
+#include <mutex>
 
 namespace gu {
+
+// ---- allocation helpers with a host-side failure injector --------------------------
+// After `after` more successful allocations, the next `count` fail.
+static std::atomic<long long> g_fail_after{0}, g_fail_count{0};
+
+void set_alloc_failures(long long after, long long count)
+{
+    g_fail_count.store(0);
+    g_fail_after.store(after < 0 ? 0 : after);
+    g_fail_count.store(count < 0 ? 0 : count);
+}
+
+static bool injected_failure()
+{
+    if (g_fail_count.load(std::memory_order_relaxed) <= 0) return false;
+    static std::mutex mu;
+    std::lock_guard<std::mutex> lk(mu);
+    if (g_fail_count.load() <= 0) return false;
+    if (g_fail_after.load() > 0) {
+        g_fail_after.fetch_sub(1);
+        return false;
+    }
+    g_fail_count.fetch_sub(1);
+    return true;
+}
+
+cudaError_t dev_malloc(void **p, size_t bytes)
+{
+    if (injected_failure()) {
+        *p = nullptr;
+        return cudaErrorMemoryAllocation;
+    }
+    const cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) *p = nullptr;
+    return e;
+}
+
+cudaError_t pinned_alloc(void **p, size_t bytes)
+{
+    if (injected_failure()) {
+        *p = nullptr;
+        return cudaErrorMemoryAllocation;
+    }
+    const cudaError_t e = cudaHostAlloc(p, bytes, cudaHostAllocDefault);
+    if (e != cudaSuccess) *p = nullptr;
+    return e;
+}
+
+static std::atomic<unsigned long long> g_wait_ns{4ull * 1000ull * 1000ull * 1000ull};
+unsigned long long wait_limit_ns() { return g_wait_ns.load(std::memory_order_relaxed); }
+void set_wait_limit_ns(unsigned long long ns) { g_wait_ns.store(ns); }
+
+// Diagnostic launch for gu_check_grid_barrier: every CTA but `absent` meets at two
+// grid barriers; CTA `absent` leaves before its first arrival, so the others'
+// first wait can only end by its limit.
+__global__ void barrier_check_kernel(unsigned *bar, int *err, int absent, unsigned long long limit_ns, int *passed)
+{
+    unsigned epoch = 0;
+    if ((int)blockIdx.x == absent) return;
+    if (!grid_barrier(bar, err, epoch, limit_ns)) return;
+    if (!grid_barrier(bar, err, epoch, limit_ns)) return;
+    if (threadIdx.x == 0) atomicAdd(passed, 1);
+}
+
+int check_grid_barrier(int absent, unsigned long long limit_ns, cudaStream_t st, double *seconds)
+{
+    int dev = 0;
+    GU_CUDA_CHECK(cudaGetDevice(&dev));
+    const int blocks = device_sm_count(dev);
+    if (absent < -1 || absent >= blocks)
+        throw gu_error(GU_ERR_INVALID_ARGUMENT, "absent block must be -1 or in [0, " + std::to_string(blocks) + ")");
+    struct Buf {
+        int *p = nullptr;
+        cudaEvent_t e0 = nullptr, e1 = nullptr;
+        ~Buf()
+        {
+            if (p) cudaFree(p);
+            if (e0) cudaEventDestroy(e0);
+            if (e1) cudaEventDestroy(e1);
+        }
+    } b;
+    GU_CUDA_CHECK(dev_malloc(reinterpret_cast<void **>(&b.p), 4 * sizeof(int)));
+    GU_CUDA_CHECK(cudaEventCreate(&b.e0));
+    GU_CUDA_CHECK(cudaEventCreate(&b.e1));
+    GU_CUDA_CHECK(cudaMemsetAsync(b.p, 0, 4 * sizeof(int), st));
+    unsigned *bar = reinterpret_cast<unsigned *>(b.p);
+    int *err = b.p + 1, *passed = b.p + 2;
+    void *params[] = {&bar, &err, &absent, &limit_ns, &passed};
+    GU_CUDA_CHECK(cudaEventRecord(b.e0, st));
+    GU_CUDA_CHECK(cudaLaunchCooperativeKernel((const void *)barrier_check_kernel, dim3(blocks), dim3(128), params, 0, st));
+    GU_CUDA_CHECK(cudaEventRecord(b.e1, st));
+    int h[4] = {0, 0, 0, 0};
+    GU_CUDA_CHECK(cudaMemcpyAsync(h, b.p, sizeof(h), cudaMemcpyDeviceToHost, st));
+    GU_CUDA_CHECK(cudaStreamSynchronize(st));
+    float ms = 0.f;
+    GU_CUDA_CHECK(cudaEventElapsedTime(&ms, b.e0, b.e1));
+    if (seconds) *seconds = ms * 1e-3;
+    if (h[1] == DEV_ERR_BARRIER_TIMEOUT)
+        throw gu_error(GU_ERR_TIMEOUT, "a grid-barrier wait exceeded its limit (block " + std::to_string(absent) +
+                                           " never arrived); " + std::to_string(h[2]) + " of " +
+                                           std::to_string(blocks) + " blocks passed both barriers");
+    if (h[1] != 0) throw gu_error(GU_ERR_INTERNAL, "device reported error code " + std::to_string(h[1]));
+    if (h[2] != blocks - (absent >= 0 ? 1 : 0))
+        throw gu_error(GU_ERR_INTERNAL, "grid barrier check: " + std::to_string(h[2]) + " of " +
+                                            std::to_string(blocks) + " blocks passed");
+    return blocks;
+}
 
 int device_sm_count(int device)
 {
@@ -30,11 +139,11 @@ void *Workspace::get(size_t need)
         bytes = 0;
     }
     size_t want = need + need / 8;
-    cudaError_t e = cudaMalloc(&ptr, want);
+    cudaError_t e = dev_malloc(&ptr, want);
     if (e != cudaSuccess) {
         (void)cudaGetLastError();
         ptr = nullptr;
-        e = cudaMalloc(&ptr, need);
+        e = dev_malloc(&ptr, need);
         if (e != cudaSuccess) {
             (void)cudaGetLastError();
             ptr = nullptr;
@@ -112,7 +221,7 @@ __global__ void coo_from_csr_kernel(const int32_t *__restrict__ R, int32_t n, in
 void ensure_coo(DeviceGraph &g, cudaStream_t stream)
 {
     if (g.F || g.m == 0) return;
-    GU_CUDA_CHECK(cudaMalloc(&g.F, sizeof(int32_t) * (size_t)g.m));
+    GU_CUDA_CHECK(dev_malloc((void **)&g.F, sizeof(int32_t) * (size_t)g.m));
     g.bytes += sizeof(int32_t) * (size_t)g.m;
     coo_from_csr_kernel<<<g.sm_count * 4, 256, 0, stream>>>(g.R, g.n, g.F);
     GU_CUDA_CHECK(cudaGetLastError());
@@ -149,8 +258,8 @@ DeviceGraph *create_device_graph(const int32_t *R, const int32_t *C, int32_t n, 
     std::vector<int32_t> Cs(C, C + m);
     sort_adjacency_by_key(R, Cs.data(), n, outdeg.data());
     g->host_R.assign(R, R + n + 1);
-    GU_CUDA_CHECK(cudaMalloc(&g->R, sizeof(int32_t) * ((size_t)n + 1)));
-    GU_CUDA_CHECK(cudaMalloc(&g->C, sizeof(int32_t) * (size_t)(m > 0 ? m : 1)));
+    GU_CUDA_CHECK(dev_malloc((void **)&g->R, sizeof(int32_t) * ((size_t)n + 1)));
+    GU_CUDA_CHECK(dev_malloc((void **)&g->C, sizeof(int32_t) * (size_t)(m > 0 ? m : 1)));
     GU_CUDA_CHECK(cudaMemcpyAsync(g->R, R, sizeof(int32_t) * ((size_t)n + 1), cudaMemcpyHostToDevice, stream));
     if (m > 0) GU_CUDA_CHECK(cudaMemcpyAsync(g->C, Cs.data(), sizeof(int32_t) * (size_t)m, cudaMemcpyHostToDevice, stream));
     g->bytes = sizeof(int32_t) * ((size_t)n + 1 + (size_t)m);
@@ -162,8 +271,8 @@ DeviceGraph *create_device_graph(const int32_t *R, const int32_t *C, int32_t n, 
         HostGraph t = transpose(h);
         sort_adjacency_by_key(t.R.data(), t.C.data(), n, outdeg.data());
         g->host_RT = t.R;
-        GU_CUDA_CHECK(cudaMalloc(&g->RT, sizeof(int32_t) * ((size_t)n + 1)));
-        GU_CUDA_CHECK(cudaMalloc(&g->CT, sizeof(int32_t) * (size_t)(m > 0 ? m : 1)));
+        GU_CUDA_CHECK(dev_malloc((void **)&g->RT, sizeof(int32_t) * ((size_t)n + 1)));
+        GU_CUDA_CHECK(dev_malloc((void **)&g->CT, sizeof(int32_t) * (size_t)(m > 0 ? m : 1)));
         GU_CUDA_CHECK(cudaMemcpyAsync(g->RT, t.R.data(), sizeof(int32_t) * ((size_t)n + 1), cudaMemcpyHostToDevice, stream));
         if (m > 0) GU_CUDA_CHECK(cudaMemcpyAsync(g->CT, t.C.data(), sizeof(int32_t) * (size_t)m, cudaMemcpyHostToDevice, stream));
         GU_CUDA_CHECK(cudaStreamSynchronize(stream));  // t goes out of scope
@@ -190,7 +299,7 @@ DeviceGraph *create_device_graph(const int32_t *R, const int32_t *C, int32_t n, 
         auto upload = [&](const std::vector<int32_t> &src, int32_t *&dst, int32_t &cnt) {
             cnt = (int32_t)src.size();
             if (src.empty()) return;
-            GU_CUDA_CHECK(cudaMalloc(&dst, sizeof(int32_t) * src.size()));
+            GU_CUDA_CHECK(dev_malloc((void **)&dst, sizeof(int32_t) * src.size()));
             GU_CUDA_CHECK(cudaMemcpyAsync(dst, src.data(), sizeof(int32_t) * src.size(), cudaMemcpyHostToDevice, stream));
             g->bytes += sizeof(int32_t) * src.size();
         };

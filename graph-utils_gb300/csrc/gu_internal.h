@@ -54,6 +54,23 @@ void set_last_error(const std::string &msg);
         }                                                                                            \
     } while (0)
 
+// Every device and pinned host allocation of the library goes through these two
+// (graph.cu).  They return cudaErrorMemoryAllocation on their own when a failure
+// has been injected with gu_debug_fail_allocations, so that tests can drive each
+// caller's out-of-memory path (GU_ERR_OUT_OF_MEMORY, the handle left usable)
+// without exhausting the GPU.
+cudaError_t dev_malloc(void **p, size_t bytes);
+cudaError_t pinned_alloc(void **p, size_t bytes);
+void set_alloc_failures(long long after, long long count);
+
+// Bound of every device-side wait (grid barriers) in nanoseconds, passed to each
+// persistent launch; gu_set_wait_limit sets it for the process (4 s by default).
+unsigned long long wait_limit_ns();
+void set_wait_limit_ns(unsigned long long ns);
+// gu_check_grid_barrier: returns the number of CTAs launched; throws GU_ERR_TIMEOUT
+// when the absent CTA's missing arrival made the others' wait run out.
+int check_grid_barrier(int absent, unsigned long long limit_ns, cudaStream_t st, double *seconds);
+
 // Host CSR graph (the reference's host_graph, parse.h:15-35, without F; F is
 // derived on the device when a variant needs it).
 struct HostGraph {

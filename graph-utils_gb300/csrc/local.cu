@@ -182,7 +182,7 @@ bool launch_local_bfs(DeviceGraph &g, const int32_t *sources, int32_t k, int32_t
         const int width = g.max_degree <= 4 ? 4 : g.max_degree <= 8 ? 8 : 16;
         if (g.max_degree > 16) throw gu_error(GU_ERR_INTERNAL, "per-source engine on a graph of out-degree > 16");
         const size_t bytes = (size_t)(g.n > 0 ? g.n : 1) * width * sizeof(int32_t);
-        GU_CUDA_CHECK(cudaMalloc(&g.ell, bytes));
+        GU_CUDA_CHECK(dev_malloc((void **)&g.ell, bytes));
         g.extra_allocs.push_back(g.ell);
         g.bytes += bytes;
         g.ell_width = width;

@@ -135,6 +135,7 @@ struct MsArgs {
     float alpha, beta, gamma;
     float rare_frac;  // bottom-up levels leave a source covered by fewer CTAs to top-down
     int degbits;
+    unsigned long long wait_ns;  // bound of every grid-barrier wait (gu_set_wait_limit)
 };
 
 struct Lvl {
@@ -1456,7 +1457,8 @@ __global__ void __launch_bounds__(MS_THREADS, MS_MIN_BLOCKS) ms_grid_kernel(MsAr
     int ev_idx = 0;
     MsCtl *ctl = a.ctl;
     auto barrier = [&]() {
-        return grid_barrier(&ctl->bar, &ctl->err, epoch, reinterpret_cast<const u64 *>(ctl), reinterpret_cast<u64 *>(&s_ctl),
+        return grid_barrier(&ctl->bar, &ctl->err, epoch, a.wait_ns, reinterpret_cast<const u64 *>(ctl),
+                            reinterpret_cast<u64 *>(&s_ctl),
                             (int)(sizeof(MsCtl) / sizeof(u64)));
     };
     const long long rank = GridG::rank(), size = GridG::size();
@@ -1833,6 +1835,7 @@ void launch_msbfs(DeviceGraph &g, const int32_t *sources, int32_t k, int32_t *di
     int degbits = 1;
     while (degbits < 31 && (1ll << degbits) <= (long long)g.max_degree) ++degbits;
     a.degbits = degbits;
+    a.wait_ns = wait_limit_ns();
     GU_CUDA_CHECK(cudaMemsetAsync(a.ctl, 0, CTL_REGION, stream));
     const int sms = g.sm_count;
     const int mb = opt.max_blocks;
@@ -1851,7 +1854,7 @@ void launch_msbfs(DeviceGraph &g, const int32_t *sources, int32_t k, int32_t *di
     }
     if (opt.timed) g.mark_stop(stream);
     if (&wsp == &g.ws) {  // the control block comes back with the launch: one round trip per call
-        if (!g.ctl_host) GU_CUDA_CHECK(cudaHostAlloc(&g.ctl_host, sizeof(MsCtl), cudaHostAllocDefault));
+        if (!g.ctl_host) GU_CUDA_CHECK(pinned_alloc(&g.ctl_host, sizeof(MsCtl)));
         GU_CUDA_CHECK(cudaMemcpyAsync(g.ctl_host, a.ctl, sizeof(MsCtl), cudaMemcpyDeviceToHost, stream));
     }
 }
@@ -2048,6 +2051,7 @@ static void bfs_noalloc(const int32_t *R, const int32_t *C, int32_t n, int64_t m
     int degbits = 1;
     while (degbits < 31 && (1ll << degbits) <= (long long)m) ++degbits;
     a.degbits = degbits;
+    a.wait_ns = wait_limit_ns();
     // the previous call's contents stay in the array: clear the control block
     GU_CUDA_CHECK(cudaMemsetAsync(a.ctl, 0, CTL_REGION, st));
     launch_one<GU_BFS_AUTO, 1>(a, sms, st);

@@ -60,7 +60,7 @@ struct PinnedBuf {
         if (p) cudaFreeHost(p);
         p = nullptr;
         bytes = 0;
-        GU_CUDA_CHECK(cudaHostAlloc(&p, need, cudaHostAllocDefault));
+        GU_CUDA_CHECK(pinned_alloc(&p, need));
         bytes = need;
         return p;
     }

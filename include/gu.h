@@ -87,6 +87,31 @@ typedef struct gu_timer_s *gu_timer;
 gu_status gu_timer_start(void *stream, gu_timer *out);
 gu_status gu_timer_stop(gu_timer t, void *stream, double *seconds); /* also frees t */
 
+/* Bound of every device-side wait (the grid barriers between the levels of the
+ * persistent kernels), in seconds, for launches made after the call; 4 s by
+ * default, accepted range [1e-4, 3600].  A wait that runs out ends the launch:
+ * the call returns GU_ERR_TIMEOUT and its handle stays usable.  The reference
+ * has no bounded waits (its kernels end levels with __syncthreads and kernel
+ * boundaries), so no counterpart. */
+gu_status gu_set_wait_limit(double seconds);
+gu_status gu_get_wait_limit(double *seconds);
+
+/* Diagnostic of the grid barrier every persistent kernel is built on: a
+ * cooperative launch of one 128-thread CTA per SM whose CTAs meet at two grid
+ * barriers bounded by `limit_seconds`.  absent_block = -1: every CTA arrives and
+ * the call returns GU_OK.  absent_block = b: CTA b leaves without arriving, the
+ * others' wait runs out after limit_seconds and the call returns GU_ERR_TIMEOUT
+ * (no fault, no trap: the device stays usable).  *elapsed_seconds = the launch's
+ * CUDA-event time.  No reference counterpart. */
+gu_status gu_check_grid_barrier(int absent_block, double limit_seconds, void *stream, double *elapsed_seconds);
+
+/* Test hook: after `after` more successful device or pinned-host allocations by
+ * this library, the next `count` fail as if the GPU were out of memory (count 0
+ * switches it off).  Lets tests drive every call's GU_ERR_OUT_OF_MEMORY path on
+ * the host side.  No reference counterpart (the reference exits on failure,
+ * util_device.cuh:10-22). */
+gu_status gu_debug_fail_allocations(int64_t after, int64_t count);
+
 /* Board power during a run (power_measurer::start_power_sample /
  * end_power_sample, util_device.cu:78-130): a background thread reads the
  * device's power draw every period_ms until gu_power_stop, which returns the

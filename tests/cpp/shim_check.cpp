@@ -61,7 +61,10 @@ int main(int argc, char **argv)
     if (end > n) end = n;
 
     int dev = -1;
-    gu_choose_device(-1, &dev);
+    if (gu_choose_device(-1, &dev) != GU_OK || dev < 0) {
+        std::printf("FAIL gu_choose_device: %s\n", gu_last_error());
+        return 1;
+    }
     device_graph g(h);
     program_options op;
 

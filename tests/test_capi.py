@@ -141,3 +141,34 @@ def test_drop_in_header_compiles_and_links(tmp_path):
            "-o", str(tmp_path / "shim_check")]
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+def test_wait_limit_and_alloc_hook_arguments_on_the_host():
+    """gu_set_wait_limit / gu_debug_fail_allocations validate their arguments
+    without touching a GPU; gu_choose_device without one reports a CUDA status."""
+    L = gu.lib()
+    L.gu_set_wait_limit.argtypes = [ctypes.c_double]
+    L.gu_get_wait_limit.argtypes = [ctypes.POINTER(ctypes.c_double)]
+    L.gu_debug_fail_allocations.argtypes = [ctypes.c_int64, ctypes.c_int64]
+    v = ctypes.c_double()
+    assert L.gu_get_wait_limit(ctypes.byref(v)) == 0 and v.value == pytest.approx(4.0)
+    for bad in (0.0, -1.0, 5e-5, 4000.0, float("nan")):
+        assert L.gu_set_wait_limit(bad) == 1
+    assert L.gu_get_wait_limit(ctypes.byref(v)) == 0 and v.value == pytest.approx(4.0)
+    assert L.gu_set_wait_limit(0.25) == 0
+    assert L.gu_get_wait_limit(ctypes.byref(v)) == 0 and v.value == pytest.approx(0.25)
+    assert L.gu_set_wait_limit(4.0) == 0
+    assert L.gu_get_wait_limit(None) == 1
+    assert L.gu_debug_fail_allocations(-1, 1) == 1
+    assert L.gu_debug_fail_allocations(0, -1) == 1
+    assert L.gu_debug_fail_allocations(0, 0) == 0
+    try:
+        import torch
+        has_gpu = torch.cuda.is_available()
+    except Exception:
+        has_gpu = False
+    if not has_gpu:
+        chosen = ctypes.c_int(-7)
+        assert L.gu_choose_device(-1, ctypes.byref(chosen)) == 2  # GU_ERR_CUDA, no exit()
+        assert chosen.value == -7
+        assert L.gu_last_error()
