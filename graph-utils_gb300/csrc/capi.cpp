@@ -14,6 +14,7 @@ namespace gu {
 DeviceGraph *create_device_graph(const int32_t *R, const int32_t *C, int32_t n, int64_t m, bool directed,
                                  cudaStream_t stream);
 void msbfs_read_status(DeviceGraph &g, int *dev_err, int *td_levels, int *bu_levels, int *max_level);
+int msbfs_read_idle(DeviceGraph &g, int max_entries, double *idle_ms, int *nblocks);
 int msbfs_read_timeline(DeviceGraph &g, int max_entries, int32_t *batch, int32_t *level, int32_t *kind,
                         int64_t *frontier_vertices, int64_t *frontier_edges, double *t_ms);
 
@@ -406,6 +407,21 @@ gu_status gu_graph_level_profile(gu_graph g, int max_entries, int32_t *batch, in
         const int c = dg.timeline == 1
                           ? bc_read_timeline(dg, max_entries, batch, level, kind, frontier_vertices, frontier_edges, t_ms)
                           : msbfs_read_timeline(dg, max_entries, batch, level, kind, frontier_vertices, frontier_edges, t_ms);
+        if (count) *count = c;
+    });
+}
+
+gu_status gu_graph_level_idle(gu_graph g, int max_entries, double *idle_cta_ms, int *nblocks, int *count)
+{
+    return guarded([&] {
+        if (!g || max_entries < 0) throw gu_error(GU_ERR_INVALID_ARGUMENT, "bad arguments");
+        DeviceGraph &dg = *g->g;
+        std::lock_guard<std::mutex> lk(dg.mu);
+        DeviceScope ds(dg.device);
+        if (!dg.timed || !dg.ws.ptr || dg.timeline == 1)
+            throw gu_error(GU_ERR_INVALID_ARGUMENT, "no batched search recorded on this graph yet");
+        GU_CUDA_CHECK(cudaEventSynchronize(dg.ev_stop));
+        const int c = msbfs_read_idle(dg, max_entries, idle_cta_ms, nblocks);
         if (count) *count = c;
     });
 }

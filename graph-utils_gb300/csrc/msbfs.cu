@@ -63,11 +63,13 @@ struct __align__(128) MsCtl {
     int td_levels;
     int bu_levels;
     int max_level;
-    int pad0[3];
+    int nblocks;  // grid size of the launch (profiling)
+    int pad0[2];
     u64 qpack[4];
     int work[4];
     u64 rpack;  // bottom-up level: rare-source frontier list, (count << 38) | edges
-    int pad1[2];
+    int wo_next;  // distance write-out: next tile to take (zeroed with the batch)
+    int pad1;
     u64 active[4][MAXW];
 };
 static_assert(sizeof(MsCtl) <= 256, "control block must fit its reserved space");
@@ -81,6 +83,7 @@ struct MsEvent {
     int32_t batch, level;
     int32_t bottom_up, qlen;
     long long qedges;
+    u64 idle_ns;  // summed over CTAs: time spent waiting at the grid barriers of this phase
 };
 // Per-source coverage of each level's discoveries: cover[j & 3][s] counts the
 // CTAs that discovered source s in F_j (a source with a frontier of a few dozen
@@ -1217,31 +1220,43 @@ __device__ void write_distances_nibble(const MsArgs &a, int row0, int nb)
     constexpr int TILE = ROWS * TV;
     constexpr int SWZ = 32 / W;   // byte rotation per word
     static_assert(2 * TILE <= MS_SMEM_BYTES, "byte tiles exceed the shared buffer");
+    // Tiles are taken from a counter (ctl->wo_next) rather than by a fixed
+    // stride, so that CTAs whose stores drain faster take more of them (a fixed
+    // split left a fifth of the CTA time idle).  Tile of iteration i: s_tile[i & 3],
+    // taken by thread 0 two iterations ahead (the decoders prefetch the next one).
+    __shared__ int s_tile[4];
     unsigned char *tiles = ms_smem();
     const size_t pstride = (size_t)a.n * W;
     const bool decoder = threadIdx.x < HALF;
     const int tid = decoder ? threadIdx.x : threadIdx.x - HALF;
     const int q = tid % W, vl = tid / W;
     const int nq = (nb + 63) / 64;
-    const long long ntile = ((long long)a.n + TV - 1) / TV;
+    const int ntile = (int)(((long long)a.n + TV - 1) / TV);
     const int col = (vl + SWZ * q) % TV;
-    auto load = [&](long long t, u64 &s, u64 (&pl)[4]) {
-        const int32_t v = (int32_t)(t * TV) + vl;
+    int *next = &a.ctl->wo_next;
+    auto load = [&](int t, u64 &s, u64 (&pl)[4]) {
+        const int32_t v = t * TV + vl;
         const bool valid = decoder && t < ntile && v < a.n && q < nq;
         const size_t o = (size_t)v * W + q;
         s = valid ? __ldcs(a.seen + o) : 0ull;
 #pragma unroll
         for (int b = 0; b < 4; ++b) pl[b] = (b < a.nplanes && valid) ? __ldcs(a.plane + b * pstride + o) : 0ull;
     };
+    if (threadIdx.x == 0) {
+        s_tile[0] = atomicAdd(next, 1);
+        s_tile[1] = atomicAdd(next, 1);
+    }
+    __syncthreads();
     u64 s, pl[4];
-    load(G::blk(), s, pl);
-    for (long long i = 0;; ++i) {  // block-uniform
-        const long long td = G::blk() + i * G::nblk(), ts = td - G::nblk();
-        if (ts >= ntile) break;
+    load(s_tile[0], s, pl);
+    for (int i = 0;; ++i) {  // block-uniform
+        const int td = s_tile[i & 3], ts = i > 0 ? s_tile[(i - 1) & 3] : ntile, tn = s_tile[(i + 1) & 3];
+        if (td >= ntile && ts >= ntile) break;
+        if (threadIdx.x == 0) s_tile[(i + 2) & 3] = td < ntile ? atomicAdd(next, 1) : ntile;
         if (decoder) {
             if (td < ntile) {
                 u64 s_n, pl_n[4];
-                load(td + G::nblk(), s_n, pl_n);
+                load(tn, s_n, pl_n);
                 unsigned char *tile = tiles + (i & 1) * TILE;
 #pragma unroll
                 for (int g = 0; g < 8; ++g) {
@@ -1265,9 +1280,9 @@ __device__ void write_distances_nibble(const MsArgs &a, int row0, int nb)
 #pragma unroll
                 for (int b = 0; b < 4; ++b) pl[b] = pl_n[b];
             }
-        } else if (i > 0) {
+        } else if (ts < ntile) {
             const unsigned char *tile = tiles + ((i - 1) & 1) * TILE;
-            const int32_t vbase = (int32_t)(ts * TV);
+            const int32_t vbase = ts * TV;
             const int nv = min(TV, a.n - vbase), nv4 = nv >> 2;
             for (int k = tid; k < ROWS * (TV / 4); k += HALF) {
                 const int row = k / (TV / 4), c4 = k - row * (TV / 4);
@@ -1456,15 +1471,22 @@ __global__ void __launch_bounds__(MS_THREADS, MS_MIN_BLOCKS) ms_grid_kernel(MsAr
     unsigned epoch = 0;
     int ev_idx = 0;
     MsCtl *ctl = a.ctl;
-    auto barrier = [&]() {
-        return grid_barrier(&ctl->bar, &ctl->err, epoch, a.wait_ns, reinterpret_cast<const u64 *>(ctl),
-                            reinterpret_cast<u64 *>(&s_ctl),
-                            (int)(sizeof(MsCtl) / sizeof(u64)));
+    // slot: the timeline entry whose phase the barrier ends (or is inside of); each
+    // CTA adds its wait there (profiling hook: idle CTA time per phase)
+    auto barrier = [&](int slot) {
+        const u64 t_arrive = threadIdx.x == 0 ? global_timer_ns() : 0ull;
+        const bool ok = grid_barrier(&ctl->bar, &ctl->err, epoch, a.wait_ns, reinterpret_cast<const u64 *>(ctl),
+                                     reinterpret_cast<u64 *>(&s_ctl), (int)(sizeof(MsCtl) / sizeof(u64)));
+        if (threadIdx.x == 0 && slot < TIMELINE_MAX)
+            atomicAdd(&reinterpret_cast<MsEvent *>(reinterpret_cast<char *>(ctl) + 256)[slot].idle_ns,
+                      global_timer_ns() - t_arrive);
+        return ok;
     };
     const long long rank = GridG::rank(), size = GridG::size();
     const size_t pstride = (size_t)a.n * W;
     if (threadIdx.x < MAXW) s_act[threadIdx.x] = 0;
     if (threadIdx.x == 0) *cq_count() = 0;
+    if (rank == 0) ctl->nblocks = (int)gridDim.x;
     const int bsz = 64 * W;
     const int nbatch = (a.k + bsz - 1) / bsz;
     // First-discovery stamps carry level tags that grow across the launch's batches
@@ -1496,6 +1518,7 @@ __global__ void __launch_bounds__(MS_THREADS, MS_MIN_BLOCKS) ms_grid_kernel(MsAr
             if (W > 1 && tag_base == 0)
                 for (long long w = rank; w < a.n; w += size) a.stamp[w] = 0;
         }
+        if (rank == 0) ctl->wo_next = 0;
         if (rank < 4) {
             ctl->qpack[rank] = 0;
             ctl->work[rank] = 0;
@@ -1503,7 +1526,7 @@ __global__ void __launch_bounds__(MS_THREADS, MS_MIN_BLOCKS) ms_grid_kernel(MsAr
             for (int q = 0; q < MAXW; ++q) ctl->active[rank][q] = 0;
         }
         if (rank < 4 * COVER_SLOT) a.cover[rank] = 0;
-        if (!barrier()) return;
+        if (!barrier(ev_idx)) return;
         if (rank < nb) {
             const int32_t s = __ldg(a.sources + row0 + rank);
             if ((unsigned)s >= (unsigned)a.n) {  // reported by the call; its row is never seeded
@@ -1523,7 +1546,7 @@ __global__ void __launch_bounds__(MS_THREADS, MS_MIN_BLOCKS) ms_grid_kernel(MsAr
     seeded:
         if (threadIdx.x == 0) record_event(ctl, ev_idx, rank == 0, b, 0, 4, nb, 0);  // batch initialised, seeded
         ++ev_idx;
-        if (!barrier()) return;
+        if (!barrier(ev_idx - 1)) return;
 
         bool prev_bu = false;
         int j = 1;
@@ -1590,7 +1613,7 @@ __global__ void __launch_bounds__(MS_THREADS, MS_MIN_BLOCKS) ms_grid_kernel(MsAr
                 // timeline kinds 5-7: parts A and B, and the light class within B
                 if (threadIdx.x == 0) record_event(ctl, ev_idx, rank == 0, b, j, 5, L.qlen, L.qedges);
                 ++ev_idx;
-                if (!barrier()) return;
+                if (!barrier(ev_idx - 1)) return;
                 // part B: sources searched bottom-up and rare ones, from the coverage
                 if (threadIdx.x < 64 * W) {
                     const float c = (float)ld_volatile_i32(&a.cover[L.slot * COVER_SLOT + threadIdx.x]);
@@ -1625,7 +1648,7 @@ __global__ void __launch_bounds__(MS_THREADS, MS_MIN_BLOCKS) ms_grid_kernel(MsAr
                 if (L.rare_td) {  // part C
                     if (threadIdx.x == 0) record_event(ctl, ev_idx, rank == 0, b, j, 7, L.qlen, L.qedges);
                     ++ev_idx;
-                    if (!barrier()) return;
+                    if (!barrier(ev_idx - 1)) return;
                     const u64 rp = s_ctl.rpack;
                     Lvl LC = L;
                     LC.qcur = a.q[L.prv];
@@ -1650,7 +1673,7 @@ __global__ void __launch_bounds__(MS_THREADS, MS_MIN_BLOCKS) ms_grid_kernel(MsAr
                 else if (VARIANT == GU_BFS_LINEAR) gather_linear<W, GridG>(a, L);
                 else gather_mp<W, GridG>(a, L);  // AUTO, BOTTOM_UP level 1
                 if (L.scanq) {
-                    if (!barrier()) return;  // every claim of the level is in F_j
+                    if (!barrier(ev_idx)) return;  // every claim of the level is in F_j
                     const CtaQ cq{reinterpret_cast<int32_t *>(ms_smem()), cq_count(), MS_SMEM_BYTES / 4};
                     for (long long v = rank; v < a.n; v += size) {
                         const size_t o = (size_t)v * W;
@@ -1688,7 +1711,7 @@ __global__ void __launch_bounds__(MS_THREADS, MS_MIN_BLOCKS) ms_grid_kernel(MsAr
             if (threadIdx.x == 0) record_event(ctl, ev_idx, rank == 0, b, j, bu ? 1 : 0, L.qlen, L.qedges);
             ++ev_idx;
             prev_bu = bu;
-            if (!barrier()) return;
+            if (!barrier(ev_idx - 1)) return;
         }
         // F_{j-1} is empty: levels of this batch are 0..j-2.  F_{j-2} is the only
         // frontier array with bits left: clear it through its queue, so that the
@@ -1706,7 +1729,7 @@ __global__ void __launch_bounds__(MS_THREADS, MS_MIN_BLOCKS) ms_grid_kernel(MsAr
         if (a.reach) count_reached<W, GridG>(a, row0, nb);
         if (threadIdx.x == 0) record_event(ctl, ev_idx, rank == 0, b, j, 2, 0, 0);  // distance rows written
         ++ev_idx;
-        if (!barrier()) return;
+        if (!barrier(ev_idx - 1)) return;
     }
 }
 
@@ -1908,6 +1931,23 @@ int msbfs_read_timeline(DeviceGraph &g, int max_entries, int32_t *batch, int32_t
         if (frontier_edges) frontier_edges[i] = ev[i].qedges;
         if (t_ms) t_ms[i] = (double)(ev[i].t_last_ns - ev[0].t_last_ns) * 1e-6;
     }
+    return nout;
+}
+
+// Idle CTA time per phase of the last batched launch (after a stream sync): for
+// each timeline entry, the sum over CTAs of their waits at the grid barriers of
+// that phase, in ms; *nblocks = the launch's CTAs.
+int msbfs_read_idle(DeviceGraph &g, int max_entries, double *idle_ms, int *nblocks)
+{
+    std::vector<char> buf(CTL_REGION);
+    GU_CUDA_CHECK(cudaMemcpy(buf.data(), g.ws.ptr, CTL_REGION, cudaMemcpyDeviceToHost));
+    const MsCtl *c = reinterpret_cast<const MsCtl *>(buf.data());
+    const MsEvent *ev = reinterpret_cast<const MsEvent *>(buf.data() + 256);
+    const int cnt = *reinterpret_cast<const int *>(ev + TIMELINE_MAX);
+    const int nout = cnt < max_entries ? cnt : max_entries;
+    for (int i = 0; i < nout; ++i)
+        if (idle_ms) idle_ms[i] = (double)ev[i].idle_ns * 1e-6;
+    if (nblocks) *nblocks = c->nblocks;
     return nout;
 }
 

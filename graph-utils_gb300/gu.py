@@ -96,6 +96,8 @@ def lib():
                                   ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
         "gu_graph_launch_times": ([_vp, ctypes.c_int, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int)],
                                   ctypes.c_int),
+        "gu_graph_level_idle": ([_vp, ctypes.c_int, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int),
+                                 ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
         "gu_graph_autotune": ([_vp, _vp, ctypes.c_int32, ctypes.POINTER(GuTuning), ctypes.POINTER(GuTuning),
                                ctypes.c_int, ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
         "gu_graph_set_tuning": ([_vp, ctypes.POINTER(GuTuning)], ctypes.c_int),
@@ -319,6 +321,14 @@ class Graph:
         return [dict(batch=int(b[i]), level=int(lv[i]), kind=kinds.get(int(kd[i]), "?"),
                      frontier_vertices=int(fv[i]), frontier_edges=int(fe[i]), t_ms=float(t[i]))
                 for i in range(cnt.value)]
+
+    def level_idle(self, max_entries=1024):
+        """(idle CTA-ms per timeline entry, CTAs of the launch) of the last batched search."""
+        out = np.zeros(max_entries, np.float64)
+        nb, cnt = ctypes.c_int(), ctypes.c_int()
+        check(lib().gu_graph_level_idle(self._h, max_entries, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                        ctypes.byref(nb), ctypes.byref(cnt)))
+        return out[:cnt.value].copy(), nb.value
 
     def bfs(self, sources_dev, dist_dev, variant="auto", ld=None, stream=None):
         """Device form: sources_dev (int32 cuda tensor, k), dist_dev (int32 cuda tensor, k x ld)."""

@@ -199,6 +199,12 @@ gu_status gu_graph_launch_times(gu_graph g, int max_entries, double *kernel_seco
 gu_status gu_graph_level_profile(gu_graph g, int max_entries, int32_t *batch, int32_t *level, int32_t *kind,
                                  int64_t *frontier_vertices, int64_t *frontier_edges, double *t_ms, int *count);
 
+/* Idle time of the last batched search per timeline entry (the entries of
+ * gu_graph_level_profile, same order): the sum over the launch's CTAs of the
+ * time each waited at the grid barriers of that phase, in CTA-milliseconds;
+ * *nblocks = the launch's CTAs.  Batched search only.  No reference counterpart. */
+gu_status gu_graph_level_idle(gu_graph g, int max_entries, double *idle_cta_ms, int *nblocks, int *count);
+
 /* ---- autotuning AUTO --------------------------------------------------------- */
 /* AUTO's built-in choice goes by graph shape (out-degree, size) and fixed
  * direction thresholds.  gu_graph_autotune measures instead: it runs the

@@ -286,3 +286,27 @@ def test_launch_times_ring():
     assert len(t) == 64 and all(x > 0 for x in t)
     assert t[-1] == pytest.approx(g.last_launch()[0])
     assert len(g.launch_times(5)) == 5
+
+
+def test_level_idle_per_phase():
+    """gu_graph_level_idle: one entry per timeline phase, the CTAs' barrier waits,
+    between zero and the phase's duration times the launch's CTAs."""
+    hg = gu.HostGraph.rmat(15, 16, seed=2)
+    g = gu.Graph(hg)
+    srcs = gu.sources(hg.n, 300, seed=4)
+    ref, _ = oracle.bfs_multi(hg.R, hg.C, hg.n, srcs, nthreads=8)
+    np.testing.assert_array_equal(run_bfs(g, srcs, "auto_batched")[0], ref)
+    tl = g.level_profile()
+    idle, nblocks = g.level_idle()
+    assert len(idle) == len(tl) and nblocks >= torch.cuda.get_device_properties(0).multi_processor_count
+    assert (idle >= 0).all() and idle.sum() > 0
+    t = [0.0] + [e["t_ms"] for e in tl]
+    for i in range(1, len(tl)):
+        # a phase's waits end with the barrier after it; the slowest CTA's stamp
+        # precedes that barrier, so allow the barrier's own time on top
+        assert idle[i] <= (t[i + 1] - t[i] + 0.05) * nblocks, i
+    g2 = gu.Graph(gu.HostGraph.rmat(12, 8, seed=1))
+    g2.bc(torch.as_tensor(gu.sources(g2.n, 64, seed=1), device="cuda"),
+          torch.empty(g2.n, dtype=torch.float64, device="cuda"))
+    with pytest.raises(gu.GuError):
+        g2.level_idle()  # BC passes have no idle record
