@@ -51,6 +51,9 @@ def parse_args():
     p.add_argument("--variant", default="auto")
     p.add_argument("--scale", type=int, default=SCALE)
     p.add_argument("--sources", type=int, default=K_SOURCES)
+    p.add_argument("--autotune", action="store_true",
+                   help="before the timed region, time AUTO's candidates on the workload's sources "
+                        "(gu_graph_autotune) and keep the fastest; reported under 'tuning'")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cpu-seconds", type=float, default=15.0, help="budget of the cpu_baseline sample")
     p.add_argument("--kernel-only", action="store_true", help="skip e2e (for profiling runs)")
@@ -149,7 +152,7 @@ def roofline_line(traffic, traffic_src, kt_avg, alg_eff, alg_min, peak, peak_kin
             "frac": phys / peak if phys else None, "traffic": traffic,
             "peak_source": f"{peak_kind} hbm_gbs (MEASURED_PEAKS.json)" if peak_kind == "measured"
             else "fallback 6800 GB/s",
-            "kernel": "gu::ms_grid_kernel<AUTO,4>", "kernel_ms": 1e3 * kt_avg,
+            "kernel": "gu::ms_grid_kernel<V,4>", "kernel_ms": 1e3 * kt_avg,
             "achieved_basis": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch (traffic, "
                               "profiles/ms_grid_kernel_auto_rmat20.md) / this run's mean CUDA-event kernel time",
             "traffic_kernel_source_sha16": traffic_src, "kernel_source_sha16": src_now,
@@ -324,6 +327,11 @@ def run_ours(args):
     dist_buf = torch.empty((len(srcs), hg.n), dtype=torch.int32, device=dev)
     deg = torch.as_tensor(np.diff(hg.R).astype(np.float64), device=dev)
 
+    tuning = None
+    if args.autotune:
+        best, trials = g.autotune(s_dev)
+        tuning = {"best": best, "trials": len(trials)}
+
     def step():
         g.bfs(s_dev, dist_buf, variant=args.variant, stream=stream)
 
@@ -407,6 +415,7 @@ def run_ours(args):
                 "data": "synthetic",
                 "config": config_of(args, hg),
                 "workload_stats": {"edges_per_step": gteps_edges, "levels_td_bu_max": levels},
+                "tuning": tuning,
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
                 "gpu_launches": args.steps}
         if power:
