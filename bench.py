@@ -14,6 +14,11 @@ reaches (Graph500 convention: sum over sources of scanned CSR entries / 2).
 ours:      `value`  -- device-resident inputs, CUDA events around K steps.
            `e2e`    -- the C-ABI host-buffer call (gu_bfs_host): pinned host
                        sources in, pinned host distance rows out, copies inside.
+Also on the default line (one GPU): `bc`, sampled Brandes BC on R-MAT scale 18
+(8192 sources, 1024 per pass: GTEPS, kernel time, physical DRAM fraction, error
+against the FP64 oracle), and `serve`, a short serving run (p50 / p99 at a
+moderate rate; saturation throughput against one call per request).
+
 reference: the oracle port of the reference CPU path
            (examples/multi_search/multi_search_test.cu:17-38) on all host
            threads, each step a bounded sample of the sources.
@@ -54,12 +59,14 @@ def parse_args():
     p.add_argument("--autotune", action="store_true",
                    help="before the timed region, time AUTO's candidates on the workload's sources "
                         "(gu_graph_autotune) and keep the fastest; reported under 'tuning'")
+    p.add_argument("--no-sublines", action="store_true",
+                   help="leave out the sampled-BC and serving objects of the default line")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cpu-seconds", type=float, default=15.0, help="budget of the cpu_baseline sample")
     p.add_argument("--kernel-only", action="store_true", help="skip e2e (for profiling runs)")
     p.add_argument("--power", action="store_true",
                    help="sample board power (NVML, read-only) during the timed region: adds a power object")
-    p.add_argument("--workload", choices=["c2", "c1", "c3", "c3-pass", "c4", "c4-pass", "c5", "io", "dag"], default="c2",
+    p.add_argument("--workload", choices=["c2", "c1", "c3", "c3-pass", "c3-launch", "c4", "c4-pass", "c5", "io", "dag"], default="c2",
                    help="c2: the headline BFS line (default); c1/c3/c4/c5/io/dag: the other configurations, "
                         "one JSON line each (bench_configs.py)")
     return p.parse_args()
@@ -408,6 +415,15 @@ def run_ours(args):
                "sample": f"first {nsrc} of the {len(srcs)} workload sources, oracle port of "
                          f"multi_search_test.cu:17-38 on {cores} host threads, {t_cpu:.1f} s"}
 
+    sub = {}
+    if rank == 0 and ws == 1 and not (args.kernel_only or args.no_sublines):
+        import bench_configs
+        g.close()
+        del dist_buf
+        torch.cuda.empty_cache()
+        sub["bc"] = bench_configs.bc_subline(torch)
+        sub["serve"] = bench_configs.serve_subline(torch)
+
     if rank == 0:
         line = {"metric": "multi-source BFS GTEPS", "value": value, "unit": "GTEPS", "n_gpus": ws,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_total / args.steps,
@@ -420,6 +436,7 @@ def run_ours(args):
                 "gpu_launches": args.steps}
         if power:
             line["power"] = power
+        line.update(sub)
         print(json.dumps(line), flush=True)
     g.close()
     if ws > 1:

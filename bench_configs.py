@@ -127,6 +127,97 @@ def _hbm_peak():
         return 6800.0
 
 
+BC_PROFILE = os.path.join(ROOT, "profiles", "bc_grid_kernel_rmat18.md")
+
+
+def _profile_value(path, key):
+    """A `key: value` line of a committed profile summary (None if absent)."""
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        k, _, v = line.partition(":")
+        if k == key:
+            return v.strip()
+    return None
+
+
+def source_hash(files):
+    """sha256 (first 16 hex digits) of kernel sources, as the profile summaries record it."""
+    import hashlib
+    h = hashlib.sha256()
+    for f in files:
+        with open(os.path.join(ROOT, "graph-utils_gb300", "csrc", f), "rb") as fh:
+            h.update(fh.read())
+    return h.hexdigest()[:16]
+
+
+BC_SOURCES = ("bc.cu", "device_utils.cuh", "gu_internal.h")
+
+
+def bc_subline(torch):
+    """Sampled BC for the default bench line: R-MAT scale 18 (ef 16, seed 1), 8192 sources
+    (seed 2) in passes of 1024 in one persistent launch; kernel time (median of 3 after a
+    warm-up), GTEPS of forward-sweep edges, the launch's physical DRAM fraction (ncu bytes of
+    the same launch from the committed profile, with the build it was taken on), and the
+    largest relative error against the FP64 oracle over the first 256 sources."""
+    import gu
+    import oracle
+    cores = os.cpu_count() or 1
+    hg = gu.HostGraph.rmat(18, 16, 0.57, 0.19, 0.19, seed=1, permute=True)
+    g = gu.Graph(hg)
+    srcs = gu.sources(hg.n, 8192, seed=2)
+    deg = torch.as_tensor(np.diff(hg.R).astype(np.float64), device="cuda")
+    E, V = _edges_reached(torch, g, srcs, deg)
+    edges = E / 2.0
+    s = torch.as_tensor(srcs, device="cuda")
+    bc = torch.empty(hg.n, dtype=torch.float64, device="cuda")
+    g.bc(s, bc, batch=1024)
+    times = []
+    for _ in range(3):
+        g.bc(s, bc, batch=1024)
+        times.append(g.last_launch()[0])
+    kt = statistics.median(times)
+    g.bc(s[:256], bc, batch=256)
+    got = bc.cpu().numpy()
+    want = oracle.bc(hg.R, hg.C, hg.n, srcs[:256], nthreads=cores)
+    diff = np.abs(got - want)
+    rel = np.where(diff > 1e-300, diff / np.maximum(np.abs(want), 1e-300), 0.0)
+    peak = _hbm_peak()
+    tr = _profile_value(BC_PROFILE, "traffic_bytes_per_launch_8192src_batch1024")
+    tr = int(tr) if tr else None
+    src_prof = _profile_value(BC_PROFILE, "kernel_source_sha16")
+    src_now = source_hash(BC_SOURCES)
+    alg = len(srcs) * 28.0 * hg.n + 32.0 * V + 40.0 * E
+    g.close()
+    return {"workload": "rmat18_ef16_8192src_bc_batch1024", "unit": "GTEPS", "value": edges / kt / 1e9,
+            "kernel_ms": kt * 1e3, "edges": edges, "dtype": "u64 sigma, f64 delta/bc",
+            "max_rel_err_256src": float(rel.max()), "tolerance": 1e-12,
+            "roofline": {"bound": "hbm", "traffic": tr, "achieved": tr / kt / 1e9 if tr else None,
+                         "peak": peak, "unit": "GB/s", "frac": tr / kt / 1e9 / peak if tr else None,
+                         "traffic_kernel_source_sha16": src_prof, "kernel_source_sha16": src_now,
+                         "traffic_matches_build": src_prof == src_now,
+                         "effective_frac": alg / kt / 1e9 / peak,
+                         "effective_model": "per-source 28n + 32 V_s + 40 E_s (a pass shares its reads among "
+                                            "up to 1024 sources, so this can exceed 1)"}}
+
+
+def wl_c3_launch(args):
+    """Profiling case: the sampled-BC launch of the default bench line (8192 sources of the
+    C3 graph, 1024 per pass), three times; prints the kernel times."""
+    import gu
+    torch = _torch()
+    hg = gu.HostGraph.rmat(18, 16, 0.57, 0.19, 0.19, seed=1, permute=True)
+    g = gu.Graph(hg)
+    s = torch.as_tensor(gu.sources(hg.n, 8192, seed=2), device="cuda")
+    bc = torch.empty(hg.n, dtype=torch.float64, device="cuda")
+    times = []
+    for _ in range(3):
+        g.bc(s, bc, batch=1024)
+        times.append(g.last_launch()[0] * 1e3)
+    _emit({"workload": "c3_launch_rmat18_8192src_bc_batch1024", "metric": "kernel time of the BC launch",
+           "unit": "ms", "kernel_ms": times})
+
+
 def wl_c3_pass(args):
     """Profiling case: one Brandes pass over 256 of the C3 sources (batch 256), three
     times, on the C3 graph; prints the kernel times and the pass's phase timeline."""
@@ -203,6 +294,12 @@ def wl_c3(args):
     # and backward reads of the adjacency, levels, sigma and delta per reached vertex and edge)
     alg = len(srcs) * 28.0 * hg.n + 32.0 * V + 40.0 * E
     best = min(res[f"bc_batch{b}_kernel_ms"] for b in (64, 128, 256, 512, 1024))
+    # accuracy on a fixed subset (the first 256 sources, one pass of 256) against the FP64 oracle
+    g.bc(s[:256], bc, batch=256)
+    got = bc.cpu().numpy()
+    want = oracle.bc(hg.R, hg.C, hg.n, srcs[:256], nthreads=cores)
+    diff = np.abs(got - want)
+    res["max_rel_err_first256"] = float(np.where(diff > 1e-300, diff / np.maximum(np.abs(want), 1e-300), 0).max())
     sub1, subN = srcs[:4], srcs[:4 * cores]
     _, c1 = _cpu(oracle.bc, hg.R, hg.C, hg.n, sub1, nthreads=1)
     _, cN = _cpu(oracle.bc, hg.R, hg.C, hg.n, subN, nthreads=cores)
@@ -260,102 +357,112 @@ def wl_c4(args):
                        "sample": f"first {len(sub)} sources, per-source edges from the full set"}})
 
 
-def wl_c5(args):
+def _serving_set(torch, n_rmat, scales, n_dag, dag_log2, rng):
+    """R-MAT graphs and random DAGs resident on the device (a serving replica's set),
+    with the per-vertex component edge counts GTEPS needs."""
     import gu
-    import oracle
-    torch = _torch()
-    rng = np.random.default_rng(5)
-    # 12 R-MAT graphs, scales 12-18 and edge factors 8/16/32, and 4 random DAGs
-    # (n from 2^16 to 2^18, m = 8n): the resident set of a serving replica
+    import scipy.sparse
+    import scipy.sparse.csgraph
     rmats, dags = [], []
-    for i in range(12):
-        sc, ef = int(rng.integers(12, 19)), int(rng.choice([8, 16, 32]))
+    for i in range(n_rmat):
+        sc, ef = int(rng.integers(scales[0], scales[1] + 1)), int(rng.choice([8, 16, 32]))
         hg = gu.HostGraph.rmat(sc, ef, 0.57, 0.19, 0.19, seed=100 + i, permute=True)
         rmats.append((f"rmat{sc}_ef{ef}_s{100 + i}", hg, gu.Graph(hg)))
-    for i in range(4):
-        n = int(2 ** rng.uniform(16, 18))
+    for i in range(n_dag):
+        n = int(2 ** rng.uniform(dag_log2[0], dag_log2[1]))
         hg = gu.HostGraph.dag(n, 8 * n, seed=200 + i)
         dags.append((f"dag{n}_s{200 + i}", hg, gu.Graph(hg)))
     torch.cuda.synchronize()
     # edges a search from s traverses on an undirected graph: its component's CSR entries
     # (each undirected edge once per direction); GTEPS counts them once, as the other lines do
-    import scipy.sparse
-    import scipy.sparse.csgraph
     comp_edges = {}
     for name, hg, g in rmats:
         A = scipy.sparse.csr_matrix((np.ones(hg.m, np.int8), hg.C, hg.R), shape=(hg.n, hg.n))
         _, lab = scipy.sparse.csgraph.connected_components(A, directed=False)
         per = np.bincount(lab, weights=np.diff(hg.R).astype(np.float64))
         comp_edges[id(hg)] = per[lab] / 2.0
+    return rmats, dags, comp_edges
 
-    def req_edges(q, hg, srcs):
-        return float(comp_edges[id(hg)][srcs].sum()) if q != gu.QUERY_REACH else 0.0
-    results = []
-    cpu_ms = []
+
+def _serving_plan(rng, rmats, dags, rate, dur, bc_max):
+    """Poisson arrivals: 60% BFS rows (1-256 sources), 20% BC (64-bc_max), 20% DAG reachable counts (1-256)."""
+    import gu
+    plan, t = [], 0.0
+    while t < dur:
+        t += float(rng.exponential(1.0 / rate))
+        u = rng.random()
+        if u < 0.6:
+            name, hg, g = rmats[int(rng.integers(len(rmats)))]
+            k = int(rng.integers(1, 257))
+            plan.append((t, gu.QUERY_BFS, hg, g, rng.choice(hg.n, k, replace=False).astype(np.int32)))
+        elif u < 0.8:
+            name, hg, g = rmats[int(rng.integers(len(rmats)))]
+            k = int(rng.integers(64, bc_max + 1))
+            plan.append((t, gu.QUERY_BC, hg, g, rng.choice(hg.n, k, replace=False).astype(np.int32)))
+        else:
+            name, hg, g = dags[int(rng.integers(len(dags)))]
+            k = int(rng.integers(1, 257))
+            plan.append((t, gu.QUERY_REACH, hg, g, rng.choice(hg.n, k, replace=False).astype(np.int32)))
+    return plan
+
+
+def _req_edges(comp_edges, q, hg, srcs):
+    import gu
+    return float(comp_edges[id(hg)][srcs].sum()) if q != gu.QUERY_REACH else 0.0
+
+
+def _serve_stream(plan, comp_edges, slots=4, max_batch=1024):
+    """Runs one open-loop request stream through a gu.Server; latency from the planned arrival."""
+    import gu
     import queue
     import threading
-    for rate in (100.0, 400.0, 1600.0, 3200.0, 6400.0):
-        srv = gu.Server(hbm_budget_bytes=64 << 30, slots=4, max_batch=1024)
-        plan, t = [], 0.0
-        dur = 2.0
-        while t < dur:
-            t += float(rng.exponential(1.0 / rate))
-            u = rng.random()
-            if u < 0.6:
-                name, hg, g = rmats[int(rng.integers(len(rmats)))]
-                k = int(rng.integers(1, 257))
-                plan.append((t, gu.QUERY_BFS, hg, g, rng.choice(hg.n, k, replace=False).astype(np.int32)))
-            elif u < 0.8:
-                name, hg, g = rmats[int(rng.integers(len(rmats)))]
-                k = int(rng.integers(64, 257))
-                plan.append((t, gu.QUERY_BC, hg, g, rng.choice(hg.n, k, replace=False).astype(np.int32)))
-            else:
-                name, hg, g = dags[int(rng.integers(len(dags)))]
-                k = int(rng.integers(1, 257))
-                plan.append((t, gu.QUERY_REACH, hg, g, rng.choice(hg.n, k, replace=False).astype(np.int32)))
-        pending = queue.Queue()
-        lat = []  # open-loop latency: from the planned arrival, so a late submit counts
+    srv = gu.Server(hbm_budget_bytes=64 << 30, slots=slots, max_batch=max_batch)
+    pending = queue.Queue()
+    lat = []  # open-loop latency: from the planned arrival, so a late submit counts
 
-        def waiter():  # waits in submission order, so finished outputs are released as it goes
-            while True:
-                item = pending.get()
-                if item is None:
-                    return
-                rid, lag = item
-                lat.append(srv.wait(rid) + lag)
+    def waiter():  # waits in submission order, so finished outputs are released as it goes
+        while True:
+            item = pending.get()
+            if item is None:
+                return
+            rid, lag = item
+            lat.append(srv.wait(rid) + lag)
 
-        th = threading.Thread(target=waiter)
-        th.start()
-        t0 = time.perf_counter()
-        for (ta, q, hg, g, srcs) in plan:
-            now = time.perf_counter() - t0
-            if ta > now:
-                time.sleep(ta - now)
-            if q == gu.QUERY_BFS:
-                out = np.empty((len(srcs), hg.n), np.int32)
-            elif q == gu.QUERY_BC:
-                out = np.empty(hg.n, np.float64)
-            else:
-                out = np.empty(len(srcs), np.int64)
-            rid = srv.submit(g, q, srcs, out)
-            pending.put((rid, max(0.0, time.perf_counter() - t0 - ta)))
-        pending.put(None)
-        th.join()
-        wall = time.perf_counter() - t0
-        st = srv.stats()
-        srv.close()
-        lat.sort()
-        edges = sum(req_edges(q, hg, srcs) for (_, q, hg, _, srcs) in plan)
-        results.append({"offered_rate_per_s": rate, "requests": len(plan), "wall_s": wall,
-                        "served_per_s": len(plan) / wall, "served_gteps_bfs_bc": edges / wall / 1e9,
-                        "p50_ms": 1e3 * lat[len(lat) // 2], "p99_ms": 1e3 * lat[min(len(lat) - 1, int(0.99 * len(lat)))],
-                        "server_p50_ms": st["p50_s"] * 1e3, "server_p99_ms": st["p99_s"] * 1e3,
-                        "batches": st["batches"], "mean_requests_per_batch": st["mean_requests_per_batch"]})
-    # the same request stream one call per request, no batching or overlap (the plain form):
-    # host sources in, host results out, as the server's requests
-    sample = plan[:2000]
+    th = threading.Thread(target=waiter)
+    th.start()
     t0 = time.perf_counter()
-    for (_, q, hg, g, srcs) in sample:
+    for (ta, q, hg, g, srcs) in plan:
+        now = time.perf_counter() - t0
+        if ta > now:
+            time.sleep(ta - now)
+        if q == gu.QUERY_BFS:
+            out = np.empty((len(srcs), hg.n), np.int32)
+        elif q == gu.QUERY_BC:
+            out = np.empty(hg.n, np.float64)
+        else:
+            out = np.empty(len(srcs), np.int64)
+        rid = srv.submit(g, q, srcs, out)
+        pending.put((rid, max(0.0, time.perf_counter() - t0 - ta)))
+    pending.put(None)
+    th.join()
+    wall = time.perf_counter() - t0
+    st = srv.stats()
+    srv.close()
+    lat.sort()
+    edges = sum(_req_edges(comp_edges, q, hg, srcs) for (_, q, hg, _, srcs) in plan)
+    return {"requests": len(plan), "wall_s": wall,
+            "served_per_s": len(plan) / wall, "served_gteps_bfs_bc": edges / wall / 1e9,
+            "p50_ms": 1e3 * lat[len(lat) // 2], "p99_ms": 1e3 * lat[min(len(lat) - 1, int(0.99 * len(lat)))],
+            "server_p50_ms": st["p50_s"] * 1e3, "server_p99_ms": st["p99_s"] * 1e3,
+            "batches": st["batches"], "mean_requests_per_batch": st["mean_requests_per_batch"]}
+
+
+def _one_call_per_request(torch, plan, comp_edges):
+    """The same requests one synchronous C-ABI call each (host sources in, host results
+    out), no batching and no overlap: the plain per-request form."""
+    import gu
+    t0 = time.perf_counter()
+    for (_, q, hg, g, srcs) in plan:
         if q == gu.QUERY_BFS:
             g.bfs_host(srcs, variant="auto")
         else:
@@ -368,11 +475,61 @@ def wl_c5(args):
                 g.reach(sd, o)
             o.cpu()
     torch.cuda.synchronize()
-    one_wall = time.perf_counter() - t0
-    one_edges = sum(req_edges(q, hg, srcs) for (_, q, hg, _, srcs) in sample)
-    one_by_one = {"requests": len(sample), "wall_s": one_wall, "requests_per_s": len(sample) / one_wall,
-                  "gteps_bfs_bc": one_edges / one_wall / 1e9,
-                  "note": "the first 2000 requests of the last rate's stream, one synchronous call per request"}
+    wall = time.perf_counter() - t0
+    edges = sum(_req_edges(comp_edges, q, hg, srcs) for (_, q, hg, _, srcs) in plan)
+    return {"requests": len(plan), "wall_s": wall, "requests_per_s": len(plan) / wall,
+            "gteps_bfs_bc": edges / wall / 1e9}
+
+
+def serve_subline(torch, rate=800.0, seconds=1.0, burst=2000):
+    """Short serving run for the default bench line, on 6 R-MAT graphs (scales 12-16) and 2
+    random DAGs (n about 2^16) resident on the device, with the C5 request mix (BC of 64-256
+    sources): p50 / p99 latency of a Poisson stream at `rate`, and at saturation (`burst`
+    requests submitted at once) the served throughput against the same requests issued one
+    synchronous call each."""
+    rng = np.random.default_rng(11)
+    rmats, dags, comp = _serving_set(torch, 6, (12, 16), 2, (16, 16.5), rng)
+    plan = _serving_plan(rng, rmats, dags, rate, seconds, 256)
+    lat = _serve_stream(plan, comp)
+    sat_plan = [(0.0,) + p[1:] for p in _serving_plan(rng, rmats, dags, float(burst), 1.0, 256)[:burst]]
+    sat = _serve_stream(sat_plan, comp)
+    plain = _one_call_per_request(torch, sat_plan, comp)
+    for _, _, g in rmats + dags:
+        g.close()
+    return {"workload": "6 R-MAT graphs (scales 12-16, ef 8/16/32) + 2 DAGs (n ~ 2^16, m = 8n); requests: 60% BFS "
+                        "rows (1-256 sources), 20% BC (64-256), 20% DAG reachable counts (1-256); host buffers in "
+                        "and out",
+            "latency": {"offered_rate_per_s": rate, "requests": lat["requests"], "p50_ms": lat["p50_ms"],
+                        "p99_ms": lat["p99_ms"], "mean_requests_per_batch": lat["mean_requests_per_batch"]},
+            "saturation": {"requests": sat["requests"], "served_per_s": sat["served_per_s"],
+                           "served_gteps_bfs_bc": sat["served_gteps_bfs_bc"],
+                           "mean_requests_per_batch": sat["mean_requests_per_batch"],
+                           "one_call_per_request_per_s": plain["requests_per_s"],
+                           "speedup_vs_one_call_per_request": sat["served_per_s"] / plain["requests_per_s"]},
+            "note": "latency is open-loop, from each request's planned arrival; at saturation every request is "
+                    "submitted at once and the one-call form runs the same requests back to back"}
+
+
+def wl_c5(args):
+    import gu
+    import oracle
+    torch = _torch()
+    rng = np.random.default_rng(5)
+    # 12 R-MAT graphs, scales 12-18 and edge factors 8/16/32, and 4 random DAGs
+    # (n from 2^16 to 2^18, m = 8n): the resident set of a serving replica
+    rmats, dags, comp_edges = _serving_set(torch, 12, (12, 18), 4, (16, 18), rng)
+    results = []
+    cpu_ms = []
+    plan = None
+    for rate in (100.0, 400.0, 1600.0, 3200.0, 6400.0):
+        plan = _serving_plan(rng, rmats, dags, rate, 2.0, 256)
+        r = _serve_stream(plan, comp_edges)
+        r["offered_rate_per_s"] = rate
+        results.append(r)
+    # the same request stream one call per request, no batching or overlap (the plain form):
+    # host sources in, host results out, as the server's requests
+    one_by_one = _one_call_per_request(torch, plan[:2000], comp_edges)
+    one_by_one["note"] = "the first 2000 requests of the last rate's stream, one synchronous call per request"
     # CPU: per-request oracle time on a sample of requests of each kind
     for (t_, q, hg, g, srcs) in plan[:24]:
         if q == gu.QUERY_BC:
@@ -474,4 +631,4 @@ def wl_dag(args):
 
 
 def run(workload, args):
-    {"c1": wl_c1, "c3": wl_c3, "c3-pass": wl_c3_pass, "c4": wl_c4, "c4-pass": wl_c4_pass, "c5": wl_c5, "io": wl_io, "dag": wl_dag}[workload](args)
+    {"c1": wl_c1, "c3": wl_c3, "c3-pass": wl_c3_pass, "c3-launch": wl_c3_launch, "c4": wl_c4, "c4-pass": wl_c4_pass, "c5": wl_c5, "io": wl_io, "dag": wl_dag}[workload](args)
