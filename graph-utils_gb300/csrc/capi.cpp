@@ -793,6 +793,54 @@ gu_status gu_race_and_resolve(const int32_t *predicates_dev, int32_t nwarps, int
     });
 }
 
+// ---- many searches in one work-queue launch -----------------------------------------
+gu_status gu_bfs_many(const gu_search_item *items, int32_t count, void *stream)
+{
+    return guarded([&] {
+        if (count < 0 || (count > 0 && !items)) throw gu_error(GU_ERR_INVALID_ARGUMENT, "bad item list");
+        if (count == 0) return;
+        std::vector<DeviceGraph *> graphs;
+        for (int32_t i = 0; i < count; ++i) {
+            if (!items[i].graph) throw gu_error(GU_ERR_INVALID_ARGUMENT, "null graph in item " + std::to_string(i));
+            graphs.push_back(items[i].graph->g.get());
+        }
+        const int dev = graphs[0]->device;
+        for (DeviceGraph *g : graphs)
+            if (g->device != dev) throw gu_error(GU_ERR_INVALID_ARGUMENT, "all graphs must live on one device");
+        std::sort(graphs.begin(), graphs.end());
+        graphs.erase(std::unique(graphs.begin(), graphs.end()), graphs.end());
+        std::vector<std::unique_lock<std::mutex>> locks;  // in address order: no lock-order cycle
+        for (DeviceGraph *g : graphs) locks.emplace_back(g->mu);
+        DeviceScope ds(dev);
+        std::vector<MsQueueRequest> reqs((size_t)count);
+        for (int32_t i = 0; i < count; ++i) {
+            const gu_search_item &it = items[i];
+            MsQueueRequest &r = reqs[(size_t)i];
+            r.g = it.graph->g.get();
+            r.sources = it.sources_dev;
+            r.k = it.k;
+            r.dist = it.dist_dev;
+            r.ld = it.ld;
+            r.reach = reinterpret_cast<unsigned long long *>(it.reach_dev);
+            if (it.k < 0) throw gu_error(GU_ERR_INVALID_ARGUMENT, "k must be >= 0 (item " + std::to_string(i) + ")");
+            if (it.k > 0 && (!it.sources_dev || (!it.dist_dev && !it.reach_dev)))
+                throw gu_error(GU_ERR_INVALID_ARGUMENT, "item " + std::to_string(i) + " needs sources and an output");
+            if (it.dist_dev && it.ld < r.g->n) throw gu_error(GU_ERR_INVALID_ARGUMENT, "ld must be >= n");
+        }
+        static std::mutex mu;  // the per-device queue workspace is one per process
+        static Workspace wsq[128];
+        if (dev < 0 || dev >= 128) throw gu_error(GU_ERR_UNSUPPORTED, "device ordinal out of range");
+        std::lock_guard<std::mutex> lk(mu);
+        cudaStream_t st = (cudaStream_t)stream;
+        const MsQueueLaunch L = launch_msbfs_queue(reqs, wsq[dev], graphs[0]->sm_count, 0, st);
+        GU_CUDA_CHECK(cudaStreamSynchronize(st));
+        const int e = msbfs_queue_error(wsq[dev], L);
+        if (e == DEV_ERR_BAD_SOURCE) throw gu_error(GU_ERR_INVALID_ARGUMENT, "source vertex out of range");
+        if (e == DEV_ERR_BARRIER_TIMEOUT) throw gu_error(GU_ERR_TIMEOUT, "a device-side wait exceeded its limit");
+        if (e != 0) throw gu_error(GU_ERR_INTERNAL, "device reported error code " + std::to_string(e));
+    });
+}
+
 // ---- serving -----------------------------------------------------------------------
 struct gu_server_s {
     Server *s = nullptr;

@@ -74,19 +74,23 @@ __device__ __forceinline__ u64 ld_volatile_u64(const u64 *p) { return *(const vo
 // (the error flag, and n 64-bit words from src into the shared dst): one
 // request per CTA instead of one per warp, all at the same address.
 //
+// nblocks: the CTAs that meet at the barrier (0: the whole grid; a CTA group of a
+// work-queue launch passes its own size and its own counter).
+//
 // The wait is bounded by limit_ns (a launch argument, gu_set_wait_limit; 4 s by
 // default): a wait that runs out records DEV_ERR_BARRIER_TIMEOUT in *err and
 // returns false; every block then leaves the kernel and the host reports
 // GU_ERR_TIMEOUT.  No wait is unbounded.
 __device__ __forceinline__ bool grid_barrier(unsigned *bar, int *err, unsigned &epoch, u64 limit_ns,
-                                             const u64 *src = nullptr, u64 *dst = nullptr, int n = 0)
+                                             const u64 *src = nullptr, u64 *dst = nullptr, int n = 0,
+                                             unsigned nblocks = 0)
 {
     __shared__ int s_ok;
     __syncthreads();
     if (threadIdx.x < 32) {
         if (threadIdx.x == 0) {
             epoch += 1;
-            const unsigned target = epoch * gridDim.x;
+            const unsigned target = epoch * (nblocks ? nblocks : gridDim.x);
             __threadfence();
             red_release_add_u32(bar, 1u);
             u64 t0 = 0;

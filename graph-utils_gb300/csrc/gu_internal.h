@@ -222,6 +222,27 @@ bool launch_local_bfs(DeviceGraph &g, const int32_t *sources, int32_t k, int32_t
 void launch_bc(DeviceGraph &g, const int32_t *sources, int32_t k, const BcOptions &opt, double *bc, int32_t *dist_rows,
                uint64_t *sigma_rows, double *delta_rows, int64_t ld, bool backward, cudaStream_t stream);
 size_t bc_workspace_bytes(const DeviceGraph &g, int32_t k, int batch, bool backward);
+// One request of a work-queue launch: BFS rows (dist, k x ld) and/or reachable
+// counts (reach, k) of k sources on graph g (any graph on the current device).
+struct MsQueueRequest {
+    DeviceGraph *g = nullptr;
+    const int32_t *sources = nullptr;
+    int32_t k = 0;
+    int32_t *dist = nullptr;
+    int64_t ld = 0;
+    unsigned long long *reach = nullptr;
+};
+struct MsQueueLaunch {
+    int ngroups = 0, group_size = 0, items = 0;
+    size_t stride = 0;  // bytes of workspace per group
+};
+// Runs every request in one persistent launch whose CTA groups drain a device
+// queue of (graph, source block) items (asynchronous on st; the graphs' lazily
+// built structures are not touched).  msbfs_queue_error reads the groups' device
+// error words once st is synchronised (0: none).
+MsQueueLaunch launch_msbfs_queue(const std::vector<MsQueueRequest> &reqs, Workspace &ws, int sms, int max_blocks,
+                                 cudaStream_t st);
+int msbfs_queue_error(const Workspace &ws, const MsQueueLaunch &L);
 size_t msbfs_workspace_bytes(const DeviceGraph &g, int32_t k);
 void bc_read_status(DeviceGraph &g, int *dev_err, int *max_level);
 int bc_read_timeline(DeviceGraph &g, int max_entries, int32_t *batch, int32_t *level, int32_t *kind,

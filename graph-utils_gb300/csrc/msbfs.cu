@@ -43,8 +43,11 @@
 #include "device_utils.cuh"
 #include "gu_internal.h"
 
+#include <algorithm>
 #include <climits>
+#include <cstddef>
 #include <cstdlib>
+#include <vector>
 
 namespace gu {
 
@@ -64,7 +67,8 @@ struct __align__(128) MsCtl {
     int bu_levels;
     int max_level;
     int nblocks;  // grid size of the launch (profiling)
-    int pad0[2];
+    int item;     // work-queue launch: the item the group works on (set by its first CTA)
+    int pad0;
     u64 qpack[4];
     int work[4];
     u64 rpack;  // bottom-up level: rare-source frontier list, (count << 38) | edges
@@ -166,6 +170,16 @@ struct GridG {
     __device__ static long long size() { return (long long)gridDim.x * blockDim.x; }
     __device__ static int blk() { return blockIdx.x; }
     __device__ static int nblk() { return gridDim.x; }
+};
+
+// One CTA group of a work-queue launch (ms_queue_kernel): CTAs [base, base + nblk)
+// of the grid, set by each CTA at the start of the launch.
+__shared__ int s_grp_base, s_grp_nblk;
+struct GroupG {
+    __device__ static long long rank() { return (long long)(blockIdx.x - s_grp_base) * blockDim.x + threadIdx.x; }
+    __device__ static long long size() { return (long long)s_grp_nblk * blockDim.x; }
+    __device__ static int blk() { return blockIdx.x - s_grp_base; }
+    __device__ static int nblk() { return s_grp_nblk; }
 };
 
 // One shared-memory buffer per CTA for the phases' staging (merge-path owners
@@ -1460,15 +1474,17 @@ __device__ void count_reached(const MsArgs &a, int row0, int nb)
     __syncthreads();
 }
 
-template <int VARIANT, int W>
-__global__ void __launch_bounds__(MS_THREADS, MS_MIN_BLOCKS) ms_grid_kernel(MsArgs a)
+// The batched search of one launch (G = the whole grid) or of one item of a
+// work-queue launch (G = the item's CTA group, whose barrier counter lives in the
+// item's control block).  epoch counts this CTA's barriers on that counter.
+template <int VARIANT, int W, class G>
+__device__ __forceinline__ void ms_search(const MsArgs &a, unsigned &epoch)
 {
     __shared__ u64 s_act[MAXW];
     // copy of the control block taken by each CTA's thread 0 after every barrier
     __shared__ MsCtl s_ctl;
     __shared__ u64 s_rare[MAXW];  // bottom-up level: rare sources expanded top-down
     __shared__ u64 s_excl[MAXW];  // ... and the sources it searches bottom-up
-    unsigned epoch = 0;
     int ev_idx = 0;
     MsCtl *ctl = a.ctl;
     // slot: the timeline entry whose phase the barrier ends (or is inside of); each
@@ -1476,17 +1492,18 @@ __global__ void __launch_bounds__(MS_THREADS, MS_MIN_BLOCKS) ms_grid_kernel(MsAr
     auto barrier = [&](int slot) {
         const u64 t_arrive = threadIdx.x == 0 ? global_timer_ns() : 0ull;
         const bool ok = grid_barrier(&ctl->bar, &ctl->err, epoch, a.wait_ns, reinterpret_cast<const u64 *>(ctl),
-                                     reinterpret_cast<u64 *>(&s_ctl), (int)(sizeof(MsCtl) / sizeof(u64)));
+                                     reinterpret_cast<u64 *>(&s_ctl), (int)(sizeof(MsCtl) / sizeof(u64)),
+                                     (unsigned)G::nblk());
         if (threadIdx.x == 0 && slot < TIMELINE_MAX)
             atomicAdd(&reinterpret_cast<MsEvent *>(reinterpret_cast<char *>(ctl) + 256)[slot].idle_ns,
                       global_timer_ns() - t_arrive);
         return ok;
     };
-    const long long rank = GridG::rank(), size = GridG::size();
+    const long long rank = G::rank(), size = G::size();
     const size_t pstride = (size_t)a.n * W;
     if (threadIdx.x < MAXW) s_act[threadIdx.x] = 0;
     if (threadIdx.x == 0) *cq_count() = 0;
-    if (rank == 0) ctl->nblocks = (int)gridDim.x;
+    if (rank == 0) ctl->nblocks = G::nblk();
     const int bsz = 64 * W;
     const int nbatch = (a.k + bsz - 1) / bsz;
     // First-discovery stamps carry level tags that grow across the launch's batches
@@ -1606,7 +1623,7 @@ __global__ void __launch_bounds__(MS_THREADS, MS_MIN_BLOCKS) ms_grid_kernel(MsAr
                     if ((unsigned)s0 < (unsigned)a.n) zerow<W>(L.fprv + (size_t)s0 * W);
                 }
                 if (rank == 0) ctl->rpack = 0;
-                bu_finalise_all<W, GridG>(a, L);
+                bu_finalise_all<W, G>(a, L);
                 __syncthreads();
                 if (threadIdx.x < 64 * W && ((s_act[threadIdx.x >> 6] >> (threadIdx.x & 63)) & 1ull))
                     atomicAdd(&a.cover[L.slot * COVER_SLOT + threadIdx.x], 1);
@@ -1617,7 +1634,7 @@ __global__ void __launch_bounds__(MS_THREADS, MS_MIN_BLOCKS) ms_grid_kernel(MsAr
                 // part B: sources searched bottom-up and rare ones, from the coverage
                 if (threadIdx.x < 64 * W) {
                     const float c = (float)ld_volatile_i32(&a.cover[L.slot * COVER_SLOT + threadIdx.x]);
-                    const float thr = fmaxf(1.f, a.rare_frac * (float)gridDim.x);
+                    const float thr = fmaxf(1.f, a.rare_frac * (float)G::nblk());
                     const unsigned cb = __ballot_sync(FULL_MASK, c >= thr);
                     const unsigned rb = __ballot_sync(FULL_MASK, c >= 1.f && c < thr);
                     if ((threadIdx.x & 31) == 0) {  // 32-bit halves of the 64-bit words
@@ -1636,13 +1653,13 @@ __global__ void __launch_bounds__(MS_THREADS, MS_MIN_BLOCKS) ms_grid_kernel(MsAr
                 // discovered vertices collect in the CTA's shared queue (the whole
                 // staging buffer), flushed to the level's queue at the end of part B
                 const CtaQ cq{reinterpret_cast<int32_t *>(ms_smem()), cq_count(), MS_SMEM_BYTES / 4};
-                bu_light<W, GridG>(a, L, cq);
+                bu_light<W, G>(a, L, cq);
                 if (threadIdx.x == 0) record_event(ctl, ev_idx, rank == 0, b, j, 6, L.qlen, L.qedges);
                 ++ev_idx;
-                bu_mid<W, GridG>(a, L, cq);
-                bu_wide<W, GridG>(a, L, cq);
-                bu_heavy<W, GridG>(a, L, cq);
-                if (L.rare_td) bu_rare_list<W, GridG>(a, L, s_rare);
+                bu_mid<W, G>(a, L, cq);
+                bu_wide<W, G>(a, L, cq);
+                bu_heavy<W, G>(a, L, cq);
+                if (L.rare_td) bu_rare_list<W, G>(a, L, s_rare);
                 __syncthreads();
                 if (*cq.n > 0) cta_flush(a, L, cq);
                 if (L.rare_td) {  // part C
@@ -1655,7 +1672,7 @@ __global__ void __launch_bounds__(MS_THREADS, MS_MIN_BLOCKS) ms_grid_kernel(MsAr
                     LC.qcur_off = a.qoff[L.prv];
                     LC.qlen = (int)(rp >> QPACK_SHIFT);
                     LC.qedges = (long long)(rp & QPACK_EDGES);
-                    gather_mp<W, GridG, true>(a, LC, s_rare);
+                    gather_mp<W, G, true>(a, LC, s_rare);
                 }
             } else {
                 // A top-down expansion over more edges than the graph has vertices
@@ -1664,14 +1681,14 @@ __global__ void __launch_bounds__(MS_THREADS, MS_MIN_BLOCKS) ms_grid_kernel(MsAr
                 // first-discovery stamp), and one scan after the level keeps the
                 // bits not seen before, updates seen and builds the next queue.
                 L.scanq = VARIANT == GU_BFS_AUTO && (double)L.qedges > (double)a.n;
-                td_update<W, GridG>(a, L);
-                if (VARIANT == GU_BFS_EDGE) gather_edge<W, GridG>(a, L);
-                else if (VARIANT == GU_BFS_WARP) gather_warp<W, GridG>(a, L);
-                else if (VARIANT == GU_BFS_CTA_WARP) gather_cta_warp<W, GridG>(a, L);
-                else if (VARIANT == GU_BFS_SCAN) gather_scan<W, GridG>(a, L);
-                else if (VARIANT == GU_BFS_SHUFFLE) gather_shuffle<W, GridG>(a, L);
-                else if (VARIANT == GU_BFS_LINEAR) gather_linear<W, GridG>(a, L);
-                else gather_mp<W, GridG>(a, L);  // AUTO, BOTTOM_UP level 1
+                td_update<W, G>(a, L);
+                if (VARIANT == GU_BFS_EDGE) gather_edge<W, G>(a, L);
+                else if (VARIANT == GU_BFS_WARP) gather_warp<W, G>(a, L);
+                else if (VARIANT == GU_BFS_CTA_WARP) gather_cta_warp<W, G>(a, L);
+                else if (VARIANT == GU_BFS_SCAN) gather_scan<W, G>(a, L);
+                else if (VARIANT == GU_BFS_SHUFFLE) gather_shuffle<W, G>(a, L);
+                else if (VARIANT == GU_BFS_LINEAR) gather_linear<W, G>(a, L);
+                else gather_mp<W, G>(a, L);  // AUTO, BOTTOM_UP level 1
                 if (L.scanq) {
                     if (!barrier(ev_idx)) return;  // every claim of the level is in F_j
                     const CtaQ cq{reinterpret_cast<int32_t *>(ms_smem()), cq_count(), MS_SMEM_BYTES / 4};
@@ -1725,11 +1742,150 @@ __global__ void __launch_bounds__(MS_THREADS, MS_MIN_BLOCKS) ms_grid_kernel(MsAr
         tag_base += j + 1;
         int used = 0;
         while (used < 31 && ((j - 2) >> used) != 0) ++used;
-        if (a.dist) write_distances<W, GridG>(a, row0, nb, used);  // no rows: diameter, reach queries
-        if (a.reach) count_reached<W, GridG>(a, row0, nb);
+        if (a.dist) write_distances<W, G>(a, row0, nb, used);  // no rows: diameter, reach queries
+        if (a.reach) count_reached<W, G>(a, row0, nb);
         if (threadIdx.x == 0) record_event(ctl, ev_idx, rank == 0, b, j, 2, 0, 0);  // distance rows written
         ++ev_idx;
         if (!barrier(ev_idx - 1)) return;
+    }
+}
+
+template <int VARIANT, int W>
+__global__ void __launch_bounds__(MS_THREADS, MS_MIN_BLOCKS) ms_grid_kernel(MsArgs a)
+{
+    unsigned epoch = 0;
+    ms_search<VARIANT, W, GridG>(a, epoch);
+}
+
+// Workspace layout of one batched search over n vertices with W words per vertex:
+// control region, seen, three frontier arrays, the level planes, stamps, three
+// queues with their offsets (each array 256-byte aligned).
+__host__ __device__ inline size_t ms_up256(size_t b) { return ((b + 255) / 256) * 256; }
+__host__ __device__ inline int ms_planes(size_t n)
+{
+    // every BFS level is at most n - 1: bit-length of n - 1 planes suffice
+    int nplanes = 1;
+    while (nplanes < MAX_PLANES && ((int64_t)(n > 0 ? n - 1 : 0) >> nplanes) != 0) ++nplanes;
+    return nplanes;
+}
+__host__ __device__ inline size_t ms_layout_bytes(size_t n, int W)
+{
+    return WS_CONTROL_BYTES + (4 + (size_t)ms_planes(n)) * ms_up256(n * W * sizeof(u64)) +
+           7 * ms_up256(n * sizeof(int32_t));
+}
+__host__ __device__ inline void ms_layout(char *ws, size_t n, int W, MsArgs &a)
+{
+    const size_t words_bytes = ms_up256(n * W * sizeof(u64));
+    const size_t i32_bytes = ms_up256(n * sizeof(int32_t));
+    char *p = ws;
+    a.ctl = reinterpret_cast<MsCtl *>(p);
+    a.cover = reinterpret_cast<int *>(p + COVER_OFF);
+    p += WS_CONTROL_BYTES;
+    a.seen = reinterpret_cast<u64 *>(p);
+    p += words_bytes;
+    for (int i = 0; i < 3; ++i) {
+        a.fr[i] = reinterpret_cast<u64 *>(p);
+        p += words_bytes;
+    }
+    a.plane = reinterpret_cast<u64 *>(p);
+    a.nplanes = ms_planes(n);
+    p += (size_t)a.nplanes * words_bytes;
+    a.stamp = reinterpret_cast<int32_t *>(p);
+    p += i32_bytes;
+    for (int i = 0; i < 3; ++i) {
+        a.q[i] = reinterpret_cast<int32_t *>(p);
+        p += i32_bytes;
+        a.qoff[i] = reinterpret_cast<int32_t *>(p);
+        p += i32_bytes;
+    }
+}
+
+// ---- work-queue launch: many graphs and source blocks in one persistent grid ----
+// The grid is cut into groups of group_size consecutive CTAs.  A group's first CTA
+// takes the next item from a device counter and the group barrier hands it to the
+// group's other CTAs; the group then runs the batched search of that item (one
+// graph, up to 64 W sources) in its own slice of the workspace, with barriers over
+// its own CTAs only, and takes the next item until none is left.  Items of
+// different graphs and sizes run side by side on different groups.
+struct MqItem {
+    const int32_t *R, *C, *RT, *CT;
+    const int32_t *light, *mid, *wide, *heavy;
+    int32_t n, nlight, nmid, nwide, nheavy;
+    int32_t degbits;
+    int64_t m;
+    const int32_t *sources;
+    int32_t k;
+    int32_t *dist;              // k x ld rows, or null
+    int64_t ld;
+    unsigned long long *reach;  // k reachable counts (zeroed before the launch), or null
+};
+
+struct MqArgs {
+    const MqItem *items;
+    int nitems;
+    int *next;           // item counter, zeroed before the launch
+    char *ws;            // group g's slice at ws + g * ws_stride
+    size_t ws_stride;
+    int group_size;
+    float alpha, beta, gamma, rare_frac;
+    unsigned long long wait_ns;
+};
+
+template <int W>
+__global__ void __launch_bounds__(MS_THREADS, MS_MIN_BLOCKS) ms_queue_kernel(MqArgs q)
+{
+    __shared__ int s_item;
+    __shared__ MsArgs s_args;
+    const int grp = blockIdx.x / q.group_size;
+    if (threadIdx.x == 0) {
+        s_grp_base = grp * q.group_size;
+        s_grp_nblk = min(q.group_size, (int)gridDim.x - grp * q.group_size);
+    }
+    __syncthreads();
+    char *ws = q.ws + (size_t)grp * q.ws_stride;
+    MsCtl *ctl = reinterpret_cast<MsCtl *>(ws);
+    unsigned epoch = 0;
+    while (true) {
+        if (GroupG::rank() == 0) ctl->item = atomicAdd(q.next, 1);
+        if (!grid_barrier(&ctl->bar, &ctl->err, epoch, q.wait_ns, nullptr, nullptr, 0, (unsigned)GroupG::nblk())) return;
+        if (threadIdx.x == 0) s_item = ld_volatile_i32(&ctl->item);
+        __syncthreads();
+        const int it = s_item;
+        if (it >= q.nitems) return;
+        if (threadIdx.x == 0) {  // the item's arguments, in shared memory for the whole CTA
+            const MqItem m = q.items[it];
+            MsArgs &a = s_args;
+            a.R = m.R;
+            a.C = m.C;
+            a.RT = m.RT;
+            a.CT = m.CT;
+            a.F = nullptr;  // AUTO never sweeps the COO array
+            a.light = m.light;
+            a.mid = m.mid;
+            a.wide = m.wide;
+            a.heavy = m.heavy;
+            a.n = m.n;
+            a.nlight = m.nlight;
+            a.nmid = m.nmid;
+            a.nwide = m.nwide;
+            a.nheavy = m.nheavy;
+            a.m = m.m;
+            a.sources = m.sources;
+            a.k = m.k;
+            a.dist = m.dist;
+            a.reach = m.reach;
+            a.ld = m.ld;
+            ms_layout(ws, (size_t)m.n, W, a);
+            a.alpha = q.alpha;
+            a.beta = q.beta;
+            a.gamma = q.gamma;
+            a.rare_frac = q.rare_frac;
+            a.degbits = m.degbits;
+            a.wait_ns = q.wait_ns;
+        }
+        __syncthreads();
+        ms_search<GU_BFS_AUTO, W, GroupG>(s_args, epoch);
+        if (ld_volatile_i32(&ctl->err) != 0) return;  // every CTA of the group sees it at its next barrier
     }
 }
 
@@ -1777,20 +1933,9 @@ int msbfs_words_for(int32_t k)
     return 4;
 }
 
-static int msbfs_planes(size_t n)
-{
-    // every BFS level is at most n - 1: bit-length of n - 1 planes suffice
-    int nplanes = 1;
-    while (nplanes < MAX_PLANES && ((int64_t)(n > 0 ? n - 1 : 0) >> nplanes) != 0) ++nplanes;
-    return nplanes;
-}
-
 size_t msbfs_workspace_bytes(const DeviceGraph &g, int32_t k)
 {
-    const int W = msbfs_words_for(k);
-    const size_t n = (size_t)g.n;
-    auto up = [](size_t b) { return ((b + 255) / 256) * 256; };
-    return WS_CONTROL_BYTES + (4 + (size_t)msbfs_planes(n)) * up(n * W * sizeof(u64)) + 7 * up(n * sizeof(int32_t));
+    return ms_layout_bytes((size_t)g.n, msbfs_words_for(k));
 }
 
 void launch_msbfs(DeviceGraph &g, const int32_t *sources, int32_t k, int32_t *dist, int64_t ld,
@@ -1801,14 +1946,9 @@ void launch_msbfs(DeviceGraph &g, const int32_t *sources, int32_t k, int32_t *di
     const int W = (opt.batch_words == 1 || opt.batch_words == 2 || opt.batch_words == 4) ? opt.batch_words
                                                                                          : msbfs_words_for(k);
     const size_t n = (size_t)g.n;
-    const int nplanes = msbfs_planes(n);
-    auto up = [](size_t b) { return ((b + 255) / 256) * 256; };
-    const size_t words_bytes = up(n * W * sizeof(u64));
-    const size_t i32_bytes = up(n * sizeof(int32_t));
     static_assert(CTL_REGION <= WS_CONTROL_BYTES, "timeline must fit the control region");
-    const size_t ctl_bytes = WS_CONTROL_BYTES;
     Workspace &wsp = opt.ws ? *opt.ws : g.ws;
-    char *ws = (char *)wsp.get(msbfs_workspace_bytes(g, k));
+    char *ws = (char *)wsp.get(ms_layout_bytes(n, W));
     MsArgs a;
     a.R = g.R;
     a.C = g.C;
@@ -1830,27 +1970,7 @@ void launch_msbfs(DeviceGraph &g, const int32_t *sources, int32_t k, int32_t *di
     a.dist = dist;
     a.reach = opt.reach;
     a.ld = ld;
-    char *p = ws;
-    a.ctl = reinterpret_cast<MsCtl *>(p);
-    a.cover = reinterpret_cast<int *>(p + COVER_OFF);
-    p += ctl_bytes;
-    a.seen = reinterpret_cast<u64 *>(p);
-    p += words_bytes;
-    for (int i = 0; i < 3; ++i) {
-        a.fr[i] = reinterpret_cast<u64 *>(p);
-        p += words_bytes;
-    }
-    a.plane = reinterpret_cast<u64 *>(p);
-    a.nplanes = nplanes;
-    p += (size_t)nplanes * words_bytes;
-    a.stamp = reinterpret_cast<int32_t *>(p);
-    p += i32_bytes;
-    for (int i = 0; i < 3; ++i) {
-        a.q[i] = reinterpret_cast<int32_t *>(p);
-        p += i32_bytes;
-        a.qoff[i] = reinterpret_cast<int32_t *>(p);
-        p += i32_bytes;
-    }
+    ms_layout(ws, n, W, a);
     a.alpha = opt.tuned ? opt.alpha : env_float("GU_MS_ALPHA", opt.alpha);
     a.beta = opt.tuned ? opt.beta : env_float("GU_MS_BETA", opt.beta);
     a.gamma = env_float("GU_MS_GAMMA", opt.gamma);
@@ -1880,6 +2000,122 @@ void launch_msbfs(DeviceGraph &g, const int32_t *sources, int32_t k, int32_t *di
         if (!g.ctl_host) GU_CUDA_CHECK(pinned_alloc(&g.ctl_host, sizeof(MsCtl)));
         GU_CUDA_CHECK(cudaMemcpyAsync(g.ctl_host, a.ctl, sizeof(MsCtl), cudaMemcpyDeviceToHost, stream));
     }
+}
+
+// ---- work-queue launch (host) ----------------------------------------------------
+template <int W>
+static int queue_blocks_per_sm()
+{
+    static int b = -1;
+    if (b < 0) {
+        GU_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, ms_queue_kernel<W>, MS_THREADS, 0));
+        if (b < 1) throw gu_error(GU_ERR_INTERNAL, "work-queue kernel cannot be resident");
+    }
+    return b;
+}
+
+MsQueueLaunch launch_msbfs_queue(const std::vector<MsQueueRequest> &reqs, Workspace &wsp, int sms, int max_blocks,
+                                 cudaStream_t st)
+{
+    int32_t maxk = 0;
+    size_t maxn = 0;
+    for (const MsQueueRequest &r : reqs) {
+        if (!r.g || r.k < 0 || (r.k > 0 && (!r.sources || (!r.dist && !r.reach))))
+            throw gu_error(GU_ERR_INVALID_ARGUMENT, "bad work-queue request");
+        if (r.dist && r.ld < r.g->n) throw gu_error(GU_ERR_INVALID_ARGUMENT, "ld must be >= n");
+        if (r.k == 0) continue;
+        maxk = std::max(maxk, r.k);
+        maxn = std::max(maxn, (size_t)r.g->n);
+    }
+    if (maxk == 0) return MsQueueLaunch();
+    const int W = msbfs_words_for(std::min(maxk, 64 * MAXW));
+    const int per_item = 64 * W;
+    std::vector<MqItem> items;
+    for (const MsQueueRequest &r : reqs) {
+        if (r.k == 0) continue;
+        const DeviceGraph &g = *r.g;
+        int degbits = 1;
+        while (degbits < 31 && (1ll << degbits) <= (long long)g.max_degree) ++degbits;
+        if (r.reach) GU_CUDA_CHECK(cudaMemsetAsync(r.reach, 0, sizeof(unsigned long long) * (size_t)r.k, st));
+        for (int32_t off = 0; off < r.k; off += per_item) {
+            MqItem it;
+            it.R = g.R;
+            it.C = g.C;
+            it.RT = g.RT;
+            it.CT = g.CT;
+            it.light = g.light;
+            it.mid = g.mid;
+            it.wide = g.wide;
+            it.heavy = g.heavy;
+            it.n = g.n;
+            it.nlight = g.nlight;
+            it.nmid = g.nmid;
+            it.nwide = g.nwide;
+            it.nheavy = g.nheavy;
+            it.degbits = degbits;
+            it.m = g.m;
+            it.sources = r.sources + off;
+            it.k = std::min(per_item, r.k - off);
+            it.dist = r.dist ? r.dist + (size_t)off * (size_t)r.ld : nullptr;
+            it.ld = r.ld;
+            it.reach = r.reach ? r.reach + off : nullptr;
+            items.push_back(it);
+        }
+    }
+    const int nitems = (int)items.size();
+    int bps = W == 1 ? queue_blocks_per_sm<1>() : W == 2 ? queue_blocks_per_sm<2>() : queue_blocks_per_sm<4>();
+    int blocks = sms * bps;
+    if (max_blocks > 0) blocks = std::min(blocks, max_blocks);
+    // group size: about 16 K vertices per CTA of a group, larger while there are
+    // fewer items than groups, so that the grid is used
+    int gs = (int)std::min<size_t>((maxn + 16383) / 16384, (size_t)blocks);
+    gs = std::max(gs, std::max(1, blocks / nitems));
+    gs = std::max(1, std::min(gs, blocks));
+    const int ngroups = blocks / gs;
+    blocks = ngroups * gs;
+    const size_t stride = ms_up256(ms_layout_bytes(maxn, W));
+    const size_t items_off = (size_t)ngroups * stride;
+    const size_t cnt_off = items_off + ms_up256(sizeof(MqItem) * (size_t)nitems);
+    char *ws = (char *)wsp.get(cnt_off + 256);
+    GU_CUDA_CHECK(cudaMemset2DAsync(ws, stride, 0, CTL_REGION, (size_t)ngroups, st));
+    GU_CUDA_CHECK(cudaMemsetAsync(ws + cnt_off, 0, sizeof(int), st));
+    GU_CUDA_CHECK(cudaMemcpyAsync(ws + items_off, items.data(), sizeof(MqItem) * (size_t)nitems,
+                                  cudaMemcpyHostToDevice, st));
+    MqArgs q;
+    q.items = reinterpret_cast<const MqItem *>(ws + items_off);
+    q.nitems = nitems;
+    q.next = reinterpret_cast<int *>(ws + cnt_off);
+    q.ws = ws;
+    q.ws_stride = stride;
+    q.group_size = gs;
+    q.alpha = env_float("GU_MS_ALPHA", 2.f);
+    q.beta = env_float("GU_MS_BETA", 24.f);
+    q.gamma = env_float("GU_MS_GAMMA", 4.f);
+    q.rare_frac = env_float("GU_MS_RARE", MsOptions().rare_frac);
+    q.wait_ns = wait_limit_ns();
+    void *params[] = {&q};
+    const void *fn = W == 1 ? (const void *)ms_queue_kernel<1> : W == 2 ? (const void *)ms_queue_kernel<2>
+                                                                       : (const void *)ms_queue_kernel<4>;
+    GU_CUDA_CHECK(cudaLaunchCooperativeKernel(fn, dim3(blocks), dim3(MS_THREADS), params, 0, st));
+    MsQueueLaunch L;
+    L.ngroups = ngroups;
+    L.stride = stride;
+    L.group_size = gs;
+    L.items = nitems;
+    return L;
+}
+
+// First non-zero device error word of the groups of a work-queue launch (after
+// its stream is synchronised).
+int msbfs_queue_error(const Workspace &ws, const MsQueueLaunch &L)
+{
+    if (L.ngroups == 0) return 0;
+    std::vector<int> e((size_t)L.ngroups, 0);
+    GU_CUDA_CHECK(cudaMemcpy2D(e.data(), sizeof(int), static_cast<const char *>(ws.ptr) + offsetof(MsCtl, err), L.stride,
+                               sizeof(int), (size_t)L.ngroups, cudaMemcpyDeviceToHost));
+    for (int x : e)
+        if (x) return x;
+    return 0;
 }
 
 void msbfs_status_after_sync(DeviceGraph &g, int *dev_err, int *td_levels, int *bu_levels, int *max_level)

@@ -120,6 +120,7 @@ def lib():
         "gu_server_wait": ([_vp, ctypes.c_int64, ctypes.c_double, ctypes.POINTER(ctypes.c_double)], ctypes.c_int),
         "gu_server_stats": ([_vp, _i64p, _i64p, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
                              ctypes.POINTER(ctypes.c_double)], ctypes.c_int),
+        "gu_bfs_many": ([_vp, ctypes.c_int32, _vp], ctypes.c_int),
         "gu_bfs_noalloc": ([_vp, _vp, ctypes.c_int32, ctypes.c_int64, _vp, ctypes.c_int32, _vp, ctypes.c_int64, _vp],
                            ctypes.c_int),
     }
@@ -380,6 +381,23 @@ class Graph:
         check(lib().gu_bfs_host(self._h, VARIANTS[variant] if isinstance(variant, str) else variant, _ptr(s), k,
                                 out.ctypes.data_as(_i32p), out.shape[1], _stream_handle(stream)))
         return out
+
+
+class SearchItem(ctypes.Structure):
+    """gu_search_item: one request of gu_bfs_many."""
+    _fields_ = [("graph", _vp), ("sources_dev", _vp), ("k", ctypes.c_int32), ("dist_dev", _vp),
+                ("ld", ctypes.c_int64), ("reach_dev", _vp)]
+
+
+def bfs_many(requests, stream=None):
+    """Many searches on many graphs in one work-queue launch.  requests: list of
+    (Graph, sources int32 cuda tensor, dist int32 cuda tensor k x ld or None,
+    reach int64 cuda tensor k or None)."""
+    arr = (SearchItem * max(1, len(requests)))()
+    for i, (g, s, d, r) in enumerate(requests):
+        arr[i] = SearchItem(g._h, s.data_ptr(), int(s.numel()), d.data_ptr() if d is not None else None,
+                            int(d.shape[1]) if d is not None else 0, r.data_ptr() if r is not None else None)
+    check(lib().gu_bfs_many(arr, len(requests), _stream_handle(stream)))
 
 
 def lbs(counts_dev, scanned_dev, result_dev, total_dev=None, stream=None):

@@ -290,6 +290,26 @@ gu_status gu_reach(gu_graph g, const int32_t *sources_dev, int32_t k, int64_t *c
  * reference it assumes no cycles. */
 gu_status gu_dag_reach(gu_graph g, int64_t *counts_dev, int64_t *total_pairs, void *stream);
 
+/* Many searches in one launch: BFS rows and/or reachable counts for requests on
+ * any number of graphs (all on the current device), run by one persistent grid
+ * whose CTA groups drain a device work queue of (graph, block of up to 256
+ * sources) items -- small graphs and large ones side by side, no launch per
+ * request.  Per item: dist_dev (k x ld int32 rows, ld >= the graph's n, or NULL)
+ * and/or reach_dev (k int64 counts, the source included, or NULL); at least one.
+ * Results equal gu_bfs / gu_reach on each graph alone.  A source out of range
+ * gives GU_ERR_INVALID_ARGUMENT (the outputs are then unspecified).  The
+ * reference runs one graph per setup call with a grid stride over its sources
+ * (multi_search/shuffle_based.cuh:104); this is the cross-graph form. */
+typedef struct gu_search_item {
+    gu_graph graph;
+    const int32_t *sources_dev;
+    int32_t k;
+    int32_t *dist_dev;
+    int64_t ld;
+    int64_t *reach_dev;
+} gu_search_item;
+gu_status gu_bfs_many(const gu_search_item *items, int32_t count, void *stream);
+
 /* ---- load-balanced search and race-and-resolve ------------------------------- */
 /* Load-balanced search over N work counts (device pointers, counts >= 0):
  * scanned_dev[i] = exclusive prefix sum of counts (int32), total = sum, and
