@@ -233,9 +233,11 @@ struct MsQueueRequest {
     unsigned long long *reach = nullptr;
 };
 struct MsQueueLaunch {
-    int ngroups = 0, group_size = 0, items = 0;
-    size_t stride = 0;  // bytes of workspace per group
+    int W = 0, ngroups = 0, group_size = 0, items = 0;
+    size_t stride = 0;                             // bytes of workspace per group
+    size_t items_off = 0, cnt_off = 0, bytes = 0;  // item array, counter, total workspace
 };
+MsQueueLaunch msbfs_queue_plan(const std::vector<MsQueueRequest> &reqs, int sms, int max_blocks);
 // Runs every request in one persistent launch whose CTA groups drain a device
 // queue of (graph, source block) items (asynchronous on st; the graphs' lazily
 // built structures are not touched).  msbfs_queue_error reads the groups' device

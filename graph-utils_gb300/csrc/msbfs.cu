@@ -2014,8 +2014,8 @@ static int queue_blocks_per_sm()
     return b;
 }
 
-MsQueueLaunch launch_msbfs_queue(const std::vector<MsQueueRequest> &reqs, Workspace &wsp, int sms, int max_blocks,
-                                 cudaStream_t st)
+// Words per vertex, groups and workspace of a work-queue launch over reqs.
+MsQueueLaunch msbfs_queue_plan(const std::vector<MsQueueRequest> &reqs, int sms, int max_blocks)
 {
     int32_t maxk = 0;
     size_t maxn = 0;
@@ -2027,9 +2027,33 @@ MsQueueLaunch launch_msbfs_queue(const std::vector<MsQueueRequest> &reqs, Worksp
         maxk = std::max(maxk, r.k);
         maxn = std::max(maxn, (size_t)r.g->n);
     }
-    if (maxk == 0) return MsQueueLaunch();
-    const int W = msbfs_words_for(std::min(maxk, 64 * MAXW));
-    const int per_item = 64 * W;
+    MsQueueLaunch L;
+    if (maxk == 0) return L;
+    L.W = msbfs_words_for(std::min(maxk, 64 * MAXW));
+    const int per_item = 64 * L.W;
+    for (const MsQueueRequest &r : reqs) L.items += (r.k + per_item - 1) / per_item;
+    const int bps = L.W == 1 ? queue_blocks_per_sm<1>() : L.W == 2 ? queue_blocks_per_sm<2>() : queue_blocks_per_sm<4>();
+    int blocks = sms * bps;
+    if (max_blocks > 0) blocks = std::min(blocks, max_blocks);
+    // group size: about 16 K vertices per CTA of a group, larger while there are
+    // fewer items than groups, so that the grid is used
+    int gs = (int)std::min<size_t>((maxn + 16383) / 16384, (size_t)blocks);
+    gs = std::max(gs, std::max(1, blocks / L.items));
+    L.group_size = std::max(1, std::min(gs, blocks));
+    L.ngroups = blocks / L.group_size;
+    L.stride = ms_up256(ms_layout_bytes(maxn, L.W));
+    L.items_off = (size_t)L.ngroups * L.stride;
+    L.cnt_off = L.items_off + ms_up256(sizeof(MqItem) * (size_t)L.items);
+    L.bytes = L.cnt_off + 256;
+    return L;
+}
+
+MsQueueLaunch launch_msbfs_queue(const std::vector<MsQueueRequest> &reqs, Workspace &wsp, int sms, int max_blocks,
+                                 cudaStream_t st)
+{
+    const MsQueueLaunch L = msbfs_queue_plan(reqs, sms, max_blocks);
+    if (L.items == 0) return L;
+    const int W = L.W, per_item = 64 * W;
     std::vector<MqItem> items;
     for (const MsQueueRequest &r : reqs) {
         if (r.k == 0) continue;
@@ -2062,32 +2086,18 @@ MsQueueLaunch launch_msbfs_queue(const std::vector<MsQueueRequest> &reqs, Worksp
             items.push_back(it);
         }
     }
-    const int nitems = (int)items.size();
-    int bps = W == 1 ? queue_blocks_per_sm<1>() : W == 2 ? queue_blocks_per_sm<2>() : queue_blocks_per_sm<4>();
-    int blocks = sms * bps;
-    if (max_blocks > 0) blocks = std::min(blocks, max_blocks);
-    // group size: about 16 K vertices per CTA of a group, larger while there are
-    // fewer items than groups, so that the grid is used
-    int gs = (int)std::min<size_t>((maxn + 16383) / 16384, (size_t)blocks);
-    gs = std::max(gs, std::max(1, blocks / nitems));
-    gs = std::max(1, std::min(gs, blocks));
-    const int ngroups = blocks / gs;
-    blocks = ngroups * gs;
-    const size_t stride = ms_up256(ms_layout_bytes(maxn, W));
-    const size_t items_off = (size_t)ngroups * stride;
-    const size_t cnt_off = items_off + ms_up256(sizeof(MqItem) * (size_t)nitems);
-    char *ws = (char *)wsp.get(cnt_off + 256);
-    GU_CUDA_CHECK(cudaMemset2DAsync(ws, stride, 0, CTL_REGION, (size_t)ngroups, st));
-    GU_CUDA_CHECK(cudaMemsetAsync(ws + cnt_off, 0, sizeof(int), st));
-    GU_CUDA_CHECK(cudaMemcpyAsync(ws + items_off, items.data(), sizeof(MqItem) * (size_t)nitems,
-                                  cudaMemcpyHostToDevice, st));
+    char *ws = (char *)wsp.get(L.bytes);
+    GU_CUDA_CHECK(cudaMemset2DAsync(ws, L.stride, 0, CTL_REGION, (size_t)L.ngroups, st));
+    GU_CUDA_CHECK(cudaMemsetAsync(ws + L.cnt_off, 0, sizeof(int), st));
+    GU_CUDA_CHECK(cudaMemcpyAsync(ws + L.items_off, items.data(), sizeof(MqItem) * items.size(), cudaMemcpyHostToDevice,
+                                  st));
     MqArgs q;
-    q.items = reinterpret_cast<const MqItem *>(ws + items_off);
-    q.nitems = nitems;
-    q.next = reinterpret_cast<int *>(ws + cnt_off);
+    q.items = reinterpret_cast<const MqItem *>(ws + L.items_off);
+    q.nitems = (int)items.size();
+    q.next = reinterpret_cast<int *>(ws + L.cnt_off);
     q.ws = ws;
-    q.ws_stride = stride;
-    q.group_size = gs;
+    q.ws_stride = L.stride;
+    q.group_size = L.group_size;
     q.alpha = env_float("GU_MS_ALPHA", 2.f);
     q.beta = env_float("GU_MS_BETA", 24.f);
     q.gamma = env_float("GU_MS_GAMMA", 4.f);
@@ -2096,12 +2106,7 @@ MsQueueLaunch launch_msbfs_queue(const std::vector<MsQueueRequest> &reqs, Worksp
     void *params[] = {&q};
     const void *fn = W == 1 ? (const void *)ms_queue_kernel<1> : W == 2 ? (const void *)ms_queue_kernel<2>
                                                                        : (const void *)ms_queue_kernel<4>;
-    GU_CUDA_CHECK(cudaLaunchCooperativeKernel(fn, dim3(blocks), dim3(MS_THREADS), params, 0, st));
-    MsQueueLaunch L;
-    L.ngroups = ngroups;
-    L.stride = stride;
-    L.group_size = gs;
-    L.items = nitems;
+    GU_CUDA_CHECK(cudaLaunchCooperativeKernel(fn, dim3(L.ngroups * L.group_size), dim3(MS_THREADS), params, 0, st));
     return L;
 }
 

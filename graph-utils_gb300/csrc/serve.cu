@@ -4,8 +4,11 @@
 // any host thread.  A worker thread keeps a FIFO of pending requests and a fixed
 // set of slots (stream, workspace, pinned staging of the inputs).  Whenever a
 // slot is free it forms a batch from the oldest pending request and every later
-// pending request of the same graph and kind (up to max_batch sources; a larger
-// request runs alone), admits it if the batch's device footprint (engine workspace + rows)
+// pending request it can share a launch with (up to max_batch sources; a larger
+// request runs alone): BC requests of the same graph, or BFS and reachability
+// requests of ANY graphs -- those run as one work-queue launch whose CTA groups
+// take (graph, source block) items from a device counter -- and admits it if the
+// batch's device footprint (engine workspace + rows)
 // fits the HBM budget next to the batches already running, and launches it on
 // the slot's stream with a persistent grid of 1/slots of the GPU, so batches of
 // different slots overlap on the device.  Requests that arrive while batches
@@ -84,6 +87,9 @@ struct Slot {
     bool copying = false;  // kernels done, results being copied out by the copier thread
     cudaError_t done_status = cudaSuccess;
     int touch_pending = 0;  // page-touch jobs of the batch's host buffers not yet done (tmu_)
+    bool queued = false;       // the batch runs as a work-queue launch (ql), results at offs
+    MsQueueLaunch ql;
+    std::vector<size_t> offs;  // device result offset of each request (work-queue batches)
 };
 
 struct TouchJob {
@@ -98,6 +104,7 @@ public:
     {
         GU_CUDA_CHECK(cudaGetDevice(&device_));
         const int sms = device_sm_count(device_);
+        sms_ = sms;
         nslots = std::max(1, std::min(nslots, 32));
         blocks_per_slot_ = std::max(1, 2 * sms / nslots);
         slots_.resize((size_t)nslots);
@@ -242,16 +249,35 @@ private:
         std::vector<SRequest *> batch{head};
         int32_t k = (int32_t)head->src.size();
         size_t out_bytes = row_bytes(head);
+        const bool search = head->kind != GU_QUERY_BC;  // BFS rows and reachable counts share launches
+        bool multi = false;
         for (size_t i = 1; i < pending_.size() && k < max_batch_; ++i) {
             SRequest *r = pending_[i];
-            if (r->g != head->g || r->kind != head->kind) continue;
+            if (search ? r->kind == GU_QUERY_BC : (r->g != head->g || r->kind != head->kind)) continue;
             if (k + (int64_t)r->src.size() > max_batch_) continue;
             batch.push_back(r);
             k += (int32_t)r->src.size();
             out_bytes += row_bytes(r);
+            multi |= r->g != head->g || r->kind != head->kind;
         }
         DeviceGraph &g = *head->g;
-        const size_t need = batch_need(head->kind, g, k, (int)batch.size(), out_bytes);
+        size_t need = batch_need(head->kind, g, k, (int)batch.size(), out_bytes);
+        std::vector<MsQueueRequest> qreqs;
+        if (multi) {  // work-queue launch: its own workspace plan, outputs at 256-byte offsets
+            qreqs.resize(batch.size());
+            for (size_t i = 0; i < batch.size(); ++i) {
+                qreqs[i].g = batch[i]->g;
+                qreqs[i].sources = reinterpret_cast<const int32_t *>(1);  // placeholders: only sizes are planned
+                qreqs[i].k = (int32_t)batch[i]->src.size();
+                qreqs[i].ld = batch[i]->g->n;
+                if (batch[i]->kind == GU_QUERY_BFS) qreqs[i].dist = reinterpret_cast<int32_t *>(1);
+                else qreqs[i].reach = reinterpret_cast<unsigned long long *>(1);
+            }
+            out_bytes = 0;
+            for (SRequest *r : batch) out_bytes += (row_bytes(r) + 255) / 256 * 256;
+            need = msbfs_queue_plan(qreqs, sms_, blocks_per_slot_).bytes + (size_t)k * 4 + 1024 +
+                   out_bytes;
+        }
         if (held_except(&s) + std::max(need, s.ws.bytes + s.io.bytes) > budget_) {
             for (Slot &o : slots_)  // give back memory idle slots hold
                 if (!o.busy && &o != &s) {
@@ -275,7 +301,8 @@ private:
         }
         for (SRequest *r : batch) pending_.erase(std::find(pending_.begin(), pending_.end(), r));
         try {
-            launch(s, head->kind, g, batch, k, out_bytes);
+            if (multi) launch_queue(s, batch, k, out_bytes);
+            else launch(s, head->kind, g, batch, k, out_bytes);
         } catch (const gu_error &e) {
             for (SRequest *r : batch) finish(r, e.code, e.what());
             cv_done_.notify_all();
@@ -338,6 +365,49 @@ private:
             }
         }
         s.dres = dres;
+        s.queued = false;
+        start_batch(s, kind, g, batch, out_bytes);
+    }
+
+    // Work-queue batch: BFS and reachability requests of several graphs in one
+    // launch; request i's result at s.offs[i] (256-byte aligned) in the device io.
+    void launch_queue(Slot &s, const std::vector<SRequest *> &batch, int32_t k, size_t out_bytes)
+    {
+        GU_CUDA_CHECK(cudaSetDevice(device_));
+        const size_t src_b = ((size_t)k * 4 + 255) / 256 * 256;
+        int32_t *hs = reinterpret_cast<int32_t *>(s.stage.get(src_b + 256));
+        char *io = (char *)s.io.get(src_b + out_bytes + 256);
+        int32_t *dsrc = reinterpret_cast<int32_t *>(io);
+        char *dres = io + src_b;
+        std::vector<MsQueueRequest> reqs(batch.size());
+        s.offs.assign(batch.size(), 0);
+        int32_t pos = 0;
+        size_t off = 0;
+        for (size_t i = 0; i < batch.size(); ++i) {
+            const SRequest *r = batch[i];
+            std::memcpy(hs + pos, r->src.data(), r->src.size() * sizeof(int32_t));
+            MsQueueRequest &q = reqs[i];
+            q.g = r->g;
+            q.sources = dsrc + pos;
+            q.k = (int32_t)r->src.size();
+            q.ld = r->g->n;
+            if (r->kind == GU_QUERY_BFS) q.dist = reinterpret_cast<int32_t *>(dres + off);
+            else q.reach = reinterpret_cast<unsigned long long *>(dres + off);
+            s.offs[i] = off;
+            pos += q.k;
+            off += (row_bytes(r) + 255) / 256 * 256;
+        }
+        GU_CUDA_CHECK(cudaMemcpyAsync(dsrc, hs, src_b, cudaMemcpyHostToDevice, s.st));
+        s.ql = launch_msbfs_queue(reqs, s.ws, device_sm_count(device_), blocks_per_slot_, s.st);
+        s.dres = dres;
+        s.queued = true;
+        start_batch(s, batch[0]->kind, *batch[0]->g, batch, out_bytes);
+    }
+
+    // Common tail of a launch: completion event, page touching of the requests'
+    // host buffers, the slot's state (mu_ held).
+    void start_batch(Slot &s, int kind, DeviceGraph &g, const std::vector<SRequest *> &batch, size_t out_bytes)
+    {
         GU_CUDA_CHECK(cudaEventRecord(s.ev, s.st));
         {
             // touch the requests' host buffers while the batch runs, in pieces of
@@ -394,7 +464,8 @@ private:
                 st = GU_ERR_CUDA;
                 err = cudaGetErrorString(s.done_status);
             } else {
-                const int e = s.kind == GU_QUERY_BC ? bc_ws_error(s.ws) : msbfs_ws_error(s.ws);
+                const int e = s.queued ? msbfs_queue_error(s.ws, s.ql)
+                                       : s.kind == GU_QUERY_BC ? bc_ws_error(s.ws) : msbfs_ws_error(s.ws);
                 if (e == DEV_ERR_BARRIER_TIMEOUT) {
                     st = GU_ERR_TIMEOUT;
                     err = "a device-side wait exceeded its limit";
@@ -410,9 +481,11 @@ private:
             if (st == GU_OK) {
                 size_t off = 0;
                 cudaError_t ce = cudaSuccess;
-                for (SRequest *r : reqs) {
+                for (size_t i = 0; i < reqs.size(); ++i) {
+                    SRequest *r = reqs[i];
                     const size_t b = row_bytes(r);
-                    if (ce == cudaSuccess) ce = cudaMemcpyAsync(r->out, s.dres + off, b, cudaMemcpyDeviceToHost, s.st);
+                    const size_t o = s.queued ? s.offs[i] : off;
+                    if (ce == cudaSuccess) ce = cudaMemcpyAsync(r->out, s.dres + o, b, cudaMemcpyDeviceToHost, s.st);
                     off += b;
                 }
                 if (ce == cudaSuccess) ce = cudaStreamSynchronize(s.st);
@@ -475,6 +548,7 @@ private:
     int max_batch_;
     int device_ = 0;
     int blocks_per_slot_ = 1;
+    int sms_ = 1;
     std::vector<Slot> slots_;
     std::mutex mu_;
     std::condition_variable cv_work_, cv_done_;

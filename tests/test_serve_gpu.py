@@ -160,3 +160,38 @@ def test_page_touching_stays_inside_the_buffers(graphs):
         np.testing.assert_array_equal(out, lone_bfs(g, srcs))
         assert (arena[:off] == -123).all() and (arena[off + words:] == -123).all()
     srv.close()
+
+
+def test_requests_on_different_graphs_share_a_launch(graphs):
+    """With the only slot busy, BFS and reachability requests on three graphs queue
+    up; they then run as one work-queue launch (one batch for all of them), and
+    each result equals the oracle's."""
+    srv = gu.Server(hbm_budget_bytes=16 << 30, slots=1, max_batch=4096)
+    big = graphs["rmat13"]
+    hold = np.empty(big.n, np.float64)
+    rid0 = srv.submit(big, gu.QUERY_BC, np.arange(0, 1024, dtype=np.int32), hold)  # keeps the slot busy
+    rng = np.random.default_rng(3)
+    reqs = []
+    for i in range(18):
+        gname = ["rmat12", "rmat13", "dag"][i % 3]
+        g = graphs[gname]
+        k = int(rng.integers(1, 300))
+        srcs = rng.choice(g.n, size=k, replace=False).astype(np.int32)
+        if i % 2:
+            out, q = np.empty((k, g.n), np.int32), gu.QUERY_BFS
+        else:
+            out, q = np.empty(k, np.int64), gu.QUERY_REACH
+        reqs.append((srv.submit(g, q, srcs, out), gname, q, srcs, out))
+    srv.wait(rid0)
+    for rid, gname, q, srcs, out in reqs:
+        srv.wait(rid)
+        hg = graphs[gname].host
+        ref, _ = oracle.bfs_multi(hg.R, hg.C, hg.n, srcs, nthreads=8)
+        if q == gu.QUERY_BFS:
+            np.testing.assert_array_equal(out, ref, err_msg=gname)
+        else:
+            np.testing.assert_array_equal(out, (ref != gu.UNREACHABLE).sum(1), err_msg=gname)
+    st = srv.stats()
+    srv.close()
+    assert st["completed"] == 19
+    assert st["batches"] <= 3, st  # the BC request, then the queued searches together
