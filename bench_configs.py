@@ -6,8 +6,9 @@
     c4  2048 x 2048 4-neighbour grid, each edge deleted with probability 0.05 (seed 7),
         256 sources: BFS (batched and the one-CTA-per-source form), diameter, and
         load-balanced search over the int32 degree array.
-    c5  serving: R-MAT graphs and random DAGs resident on the device, Poisson arrivals
-        of BFS / BC / reachability requests at several rates, p50 / p99 latency.
+    c5  serving: 12 R-MAT graphs (scales 12-22) and 4 random DAGs (2^16-2^20) resident,
+        Poisson arrivals of BFS / BC / reachability requests at several rates, p50 / p99
+        latency, and a saturation burst against one call per request.
     io  graph files: R-MAT scale 20 as METIS / SNAP / MatrixMarket text and the
         binary CSR cache, read by this library and by the reference parser.
     dag all-vertex reachability of random DAGs (m = 8n), n = 2^16 and 2^18.
@@ -411,22 +412,46 @@ def _req_edges(comp_edges, q, hg, srcs):
     return float(comp_edges[id(hg)][srcs].sum()) if q != gu.QUERY_REACH else 0.0
 
 
-def _serve_stream(plan, comp_edges, slots=4, max_batch=1024):
-    """Runs one open-loop request stream through a gu.Server; latency from the planned arrival."""
+def _out_bytes(q, hg, srcs):
+    import gu
+    return len(srcs) * hg.n * 4 if q == gu.QUERY_BFS else (hg.n * 8 if q == gu.QUERY_BC else len(srcs) * 8)
+
+
+def _host_cap(limit):
+    """limit, or a quarter of the host's available memory if that is smaller."""
+    try:
+        for line in open("/proc/meminfo"):
+            if line.startswith("MemAvailable:"):
+                return min(limit, int(line.split()[1]) * 1024 // 4)
+    except OSError:
+        pass
+    return limit
+
+
+def _serve_stream(plan, comp_edges, slots=4, max_batch=1024, max_out_bytes=48 << 30):
+    """Runs one open-loop request stream through a gu.Server; latency from the planned
+    arrival.  The client holds at most max_out_bytes of result buffers: beyond that
+    it waits before submitting (that wait counts in the latency)."""
     import gu
     import queue
     import threading
     srv = gu.Server(hbm_budget_bytes=64 << 30, slots=slots, max_batch=max_batch)
+    max_out_bytes = _host_cap(max_out_bytes)
     pending = queue.Queue()
     lat = []  # open-loop latency: from the planned arrival, so a late submit counts
+    held = [0]
+    cv = threading.Condition()
 
     def waiter():  # waits in submission order, so finished outputs are released as it goes
         while True:
             item = pending.get()
             if item is None:
                 return
-            rid, lag = item
+            rid, lag, b = item
             lat.append(srv.wait(rid) + lag)
+            with cv:
+                held[0] -= b
+                cv.notify_all()
 
     th = threading.Thread(target=waiter)
     th.start()
@@ -435,6 +460,10 @@ def _serve_stream(plan, comp_edges, slots=4, max_batch=1024):
         now = time.perf_counter() - t0
         if ta > now:
             time.sleep(ta - now)
+        b = _out_bytes(q, hg, srcs)
+        with cv:
+            cv.wait_for(lambda: held[0] + b <= max_out_bytes or held[0] == 0)
+            held[0] += b
         if q == gu.QUERY_BFS:
             out = np.empty((len(srcs), hg.n), np.int32)
         elif q == gu.QUERY_BC:
@@ -442,7 +471,8 @@ def _serve_stream(plan, comp_edges, slots=4, max_batch=1024):
         else:
             out = np.empty(len(srcs), np.int64)
         rid = srv.submit(g, q, srcs, out)
-        pending.put((rid, max(0.0, time.perf_counter() - t0 - ta)))
+        del out
+        pending.put((rid, max(0.0, time.perf_counter() - t0 - ta), b))
     pending.put(None)
     th.join()
     wall = time.perf_counter() - t0
@@ -511,27 +541,35 @@ def serve_subline(torch, rate=800.0, seconds=1.0, burst=2000):
 
 
 def wl_c5(args):
+    """Serving at the stated configuration: 12 R-MAT graphs (scales 12-22, edge factors
+    8/16/32) and 4 random DAGs (n = 2^16..2^20, m = 8n) resident; Poisson streams of 60%
+    BFS rows (1-256 sources), 20% BC (64-1024 sources), 20% DAG reachable counts (1-256)
+    at three rates, then a saturation burst against the same requests one call each."""
     import gu
     import oracle
     torch = _torch()
     rng = np.random.default_rng(5)
-    # 12 R-MAT graphs, scales 12-18 and edge factors 8/16/32, and 4 random DAGs
-    # (n from 2^16 to 2^18, m = 8n): the resident set of a serving replica
-    rmats, dags, comp_edges = _serving_set(torch, 12, (12, 18), 4, (16, 18), rng)
+    t_build = time.perf_counter()
+    rmats, dags, comp_edges = _serving_set(torch, 12, (12, 22), 4, (16, 20), rng)
+    t_build = time.perf_counter() - t_build
     results = []
-    cpu_ms = []
-    plan = None
-    for rate in (100.0, 400.0, 1600.0, 3200.0, 6400.0):
-        plan = _serving_plan(rng, rmats, dags, rate, 2.0, 256)
+    for rate in (50.0, 200.0, 800.0):
+        plan = _serving_plan(rng, rmats, dags, rate, 2.0, 1024)
         r = _serve_stream(plan, comp_edges)
         r["offered_rate_per_s"] = rate
         results.append(r)
-    # the same request stream one call per request, no batching or overlap (the plain form):
-    # host sources in, host results out, as the server's requests
-    one_by_one = _one_call_per_request(torch, plan[:2000], comp_edges)
-    one_by_one["note"] = "the first 2000 requests of the last rate's stream, one synchronous call per request"
+    burst = [(0.0,) + p[1:] for p in _serving_plan(rng, rmats, dags, 1000.0, 1.0, 1024)[:600]]
+    sat = _serve_stream(burst, comp_edges)
+    one_by_one = _one_call_per_request(torch, burst, comp_edges)
+    saturation = {"requests": sat["requests"], "served_per_s": sat["served_per_s"],
+                  "served_gteps_bfs_bc": sat["served_gteps_bfs_bc"], "p50_ms": sat["p50_ms"],
+                  "p99_ms": sat["p99_ms"], "mean_requests_per_batch": sat["mean_requests_per_batch"],
+                  "one_call_per_request_per_s": one_by_one["requests_per_s"],
+                  "one_call_per_request_gteps": one_by_one["gteps_bfs_bc"],
+                  "speedup_vs_one_call_per_request": sat["served_per_s"] / one_by_one["requests_per_s"]}
     # CPU: per-request oracle time on a sample of requests of each kind
-    for (t_, q, hg, g, srcs) in plan[:24]:
+    cpu_ms = []
+    for (t_, q, hg, g, srcs) in burst[:24]:
         if q == gu.QUERY_BC:
             _, c = _cpu(oracle.bc, hg.R, hg.C, hg.n, srcs[:8], nthreads=os.cpu_count() or 1)
             c *= len(srcs) / 8.0
@@ -540,11 +578,14 @@ def wl_c5(args):
         else:
             _, c = _cpu(oracle.bfs_multi, hg.R, hg.C, hg.n, srcs, nthreads=os.cpu_count() or 1)
         cpu_ms.append(c * 1e3)
-    _emit({"workload": "c5_serving_mix", "metric": "request latency p50 / p99", "unit": "ms",
-           "graphs": [n for n, _, _ in rmats + dags], "results": results, "one_call_per_request": one_by_one,
-           "mix": "60% BFS rows (1-256 sources), 20% BC (64-256 sources), 20% DAG reachable counts (1-256)",
+    _emit({"workload": "c5_serving_rmat12-22_dag2^16-2^20", "metric": "request latency p50 / p99", "unit": "ms",
+           "graphs": [n for n, _, _ in rmats + dags], "graph_build_s": t_build, "results": results,
+           "saturation": saturation,
+           "mix": "60% BFS rows (1-256 sources), 20% BC (64-1024 sources), 20% DAG reachable counts (1-256)",
+           "client": "open loop from the planned arrivals, at most min(48 GiB, a quarter of the host's available "
+                     "memory) of result buffers held",
            "cpu_per_request_ms_median": statistics.median(cpu_ms),
-           "cpu_sample": "first 24 requests of the last rate, oracle on all host threads (BC extrapolated "
+           "cpu_sample": "first 24 requests of the burst, oracle on all host threads (BC extrapolated "
                          "from 8 sources per request)"})
 
 
