@@ -14,7 +14,8 @@
 // (transitive_closure.cuh:13); extract_edges_{block,warp}
 // (load_balanced_search.cuh:12-13, called as host functions here, without the
 // <<<1, BLOCK_SIZE>>> launch configuration); parse / parse_metis / parse_snap /
-// parse_market (parse.h:37-40); get_reachability_dag (dag_reachability.h:15).
+// parse_market (parse.h:37-40); get_reachability_dag (dag_reachability.h:15);
+// start_clock / end_clock, choose_device and power_measurer (util_device.cuh:38-60).
 //
 // Semantics kept: every source in [start, end) is searched; the returned rows
 // are those of the last R = min(end - start, #SMs) sources, source s in row
@@ -24,6 +25,7 @@
 #pragma once
 
 #include <algorithm>
+#include <cmath>  // the reference's headers brought it in through CUDA's
 #include <cstdint>
 #include <cstdio>
 #include <set>
@@ -110,6 +112,56 @@ struct timer {
 inline int rows_for(int start, int end) { return std::min(end - start, sm_count()); }
 
 }  // namespace gu_shim
+
+// Timing, device choice and power sampling (util_device.cuh:38-60, util_device.cu:4-130).
+inline void start_clock(cudaEvent_t &start, cudaEvent_t &end)
+{
+    cudaEventCreate(&start);
+    cudaEventCreate(&end);
+    cudaEventRecord(start, 0);
+}
+
+inline float end_clock(cudaEvent_t &start, cudaEvent_t &end)
+{
+    float ms = 0;
+    cudaEventRecord(end, 0);
+    cudaEventSynchronize(end);
+    cudaEventElapsedTime(&ms, start, end);
+    cudaEventDestroy(start);
+    cudaEventDestroy(end);
+    return ms / 1000.0f;  // seconds, as the reference returns
+}
+
+// op.device >= 0 selects it; -1 picks the device with the highest memory bandwidth.
+inline void choose_device(program_options &op)
+{
+    int chosen = -1;
+    gu_shim::check(gu_choose_device(op.device, &chosen), "choose_device");
+    op.device = chosen;
+    std::printf("Chosen device: %d\n", chosen);
+}
+
+// Board power over an interval, sampled every `period` ms (NVML, read-only).
+class power_measurer {
+public:
+    power_measurer(long period, const program_options &op) : period_(period), device_(op.device < 0 ? 0 : op.device) {}
+    ~power_measurer() { if (p_) gu_power_stop(p_, nullptr, nullptr); }
+    void start_power_sample() { gu_shim::check(gu_power_start(device_, (int)period_, &p_), "start_power_sample"); }
+    double end_power_sample()
+    {
+        double w = 0;
+        int64_t samples = 0;
+        gu_power p = p_;
+        p_ = nullptr;
+        gu_shim::check(gu_power_stop(p, &w, &samples), "end_power_sample");
+        return w;
+    }
+
+private:
+    long period_;
+    int device_;
+    gu_power p_ = nullptr;
+};
 
 class device_graph {
 public:
