@@ -66,7 +66,7 @@ def parse_args():
     p.add_argument("--kernel-only", action="store_true", help="skip e2e (for profiling runs)")
     p.add_argument("--power", action="store_true",
                    help="sample board power (NVML, read-only) during the timed region: adds a power object")
-    p.add_argument("--workload", choices=["c2", "c1", "c3", "c3-pass", "c3-launch", "c4", "c4-pass", "c5", "io", "dag"], default="c2",
+    p.add_argument("--workload", choices=["c2", "c1", "c3", "c3-pass", "c3-launch", "c4", "c4-pass", "lbs", "c5", "io", "dag"], default="c2",
                    help="c2: the headline BFS line (default); c1/c3/c4/c5/io/dag: the other configurations, "
                         "one JSON line each (bench_configs.py)")
     return p.parse_args()

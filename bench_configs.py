@@ -239,6 +239,33 @@ def wl_c3_pass(args):
                          for i, e in enumerate(tl) if i > 0]})
 
 
+def wl_lbs(args):
+    """Load-balanced search over the int32 degree array of the C4 grid (N = 4,194,304
+    counts): 25 calls (the last 20 timed, synchronous C-ABI call), the last checked
+    against the oracle (examples/load_balanced_search/lbs.cu:18-31)."""
+    import gu
+    import oracle
+    torch = _torch()
+    hg = gu.HostGraph.grid(2048, 2048, 0.05, seed=7)
+    deg = np.diff(hg.R).astype(np.int32)
+    counts = torch.as_tensor(deg, device="cuda")
+    scanned = torch.empty_like(counts)
+    result = torch.empty(int(deg.sum()), dtype=torch.int32, device="cuda")
+    ts = []
+    for i in range(25):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        gu.lbs(counts, scanned, result)
+        if i >= 5:
+            ts.append(time.perf_counter() - t0)
+    s_ref, r_ref, tot = oracle.lbs(deg)
+    exact = bool(np.array_equal(scanned.cpu().numpy(), s_ref) and np.array_equal(result.cpu().numpy(), r_ref))
+    alg = 4.0 * len(deg) * 2 + 4.0 * tot
+    _emit({"workload": "lbs_grid2048_degrees", "metric": "load-balanced search call time", "unit": "ms",
+           "N": len(deg), "total": tot, "call_ms_min": 1e3 * min(ts), "call_ms_median": 1e3 * statistics.median(ts),
+           "alg_bytes": alg, "bit_exact": exact})
+
+
 def wl_c4_pass(args):
     """Profiling case: the per-source engine in counting mode (diameter over the 256 C4
     sources, no rows), three times, on the C4 grid."""
@@ -672,4 +699,4 @@ def wl_dag(args):
 
 
 def run(workload, args):
-    {"c1": wl_c1, "c3": wl_c3, "c3-pass": wl_c3_pass, "c3-launch": wl_c3_launch, "c4": wl_c4, "c4-pass": wl_c4_pass, "c5": wl_c5, "io": wl_io, "dag": wl_dag}[workload](args)
+    {"c1": wl_c1, "c3": wl_c3, "c3-pass": wl_c3_pass, "c3-launch": wl_c3_launch, "c4": wl_c4, "c4-pass": wl_c4_pass, "lbs": wl_lbs, "c5": wl_c5, "io": wl_io, "dag": wl_dag}[workload](args)
