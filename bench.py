@@ -289,9 +289,17 @@ def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
         return
-    hg, srcs = build_workload(args.scale, args.sources)
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
+    # the input is built by the oracle's own restatement of the generator (the same CSR and
+    # sources as the library's), so that this arm runs without the library
+    R, C = oracle.rmat(args.scale, EDGE_FACTOR, 0.57, 0.19, 0.19, seed=GRAPH_SEED, permute=True)
+
+    class _Graph:
+        pass
+    hg = _Graph()
+    hg.R, hg.C, hg.n, hg.m = R, C, len(R) - 1, len(C)
+    srcs = oracle.sources(hg.n, args.sources, SOURCE_SEED)
     cores = os.cpu_count() or 1
     per_step = cores  # one source per host thread per step
     times, edges = [], []

@@ -407,3 +407,168 @@ int64_t oracle_dag_reach_counts(const int32_t *R, const int32_t *C, int32_t n, i
     free(order);
     return pairs;
 }
+
+/* ---- the benchmark graph generator, restated for the CPU baseline --------------
+ * The reference ships no generator; the benchmark's R-MAT graph and its sources
+ * are defined by the library's generator (SplitMix64 seeding xoshiro256**, the
+ * published PRNGs of Steele-Lea-Flood and Blackman-Vigna; R-MAT descent of
+ * Chakrabarti-Zhan-Faloutsos; chunks of 65536 edges each seeded from the graph
+ * seed; Fisher-Yates relabelling; symmetrised CSR with sorted, duplicate-free
+ * lists and no self-loops).  This is an independent single-threaded statement of
+ * that definition, so that the reference arm builds its input without the
+ * library; tests/test_oracle.py checks it equals the library's output. */
+static uint64_t g_mix(uint64_t *x)
+{
+    uint64_t z = (*x += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+typedef struct {
+    uint64_t s[4];
+} g_rng;
+
+static void g_seed(g_rng *r, uint64_t seed)
+{
+    for (int i = 0; i < 4; ++i) r->s[i] = g_mix(&seed);
+}
+
+static uint64_t g_rotl(uint64_t x, int k) { return (x << k) | (x >> (64 - k)); }
+
+static uint64_t g_next(g_rng *r)
+{
+    uint64_t *s = r->s;
+    const uint64_t out = g_rotl(s[1] * 5, 7) * 9, t = s[1] << 17;
+    s[2] ^= s[0];
+    s[3] ^= s[1];
+    s[1] ^= s[2];
+    s[0] ^= s[3];
+    s[2] ^= t;
+    s[3] = g_rotl(s[3], 45);
+    return out;
+}
+
+static uint64_t g_below(g_rng *r, uint64_t bound)
+{
+    if (bound <= 1) return 0;
+    const uint64_t lim = ~0ull - (~0ull % bound);
+    uint64_t x;
+    do {
+        x = g_next(r);
+    } while (x >= lim);
+    return x % bound;
+}
+
+static int g_cmp_i32(const void *p, const void *q)
+{
+    const int32_t a = *(const int32_t *)p, b = *(const int32_t *)q;
+    return (a > b) - (a < b);
+}
+
+int oracle_rmat(int scale, int edge_factor, double a, double b, double c, uint64_t seed, int permute,
+                int32_t **R_out, int32_t **C_out, int64_t *m_out)
+{
+    if (scale < 1 || scale > 30 || edge_factor < 1) return -1;
+    const int32_t n = (int32_t)(1u << scale);
+    const int64_t ne = (int64_t)edge_factor << scale, chunk = 65536;
+    int32_t *eu = malloc(sizeof(int32_t) * (size_t)ne), *ev = malloc(sizeof(int32_t) * (size_t)ne);
+    if (!eu || !ev) return -2;
+    for (int64_t ch = 0; ch * chunk < ne; ++ch) {
+        uint64_t x = seed ^ (0xD1B54A32D192ED03ull * (uint64_t)(ch + 1));
+        g_rng r;
+        g_seed(&r, g_mix(&x));
+        for (int64_t e = ch * chunk; e < ne && e < (ch + 1) * chunk; ++e) {
+            uint32_t u = 0, v = 0;
+            for (int bit = 0; bit < scale; ++bit) {
+                const double p = (double)(g_next(&r) >> 11) * 0x1.0p-53;
+                if (p < a) continue;
+                if (p < a + b) v |= 1u << bit;
+                else if (p < a + b + c) u |= 1u << bit;
+                else {
+                    u |= 1u << bit;
+                    v |= 1u << bit;
+                }
+            }
+            eu[e] = (int32_t)u;
+            ev[e] = (int32_t)v;
+        }
+    }
+    if (permute) {
+        int32_t *perm = malloc(sizeof(int32_t) * (size_t)n);
+        if (!perm) return -2;
+        for (int32_t i = 0; i < n; ++i) perm[i] = i;
+        g_rng r;
+        g_seed(&r, seed ^ 0x5EED5EED5EED5EEDull);
+        for (int32_t i = n - 1; i > 0; --i) {
+            const int32_t j = (int32_t)g_below(&r, (uint64_t)i + 1);
+            const int32_t t = perm[i];
+            perm[i] = perm[j];
+            perm[j] = t;
+        }
+        for (int64_t e = 0; e < ne; ++e) {
+            eu[e] = perm[eu[e]];
+            ev[e] = perm[ev[e]];
+        }
+        free(perm);
+    }
+    /* symmetric CSR: both directions of every non-loop edge, then sort and unique each list */
+    int64_t *off = calloc((size_t)n + 1, sizeof(int64_t));
+    if (!off) return -2;
+    for (int64_t e = 0; e < ne; ++e)
+        if (eu[e] != ev[e]) {
+            off[eu[e] + 1]++;
+            off[ev[e] + 1]++;
+        }
+    for (int32_t v = 0; v < n; ++v) off[v + 1] += off[v];
+    int32_t *tmp = malloc(sizeof(int32_t) * (size_t)(off[n] > 0 ? off[n] : 1));
+    int64_t *pos = malloc(sizeof(int64_t) * (size_t)n);
+    if (!tmp || !pos) return -2;
+    memcpy(pos, off, sizeof(int64_t) * (size_t)n);
+    for (int64_t e = 0; e < ne; ++e)
+        if (eu[e] != ev[e]) {
+            tmp[pos[eu[e]]++] = ev[e];
+            tmp[pos[ev[e]]++] = eu[e];
+        }
+    free(eu);
+    free(ev);
+    free(pos);
+    int32_t *R = malloc(sizeof(int32_t) * ((size_t)n + 1));
+    if (!R) return -2;
+    int64_t m = 0;
+    R[0] = 0;
+    for (int32_t v = 0; v < n; ++v) {
+        int32_t *lst = tmp + off[v];
+        const int64_t len = off[v + 1] - off[v];
+        qsort(lst, (size_t)len, sizeof(int32_t), g_cmp_i32);
+        for (int64_t i = 0; i < len; ++i)
+            if (i == 0 || lst[i] != lst[i - 1]) tmp[m++] = lst[i];  /* m <= off[v]: compaction in place */
+        R[v + 1] = (int32_t)m;
+    }
+    free(off);
+    *R_out = R;
+    *C_out = tmp;
+    *m_out = m;
+    return 0;
+}
+
+int oracle_sources(int32_t n, int32_t k, uint64_t seed, int32_t *out)
+{
+    if (k < 0 || k > n) return -1;
+    int32_t *idx = malloc(sizeof(int32_t) * (size_t)(n > 0 ? n : 1));
+    if (!idx) return -2;
+    for (int32_t i = 0; i < n; ++i) idx[i] = i;
+    g_rng r;
+    g_seed(&r, seed);
+    for (int32_t i = 0; i < k; ++i) {
+        const int32_t j = i + (int32_t)g_below(&r, (uint64_t)(n - i));
+        const int32_t t = idx[i];
+        idx[i] = idx[j];
+        idx[j] = t;
+    }
+    memcpy(out, idx, sizeof(int32_t) * (size_t)k);
+    free(idx);
+    return 0;
+}
+
+void oracle_free(void *p) { free(p); }

@@ -106,6 +106,14 @@ int32_t oracle_race_and_resolve(uint32_t vote, int32_t lane);
 int64_t oracle_dag_reach_pairs(const int32_t *R, const int32_t *C, int32_t n);
 int64_t oracle_dag_reach_counts(const int32_t *R, const int32_t *C, int32_t n, int64_t *counts);
 
+/* The benchmark's R-MAT graph (symmetrised int32 CSR, malloc'd: free with
+ * oracle_free) and its k distinct sources, restated from the library's generator
+ * definition so that the CPU baseline builds its input on its own. */
+int oracle_rmat(int scale, int edge_factor, double a, double b, double c, uint64_t seed, int permute,
+                int32_t **R_out, int32_t **C_out, int64_t *m_out);
+int oracle_sources(int32_t n, int32_t k, uint64_t seed, int32_t *out);
+void oracle_free(void *p);
+
 #ifdef __cplusplus
 }
 #endif

@@ -52,6 +52,13 @@ def lib():
         L.oracle_dag_reach_pairs.restype = ctypes.c_int64
         L.oracle_dag_reach_counts.argtypes = [_i32p, _i32p, ctypes.c_int32, ctypes.POINTER(ctypes.c_int64)]
         L.oracle_dag_reach_counts.restype = ctypes.c_int64
+        L.oracle_rmat.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                  ctypes.c_uint64, ctypes.c_int, ctypes.POINTER(_i32p), ctypes.POINTER(_i32p),
+                                  ctypes.POINTER(ctypes.c_int64)]
+        L.oracle_rmat.restype = ctypes.c_int
+        L.oracle_sources.argtypes = [ctypes.c_int32, ctypes.c_int32, ctypes.c_uint64, _i32p]
+        L.oracle_sources.restype = ctypes.c_int
+        L.oracle_free.argtypes = [ctypes.c_void_p]
         _lib = L
     return _lib
 
@@ -158,3 +165,27 @@ def dag_reach_counts(R, C, n):
     out = np.zeros(max(n, 1), np.int64)
     tot = lib().oracle_dag_reach_counts(_p(R), _p(C), n, out.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)))
     return out[:n], int(tot)
+
+
+def rmat(scale, edge_factor=16, a=0.57, b=0.19, c=0.19, seed=1, permute=True):
+    """The benchmark's R-MAT graph, built by the oracle's own restatement of the
+    generator: (R, C) int32 numpy arrays of the symmetrised CSR."""
+    R, C, m = _i32p(), _i32p(), ctypes.c_int64()
+    rc = lib().oracle_rmat(scale, edge_factor, a, b, c, seed, int(permute), ctypes.byref(R), ctypes.byref(C),
+                           ctypes.byref(m))
+    if rc != 0:
+        raise ValueError(f"oracle_rmat failed ({rc})")
+    n = 1 << scale
+    Rn = np.ctypeslib.as_array(R, shape=(n + 1,)).copy()
+    Cn = np.ctypeslib.as_array(C, shape=(max(m.value, 1),))[: m.value].copy()
+    lib().oracle_free(ctypes.cast(R, ctypes.c_void_p))
+    lib().oracle_free(ctypes.cast(C, ctypes.c_void_p))
+    return Rn, Cn
+
+
+def sources(n, k, seed):
+    """k distinct sources of [0, n), as the benchmark draws them."""
+    out = np.empty(max(k, 1), np.int32)
+    if lib().oracle_sources(n, k, seed, _p(out)) != 0:
+        raise ValueError("need 0 <= k <= n")
+    return out[:k]

@@ -283,3 +283,16 @@ def test_oracle_dag_and_lbs_vs_reference_on_random_inputs(tmp_path):
         assert t == int(counts.sum()) == len(result), f"lbs case {case}"
         np.testing.assert_array_equal(s[:N], scanned, err_msg=f"lbs case {case}")
         np.testing.assert_array_equal(r[:t], result, err_msg=f"lbs case {case}")
+
+
+@pytest.mark.parametrize("scale,permute,seed", [(10, True, 3), (12, False, 5), (14, True, 1)])
+def test_oracle_generator_equals_the_library(scale, permute, seed):
+    """The oracle's restated R-MAT generator and source sampler (used by the CPU
+    baseline to build its input without the library) give the library's CSR and
+    sources exactly."""
+    import gu
+    hg = gu.HostGraph.rmat(scale, 16, 0.57, 0.19, 0.19, seed=seed, permute=permute)
+    R, C = oracle.rmat(scale, 16, 0.57, 0.19, 0.19, seed=seed, permute=permute)
+    np.testing.assert_array_equal(hg.R, R)
+    np.testing.assert_array_equal(hg.C, C)
+    np.testing.assert_array_equal(gu.sources(hg.n, 300, seed=seed + 1), oracle.sources(hg.n, 300, seed + 1))
