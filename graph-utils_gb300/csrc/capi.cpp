@@ -471,6 +471,7 @@ static void bfs_device(DeviceGraph &g, int variant, const int32_t *sources_dev, 
             opt.alpha = g.tune.alpha;
             opt.beta = g.tune.beta;
             opt.batch_words = g.tune.words;
+            opt.max_blocks = g.tune.ctas_per_sm > 0 ? g.sm_count * g.tune.ctas_per_sm : 0;
             opt.tuned = true;
         }
     } else if (variant == GU_BFS_AUTO) {
@@ -525,12 +526,13 @@ gu_status gu_graph_autotune(gu_graph g, const int32_t *sources_dev, int32_t k, g
         int32_t *const rows = scratch.rows;
         const cudaStream_t st = scratch.st;
         std::vector<gu_tuning> cand;
-        auto add = [&](int engine, float alpha, float beta, int words) {
+        auto add = [&](int engine, float alpha, float beta, int words, int ctas = 0) {
             gu_tuning t;
             t.engine = engine;
             t.alpha = alpha;
             t.beta = beta;
             t.words = words;
+            t.ctas_per_sm = ctas;
             t.seconds = 0;
             cand.push_back(t);
         };
@@ -538,8 +540,10 @@ gu_status gu_graph_autotune(gu_graph g, const int32_t *sources_dev, int32_t k, g
         if (dg.n <= 65536) add(GU_ENGINE_ONE_CTA, 0, 0, 0);
         const int wd = msbfs_words_for(k);
         const float grid[][2] = {{2.f, 24.f}, {1.f, 24.f}, {4.f, 24.f}, {8.f, 24.f}, {2.f, 12.f}, {2.f, 48.f}};
-        for (int w = wd; w >= 1 && w >= wd / 2; w /= 2)
+        for (int w = wd; w >= 1 && w >= wd / 2; w /= 2) {
             for (const auto &ab : grid) add(GU_ENGINE_BATCHED, ab[0], ab[1], w);
+            add(GU_ENGINE_BATCHED, 2.f, 24.f, w, 1);  // half the grid: one CTA per SM
+        }
         const DeviceGraph::Tuning saved = dg.tune;
         gu_tuning pick{};
         pick.seconds = -1;
@@ -551,6 +555,7 @@ gu_status gu_graph_autotune(gu_graph g, const int32_t *sources_dev, int32_t k, g
                 dg.tune.alpha = t.alpha;
                 dg.tune.beta = t.beta;
                 dg.tune.words = t.words;
+                dg.tune.ctas_per_sm = t.ctas_per_sm;
                 bool fell_back = false;
                 double best_t = 1e30;
                 for (int rep = 0; rep < 3; ++rep) {
@@ -587,6 +592,7 @@ gu_status gu_graph_autotune(gu_graph g, const int32_t *sources_dev, int32_t k, g
         dg.tune.alpha = pick.alpha;
         dg.tune.beta = pick.beta;
         dg.tune.words = pick.words;
+        dg.tune.ctas_per_sm = pick.ctas_per_sm;
         if (best) *best = pick;
         if (ntrials) *ntrials = std::min(nt, max_trials);
     });
@@ -609,11 +615,14 @@ gu_status gu_graph_set_tuning(gu_graph g, const gu_tuning *t)
         if (t->engine == GU_ENGINE_BATCHED &&
             (!(t->alpha > 0) || !(t->beta > 0) || (t->words != 0 && t->words != 1 && t->words != 2 && t->words != 4)))
             throw gu_error(GU_ERR_INVALID_ARGUMENT, "batched engine needs alpha, beta > 0 and words 0, 1, 2 or 4");
+        if (t->ctas_per_sm < 0 || t->ctas_per_sm > 2)
+            throw gu_error(GU_ERR_INVALID_ARGUMENT, "ctas_per_sm must be 0, 1 or 2");
         dg.tune.set = true;
         dg.tune.engine = t->engine;
         dg.tune.alpha = t->alpha;
         dg.tune.beta = t->beta;
         dg.tune.words = t->words;
+        dg.tune.ctas_per_sm = t->ctas_per_sm;
     });
 }
 

@@ -143,6 +143,7 @@ struct DeviceGraph {
         int engine = 0;  // gu_engine
         float alpha = 2.f, beta = 24.f;
         int words = 0;
+        int ctas_per_sm = 0;  // batched engine's grid: CTAs per SM (0: as many as fit)
     } tune;
     void *ctl_host = nullptr;  // pinned copy of the batched engine's control block, written after each launch
     int32_t *ell = nullptr;  // low-degree graphs: neighbours padded to ell_width per vertex (-1), built on first use

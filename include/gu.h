@@ -216,7 +216,8 @@ gu_status gu_graph_level_idle(gu_graph g, int max_entries, double *idle_cta_ms, 
  * one-CTA-per-source form (n <= 65536), and the batched engine over a grid of
  * direction thresholds (alpha: top-down -> bottom-up when the frontier's
  * out-edges exceed m / alpha; beta: back when the frontier holds fewer than
- * n / beta vertices) and source words per batch; slow candidates are cut after
+ * n / beta vertices), source words per batch and the persistent grid's CTAs
+ * per SM (the CTA itself is 512 threads: its register budget fixes that); slow candidates are cut after
  * one run.  trials (optional, room for max_trials) receives every measured
  * candidate in order; best receives the choice.  Distances do not depend on the
  * choice.  No reference counterpart (its examples pick the kernel by hand). */
@@ -230,6 +231,7 @@ typedef struct gu_tuning {
     int32_t engine;     /* gu_engine */
     float alpha, beta;  /* batched engine's direction thresholds */
     int32_t words;      /* batched engine: 64-source words per batch (1, 2 or 4) */
+    int32_t ctas_per_sm; /* batched engine: CTAs per SM of its persistent grid (0: as many as fit, or 1, 2) */
     double seconds;     /* measured kernel time on the sample (autotune output) */
 } gu_tuning;
 

@@ -252,6 +252,12 @@ def test_autotune_keeps_distances(shape):
         np.testing.assert_array_equal(run_bfs(g, srcs, "auto")[0], ref, err_msg=str(t))
     with pytest.raises(gu.GuError):
         g.set_tuning({"engine": "batched", "alpha": 2.0, "beta": 24.0, "words": 3})
+    # the grid's CTAs per SM is a tuning dimension too: one CTA per SM gives the same rows
+    assert any(t["engine"] == "batched" and t["ctas_per_sm"] == 1 for t in trials)
+    g.set_tuning({"engine": "batched", "alpha": 2.0, "beta": 24.0, "words": 0, "ctas_per_sm": 1})
+    np.testing.assert_array_equal(run_bfs(g, srcs, "auto")[0], ref)
+    with pytest.raises(gu.GuError):
+        g.set_tuning({"engine": "batched", "alpha": 2.0, "beta": 24.0, "words": 0, "ctas_per_sm": 3})
     g.set_tuning(None)
     np.testing.assert_array_equal(run_bfs(g, srcs, "auto")[0], ref)
 
