@@ -34,8 +34,14 @@
 
 namespace gu {
 
-constexpr int LOCAL_THREADS = 512;
-constexpr int LOCAL_QCAP = 12288;     // vertices per shared-memory level queue (two queues: 96 KiB)
+// One 1024-thread CTA per source, two per SM: 256 sources fill the GPU, and a
+// level's frontier (a few thousand vertices on a 2048 x 2048 mesh) takes one or
+// two dependent load chains per thread.  The queues are kept small because the
+// shared memory they do not use is L1: on the 2048 x 2048 grid with 256 sources,
+// rows took 62.6 ms with 512 threads and two 12288-vertex queues, 40.5 ms with
+// 1024 threads and two 6144-vertex queues, and no less with smaller queues.
+constexpr int LOCAL_THREADS = 1024;
+constexpr int LOCAL_QCAP = 6144;      // vertices per shared-memory level queue (two queues: 48 KiB)
 constexpr int LOCAL_MAX_DEGREE = 16;     // AUTO takes this engine up to this out-degree
 constexpr int PLAIN_MAX_VERTICES = 4096;  // ... and the one-CTA-per-source form up to this many vertices
 constexpr size_t LOCAL_SMEM = 2 * LOCAL_QCAP * sizeof(int32_t);
