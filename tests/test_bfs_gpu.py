@@ -161,6 +161,55 @@ def test_per_source_engine_overflow_falls_back():
     np.testing.assert_array_equal(cnt.cpu().numpy(), (ref != gu.UNREACHABLE).sum(1))
 
 
+def _layered_graph(width=5000, depth=6):
+    """Undirected, out-degree <= 5: a binary tree from vertex 0 down to a layer of
+    `width` vertices, then `depth` such layers joined vertex to vertex (and each
+    vertex to its right-hand neighbour in the layer)."""
+    u, v, layer, nxt = [], [], [0], 1
+    while len(layer) < width:
+        children = []
+        for p in layer:
+            for _ in range(2):
+                if len(children) < width:
+                    u.append(p)
+                    v.append(nxt)
+                    children.append(nxt)
+                    nxt += 1
+        layer = children
+    for _ in range(depth):
+        below = list(range(nxt, nxt + width))
+        nxt += width
+        u += layer + below[:-1]
+        v += below + below[1:]
+        layer = below
+    return gu.HostGraph.from_edges(nxt, np.array(u), np.array(v))
+
+
+def test_per_source_engine_wide_levels():
+    """Levels of 5000 vertices, near the per-source engine's shared queue (6144):
+    rows, counts and levels equal the oracle's, and so they do on the same graph
+    cut to levels of 3000."""
+    hg = _layered_graph()
+    assert hg.degrees().max() <= 16 and not hg.directed
+    g = gu.Graph(hg)
+    srcs = np.concatenate([[0], gu.sources(hg.n, 63, seed=4)]).astype(np.int32)
+    ref, _ = oracle.bfs_multi(hg.R, hg.C, hg.n, srcs, nthreads=8)
+    assert np.bincount(ref[0][ref[0] != gu.UNREACHABLE]).max() == 5000  # from the root
+    got, _ = run_bfs(g, srcs, "auto")
+    np.testing.assert_array_equal(got, ref)
+    s = torch.as_tensor(srcs, device="cuda")
+    assert g.diameter(s) == int(ref[ref != gu.UNREACHABLE].max())
+    cnt = torch.empty(len(srcs), dtype=torch.int64, device="cuda")
+    g.reach(s, cnt)
+    np.testing.assert_array_equal(cnt.cpu().numpy(), (ref != gu.UNREACHABLE).sum(1))
+    # the same graph cut to levels of 3000
+    hg2 = _layered_graph(width=3000)
+    g2 = gu.Graph(hg2)
+    ref2, _ = oracle.bfs_multi(hg2.R, hg2.C, hg2.n, srcs % hg2.n, nthreads=8)
+    got2, _ = run_bfs(g2, srcs % hg2.n, "auto")
+    np.testing.assert_array_equal(got2, ref2)
+
+
 def test_host_form_matches_device_form():
     hg = gu.HostGraph.rmat(12, 16, seed=1)
     g = gu.Graph(hg)
