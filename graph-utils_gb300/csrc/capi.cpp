@@ -793,6 +793,17 @@ gu_status gu_lbs(const int32_t *counts_dev, int32_t N, int32_t *scanned_dev, int
     });
 }
 
+gu_status gu_lbs_last_ms(double *ms)
+{
+    return guarded([&] {
+        if (!ms) throw gu_error(GU_ERR_INVALID_ARGUMENT, "null output");
+        int dev = 0;
+        GU_CUDA_CHECK(cudaGetDevice(&dev));
+        std::lock_guard<std::mutex> lk(g_scratch_call_mu);
+        *ms = lbs_last_ms(dev);
+    });
+}
+
 gu_status gu_race_and_resolve(const int32_t *predicates_dev, int32_t nwarps, int32_t *winners_dev, void *stream)
 {
     return guarded([&] {

@@ -253,6 +253,7 @@ int bc_read_timeline(DeviceGraph &g, int max_entries, int32_t *batch, int32_t *l
 size_t lbs_scratch_bytes(int32_t N, int64_t result_capacity);
 void launch_lbs(const int32_t *counts, int32_t N, int32_t *scanned, int32_t *result, int64_t result_capacity,
                 int32_t *total_dev, int64_t *total_host, void *scratch_ptr, size_t scratch_bytes, cudaStream_t st);
+double lbs_last_ms(int device);
 void launch_race_and_resolve(const int32_t *pred, int32_t nwarps, int32_t *winner, cudaStream_t st);
 
 // Board power sampling through NVML loaded at run time (power.cpp).

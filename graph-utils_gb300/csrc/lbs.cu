@@ -5,24 +5,27 @@
 // sum, and result[i] for every work slot i < total = the item owning it
 // (upper_bound(scanned, i) - 1).  The reference runs it in ONE CTA whose threads
 // each walk the scanned array from the start (quadratic in the item count);
-// here two kernels:
-//   1. lbs_scan_single: a single-pass scan with decoupled look-back.  A CTA
-//      takes the next tile of 8192 counts (a ticket, so it only ever waits on
-//      tiles already taken), scans it in shared memory, publishes the tile's sum
-//      and then -- after looking back over its predecessors' published sums --
-//      its inclusive prefix; it writes its part of scanned and the merge-path
-//      endpoints of the search tiles whose first diagonal lies in its own
-//      stretch of the merge (the merge of slot keys 0..total-1 with the offsets,
-//      ties to the offsets; the stretch of items [k0, k1) is diagonals
-//      [k0 + P, k1 + P + A), P its prefix and A its sum, and depends on nothing
-//      else).  The tile holding the last counts knows the total and decides
-//      whether the call may write results (no negative count, total within
-//      int32 and within the result capacity, a result buffer when the total is
-//      positive).  Every wait is bounded.
-//   2. lbs_search: each CTA takes search tiles of 4092 diagonals; the items a
-//      tile consumes mark their first slots in shared memory and a block-wide
-//      running maximum turns the marks into owners, written 16 bytes at a time.
-//   Both are queued at once; the host waits once, at the end.
+// here three kernels:
+//   1. lbs_tile_sums: the sum of every tile of 8192 counts (and a flag for a
+//      negative count).
+//   2. lbs_scan_apply: each tile adds the sums of the tiles before it (all final,
+//      so no tile waits on another), scans its counts again from L2, writes its
+//      part of scanned and the merge-path endpoints of the search tiles whose
+//      first diagonal lies in its own stretch of the merge; the tile holding the
+//      last counts knows the total and decides whether the call may write
+//      results (no negative count, total within int32 and within the result
+//      capacity, a result buffer when the total is positive).  A single-pass
+//      scan with decoupled look-back took longer: with 512 tiles in flight a
+//      published tile sum reached the tiles polling for it only microseconds
+//      later, however the polling was arranged.
+//   3. lbs_search: persistent CTAs (eight per SM) take search tiles of 4092
+//      diagonals; the items a tile consumes mark their first slots in shared
+//      memory and a block-wide running maximum turns the marks into owners,
+//      written 16 bytes at a time.  A CTA loads its next tile's path endpoints
+//      and first offsets before working on the current tile.
+//   Kernels 2 and 3 are launched as programmatic dependents of their
+//   predecessor, so that their launch overlaps its tail; the host waits once,
+//   at the end.
 // race_and_resolve (race_and_resolve.cuh:13-25) is exposed as a warp-level
 // kernel over an array of predicates for testing the device primitive.
 #include "device_utils.cuh"
@@ -71,51 +74,90 @@ __device__ __forceinline__ long long block_exscan_ll(long long x, long long *s_w
     return r;
 }
 
-// Tile status word of the look-back: flag in bits 62-63 (1: the tile's sum, 2:
-// its inclusive prefix), value in bits 0-61 (sums of int32 counts over at most
-// 2^31 items fit).
-constexpr unsigned long long LB_FLAG_SUM = 1ull << 62, LB_FLAG_PREFIX = 2ull << 62;
-constexpr unsigned long long LB_VALUE = (1ull << 62) - 1ull;
+// Programmatic dependent launch: a kernel launched with programmatic stream
+// serialization may start while its predecessor is still running; it waits
+// here for the predecessor's completion (and its memory) before reading its
+// results.  A kernel lets its successor start launching once all of its own
+// CTAs have started (every CTA calls launch_dependents first): the successor's
+// CTAs then only take SM room that this kernel's CTAs no longer need.
+__device__ __forceinline__ void griddep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void griddep_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;" :::); }
 
-__device__ __forceinline__ void st_release_u64(unsigned long long *p, unsigned long long v)
+// Pass 1: the sum of each tile of LBS_SCAN_TILE counts, and the negative-count
+// flag.  The counts are read with the default caching so that they are still in
+// L2 for pass 2.
+__global__ void __launch_bounds__(LBS_THREADS) lbs_tile_sums(const int32_t *__restrict__ counts, int32_t N,
+                                                            long long *__restrict__ sums, int *neg)
 {
-    asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+    griddep_launch_dependents();
+    __shared__ long long s_part[LBS_THREADS / 32];
+    const long long k0 = (long long)blockIdx.x * LBS_SCAN_TILE;
+    const int nk = (int)min((long long)LBS_SCAN_TILE, (long long)N - k0);
+    long long sum = 0;
+    bool bad = false;
+#pragma unroll
+    for (int r = 0; r < LBS_ITEMS; ++r) {
+        const int i = threadIdx.x + r * LBS_THREADS;
+        const int32_t c = i < nk ? __ldg(counts + k0 + i) : 0;
+        bad |= c < 0;
+        sum += c;
+    }
+    if (__any_sync(FULL_MASK, bad) && lane_id() == 0) atomicOr(neg, 1);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(FULL_MASK, sum, o);
+    if (lane_id() == 0) s_part[warp_in_block()] = sum;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        long long t = 0;
+#pragma unroll
+        for (int w = 0; w < LBS_THREADS / 32; ++w) t += s_part[w];
+        sums[blockIdx.x] = t;
+    }
 }
 
-// Scan, merge-path endpoints and verdict in one pass (see the file comment).
+// Pass 2: each tile adds up the sums of the tiles before it (all of them are
+// final: pass 1 has completed), scans its counts again (from L2), writes its part
+// of scanned and the merge-path endpoints of the search tiles whose first
+// diagonal lies in its own stretch of the merge (the merge of slot keys
+// 0..total-1 with the offsets, ties to the offsets; the stretch of items
+// [k0, k1) is diagonals [k0 + P, k1 + P + A), P its prefix and A its sum, and
+// depends on nothing else).  The tile holding the last counts knows the total
+// and decides whether the call may write results (no negative count, total
+// within int32 and within the result capacity, a result buffer when the total
+// is positive).
 // kpart[t] = offsets consumed at diagonal t * LBS_TILE (t < kpart_len).
-__global__ void __launch_bounds__(LBS_THREADS) lbs_scan_single(
-    const int32_t *__restrict__ counts, int32_t N, int32_t ntiles, int32_t *__restrict__ scanned,
-    unsigned long long *status, int *ticket, int *neg, long long *total_p, int *ok, int *err, int32_t *total_out,
-    long long capacity, int has_result, int32_t *__restrict__ kpart, long long kpart_len, unsigned long long limit_ns)
+__global__ void __launch_bounds__(LBS_THREADS) lbs_scan_apply(
+    const int32_t *__restrict__ counts, int32_t N, int32_t ntiles, const long long *__restrict__ sums,
+    int32_t *__restrict__ scanned, const int *neg, long long *total_p, int *ok, int32_t *total_out, long long capacity,
+    int has_result, int32_t *__restrict__ kpart, long long kpart_len)
 {
+    griddep_launch_dependents();
+    griddep_wait();
     // the tile's counts, then (in place) its offsets relative to the tile's prefix
     // (int32: a tile sum beyond INT32_MAX fails the call anyway); element i at
     // i + i / 16, so that a thread's 16 consecutive elements (stride 17 across the
     // warp) and the striped global accesses are both free of bank conflicts
     __shared__ int32_t s_val[LBS_SCAN_TILE + LBS_SCAN_TILE / 16 + 1];
     __shared__ long long s_warp[33];
-    __shared__ int s_tile;
-    __shared__ long long s_prefix;
+    __shared__ long long s_part[LBS_THREADS / 32];
     auto at = [](int i) { return i + (i >> 4); };
-    if (threadIdx.x == 0) s_tile = atomicAdd(ticket, 1);
-    __syncthreads();
-    const int t = s_tile;
+    const int t = blockIdx.x;
     const long long k0 = (long long)t * LBS_SCAN_TILE;
     const int nk = (int)min((long long)LBS_SCAN_TILE, (long long)N - k0);
-    // counts in, coalesced; each thread then sums its LBS_ITEMS consecutive ones
-    bool bad = false;
-#pragma unroll 4
-    for (int i = threadIdx.x; i < LBS_SCAN_TILE; i += LBS_THREADS) {
-        const int32_t c = i < nk ? __ldcs(counts + k0 + i) : 0;
-        bad |= c < 0;
-        s_val[at(i)] = c;
+    long long x = 0;  // the sums of tiles 0 .. t-1
+    for (int i = threadIdx.x; i < t; i += LBS_THREADS) x += __ldcg(sums + i);
+#pragma unroll
+    for (int r = 0; r < LBS_ITEMS; ++r) {
+        const int i = threadIdx.x + r * LBS_THREADS;
+        s_val[at(i)] = i < nk ? __ldg(counts + k0 + i) : 0;
     }
-    if (__any_sync(FULL_MASK, bad) && lane_id() == 0) {
-        atomicOr(neg, 1);
-        __threadfence();
-    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(FULL_MASK, x, o);
+    if (lane_id() == 0) s_part[warp_in_block()] = x;
     __syncthreads();
+    long long P = 0;
+#pragma unroll
+    for (int w = 0; w < LBS_THREADS / 32; ++w) P += s_part[w];
     const int base = threadIdx.x * (LBS_ITEMS + 1);  // at(LBS_ITEMS * threadIdx.x)
     long long sum = 0;
 #pragma unroll
@@ -128,74 +170,7 @@ __global__ void __launch_bounds__(LBS_THREADS) lbs_scan_single(
         s_val[base + i] = (int32_t)run;
         run += c;
     }
-    // look-back: warp 0 publishes the sum, then reads 128 predecessors at a time
-    // (four per lane, loads issued together) until it meets one that has published
-    // its inclusive prefix, and publishes its own.  In the first wave the
-    // published prefixes advance about one tile per L2 round trip, so a window
-    // of 32 left late tiles a dozen rounds behind.
-    constexpr int LB_WIN = 4;
-    if (threadIdx.x < 32) {
-        const int lane = lane_id();
-        long long prefix = 0;
-        if (t == 0) {
-            if (lane == 0) st_release_u64(status, LB_FLAG_PREFIX | ((unsigned long long)agg & LB_VALUE));
-        } else {
-            if (lane == 0) st_release_u64(status + t, LB_FLAG_SUM | ((unsigned long long)agg & LB_VALUE));
-            long long j = t - 1;  // the nearest predecessor of this round
-            const unsigned long long t0 = global_timer_ns();
-            bool timed_out = false;
-            while (true) {
-                unsigned long long v[LB_WIN];
-#pragma unroll
-                for (int r = 0; r < LB_WIN; ++r) {  // element e = 32 r + lane is tile j - e
-                    const long long idx = j - (32 * r + lane);
-                    v[r] = idx >= 0 ? ld_acquire_u64(status + idx) : LB_FLAG_PREFIX;
-                }
-                unsigned spins = 0;
-                while (true) {
-                    bool waiting = false;
-#pragma unroll
-                    for (int r = 0; r < LB_WIN; ++r) waiting |= (v[r] >> 62) == 0;
-                    if (!__any_sync(FULL_MASK, waiting)) break;
-#pragma unroll
-                    for (int r = 0; r < LB_WIN; ++r)  // a predecessor has not published yet
-                        if ((v[r] >> 62) == 0) v[r] = ld_acquire_u64(status + (j - (32 * r + lane)));
-                    if ((++spins & 63u) == 0) {
-                        const bool late = global_timer_ns() - t0 > limit_ns || ld_volatile_i32(err) != 0;
-                        if (__any_sync(FULL_MASK, late)) {
-                            timed_out = true;
-                            break;
-                        }
-                    }
-                }
-                if (timed_out) break;
-                int stop = 32 * LB_WIN;  // the nearest element holding a prefix (none: the whole window)
-#pragma unroll
-                for (int r = LB_WIN - 1; r >= 0; --r) {
-                    const unsigned done = __ballot_sync(FULL_MASK, (v[r] >> 62) == 2);
-                    if (done) stop = 32 * r + __ffs(done) - 1;
-                }
-                long long x = 0;
-#pragma unroll
-                for (int r = 0; r < LB_WIN; ++r)
-                    if (32 * r + lane <= stop) x += (long long)(v[r] & LB_VALUE);
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(FULL_MASK, x, o);
-                prefix += x;
-                if (stop < 32 * LB_WIN) break;
-                j -= 32 * LB_WIN;
-            }
-            if (timed_out) {
-                if (lane == 0) atomicCAS(err, 0, 1);
-                prefix = 0;
-            }
-            // published even after a timeout, so that no successor waits on this tile
-            if (lane == 0) st_release_u64(status + t, LB_FLAG_PREFIX | ((unsigned long long)(prefix + agg) & LB_VALUE));
-        }
-        if (lane == 0) s_prefix = prefix;
-    }
     __syncthreads();
-    const long long P = s_prefix;
     for (int i = threadIdx.x; i < nk; i += LBS_THREADS) scanned[k0 + i] = (int32_t)(P + s_val[at(i)]);
     // merge-path endpoints of the search tiles starting in diagonals [k0 + P, k1 + P + agg)
     const long long k1 = k0 + nk;
@@ -217,9 +192,7 @@ __global__ void __launch_bounds__(LBS_THREADS) lbs_scan_single(
         const long long end = (total + N + LBS_TILE - 1) / LBS_TILE;  // the final endpoint, at diagonal total + N
         if (end < kpart_len) kpart[end] = N;
         *total_p = total;
-        __threadfence();
-        const bool good = ld_volatile_i32(neg) == 0 && ld_volatile_i32(err) == 0 && total <= INT32_MAX &&
-                          total <= capacity && (total == 0 || has_result);
+        const bool good = *neg == 0 && total <= INT32_MAX && total <= capacity && (total == 0 || has_result);
         *ok = good ? 1 : 0;
         if (good && total_out) *total_out = (int32_t)total;
     }
@@ -242,6 +215,7 @@ __global__ void __launch_bounds__(LBS_STHREADS, 8) lbs_search(const int32_t *__r
 {
     __shared__ int32_t s_mark[LBS_SPAN + LBS_SPAN / 16];
     __shared__ int32_t s_wmax[LBS_STHREADS / 32];
+    griddep_wait();
     if (!*ok) return;
     const long long total = *total_p;
     if (total == 0) return;  // no slots; the path endpoints were not written
@@ -249,19 +223,53 @@ __global__ void __launch_bounds__(LBS_STHREADS, 8) lbs_search(const int32_t *__r
     const int ra = (int)(((uintptr_t)result >> 2) & 3);  // result's element offset from a 16-byte boundary
     const int lane = lane_id(), warp = warp_in_block();
     const int base = threadIdx.x * 17;  // position 16 t in the padded array
-    for (long long tile = blockIdx.x; tile < ntile; tile += gridDim.x) {  // block-uniform
+    // software pipeline over the CTA's tiles: the next tile's path endpoints and
+    // its first 4 * LBS_STHREADS offsets (four per thread, in registers) are
+    // loaded before the current tile is worked on
+    constexpr int PRE = 4;
+    long long tile = blockIdx.x;
+    int32_t k0 = 0, k1 = 0;
+    int32_t pre[PRE];
+    if (tile < ntile) {
+        k0 = __ldg(kpart + tile);
+        k1 = __ldg(kpart + tile + 1);
+#pragma unroll
+        for (int r = 0; r < PRE; ++r) {
+            const int t = threadIdx.x + r * LBS_STHREADS;
+            pre[r] = t < k1 - k0 ? __ldg(scanned + k0 + t) : 0;
+        }
+    }
+    for (; tile < ntile; tile += gridDim.x) {  // block-uniform
         const long long d0 = tile * LBS_TILE;
         const long long d1 = min(d0 + LBS_TILE, total + N);
-        const int32_t k0 = __ldg(kpart + tile), k1 = __ldg(kpart + tile + 1);
+        const long long nt = tile + gridDim.x;
+        int32_t k0n = 0, k1n = 0, pren[PRE];
+        if (nt < ntile) {
+            k0n = __ldg(kpart + nt);
+            k1n = __ldg(kpart + nt + 1);
+        }
         const int32_t i0 = (int32_t)(d0 - k0);  // first slot of the tile (total <= INT32_MAX)
         const int nb = k1 - k0, ns = (int)(d1 - d0) - nb;
         const int32_t a = i0 - ((i0 + ra) & 3);  // 16-byte aligned base slot
         const int sh = i0 - a;                    // the tile's slots are positions [sh, sh + ns)
 #pragma unroll
         for (int i = 0; i < 16; ++i) s_mark[base + i] = INT_MIN;
+#pragma unroll
+        for (int r = 0; r < PRE; ++r) {  // the next tile's offsets (its endpoints are in flight)
+            const int t = threadIdx.x + r * LBS_STHREADS;
+            pren[r] = (nt < ntile && t < k1n - k0n) ? __ldg(scanned + k0n + t) : 0;
+        }
         __syncthreads();
-        for (int t = threadIdx.x; t < nb; t += LBS_STHREADS) {
-            const int p = __ldg(scanned + k0 + t) - a;  // in [sh, sh + ns]
+#pragma unroll
+        for (int r = 0; r < PRE; ++r) {
+            const int t = threadIdx.x + r * LBS_STHREADS;
+            if (t < nb) {
+                const int p = pre[r] - a;  // in [sh, sh + ns]
+                if (p < LBS_SPAN) atomicMax(&s_mark[p + (p >> 4)], k0 + t);
+            }
+        }
+        for (int t = threadIdx.x + PRE * LBS_STHREADS; t < nb; t += LBS_STHREADS) {
+            const int p = __ldg(scanned + k0 + t) - a;
             if (p < LBS_SPAN) atomicMax(&s_mark[p + (p >> 4)], k0 + t);
         }
         __syncthreads();
@@ -301,6 +309,10 @@ __global__ void __launch_bounds__(LBS_STHREADS, 8) lbs_search(const int32_t *__r
             }
         }
         __syncthreads();  // s_mark and s_wmax are reused by the next tile
+        k0 = k0n;
+        k1 = k1n;
+#pragma unroll
+        for (int r = 0; r < PRE; ++r) pre[r] = pren[r];
     }
 }
 
@@ -312,9 +324,8 @@ __global__ void race_and_resolve_kernel(const int32_t *__restrict__ pred, int32_
     winner[i] = race_and_resolve_warp(pred[i] != 0);
 }
 
-// Scratch: the total, the flags, the ticket, one look-back status word per scan
-// tile, then the search tiles' path endpoints (as many as a total of
-// result_capacity slots can need).
+// Scratch: the total, the flags, one sum per scan tile, then the search tiles'
+// path endpoints (as many as a total of result_capacity slots can need).
 constexpr size_t LBS_HEAD = 64;
 size_t lbs_scratch_bytes(int32_t N, int64_t result_capacity)
 {
@@ -325,6 +336,15 @@ size_t lbs_scratch_bytes(int32_t N, int64_t result_capacity)
     return LBS_HEAD + ntiles * sizeof(unsigned long long) + (nsearch + 2) * sizeof(int32_t);
 }
 
+// Device time of the last call on each device: from before the flags are
+// cleared to after the search, CUDA events on the call's stream (the three
+// kernels overlap, so their sum would overstate it).  Calls are serialised by
+// the caller (one scratch area per device).
+static cudaEvent_t g_lbs_ev[128][2];
+static double g_lbs_last_ms[128];
+
+double lbs_last_ms(int device) { return device >= 0 && device < 128 ? g_lbs_last_ms[device] : 0.0; }
+
 void launch_lbs(const int32_t *counts, int32_t N, int32_t *scanned, int32_t *result, int64_t result_capacity,
                 int32_t *total_dev, int64_t *total_host, void *scratch_ptr, size_t scratch_bytes, cudaStream_t st)
 {
@@ -334,30 +354,58 @@ void launch_lbs(const int32_t *counts, int32_t N, int32_t *scanned, int32_t *res
     if (scratch_bytes < lbs_scratch_bytes(N, result_capacity)) throw gu_error(GU_ERR_INTERNAL, "lbs scratch too small");
     char *base = reinterpret_cast<char *>(scratch_ptr);
     long long *tot_d = reinterpret_cast<long long *>(base);
-    int *flags = reinterpret_cast<int *>(base + 8);  // neg, ok, err, ticket
-    unsigned long long *status = reinterpret_cast<unsigned long long *>(base + LBS_HEAD);
-    int32_t *kpart = reinterpret_cast<int32_t *>(status + ntiles);
+    int *flags = reinterpret_cast<int *>(base + 8);  // neg, ok
+    long long *sums = reinterpret_cast<long long *>(base + LBS_HEAD);
+    int32_t *kpart = reinterpret_cast<int32_t *>(sums + ntiles);
     const long long cap = result_capacity < 0 ? 0 : (result_capacity > INT32_MAX ? INT32_MAX : result_capacity);
     const long long nsearch_max = (cap + N + LBS_TILE - 1) / LBS_TILE;
     // both kernels are queued at once; the scan decides on the device whether the
     // search may run, and the host checks the same conditions after one wait
     long long tot = 0;
     int hflags[3] = {0, 0, 0};
+    int dev = 0;
+    GU_CUDA_CHECK(cudaGetDevice(&dev));
+    cudaEvent_t *ev = dev >= 0 && dev < 128 ? g_lbs_ev[dev] : nullptr;
+    if (ev && !ev[0]) {
+        GU_CUDA_CHECK(cudaEventCreate(&ev[0]));
+        GU_CUDA_CHECK(cudaEventCreate(&ev[1]));
+    }
     if (N > 0) {
-        GU_CUDA_CHECK(cudaMemsetAsync(flags, 0, (LBS_HEAD - 8) + (size_t)ntiles * sizeof(unsigned long long), st));
-        lbs_scan_single<<<ntiles, LBS_THREADS, 0, st>>>(counts, N, ntiles, scanned, status, flags + 3, flags, tot_d,
-                                                        flags + 1, flags + 2, total_dev, result_capacity,
-                                                        result ? 1 : 0, kpart, nsearch_max + 2, wait_limit_ns());
-        const int gsearch = (int)std::min<long long>(std::max<long long>(nsearch_max, 1), 4096);
-        lbs_search<<<gsearch, LBS_STHREADS, 0, st>>>(scanned, N, tot_d, flags + 1, kpart, result);
+        if (ev) GU_CUDA_CHECK(cudaEventRecord(ev[0], st));
+        GU_CUDA_CHECK(cudaMemsetAsync(flags, 0, LBS_HEAD - 8, st));
+        lbs_tile_sums<<<ntiles, LBS_THREADS, 0, st>>>(counts, N, sums, flags);
+        cudaLaunchAttribute pdl[1];
+        pdl[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        pdl[0].val.programmaticStreamSerializationAllowed = 1;
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3((unsigned)ntiles);
+        cfg.blockDim = dim3(LBS_THREADS);
+        cfg.stream = st;
+        cfg.attrs = pdl;
+        cfg.numAttrs = 1;
+        GU_CUDA_CHECK(cudaLaunchKernelEx(&cfg, lbs_scan_apply, counts, N, ntiles, (const long long *)sums, scanned,
+                                         (const int *)flags, tot_d, flags + 1, total_dev, (long long)result_capacity,
+                                         result ? 1 : 0, kpart, nsearch_max + 2));
+        static int sms = 0;  // persistent search CTAs: eight per SM, each pipelining its tiles
+        if (!sms) GU_CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        const int gsearch = (int)std::min<long long>(std::max<long long>(nsearch_max, 1), (long long)sms * 8);
+        cfg.gridDim = dim3((unsigned)gsearch);
+        cfg.blockDim = dim3(LBS_STHREADS);
+        GU_CUDA_CHECK(cudaLaunchKernelEx(&cfg, lbs_search, (const int32_t *)scanned, N, (const long long *)tot_d,
+                                         (const int *)(flags + 1), (const int32_t *)kpart, result));
         GU_CUDA_CHECK(cudaGetLastError());
+        if (ev) GU_CUDA_CHECK(cudaEventRecord(ev[1], st));
         GU_CUDA_CHECK(cudaMemcpyAsync(&tot, tot_d, sizeof(long long), cudaMemcpyDeviceToHost, st));
         GU_CUDA_CHECK(cudaMemcpyAsync(hflags, flags, sizeof(hflags), cudaMemcpyDeviceToHost, st));
     } else if (total_dev) {
         GU_CUDA_CHECK(cudaMemsetAsync(total_dev, 0, sizeof(int32_t), st));
     }
     GU_CUDA_CHECK(cudaStreamSynchronize(st));
-    if (hflags[2]) throw gu_error(GU_ERR_TIMEOUT, "a device-side wait exceeded its limit (scan look-back)");
+    if (ev && N > 0) {
+        float ms = 0.f;
+        GU_CUDA_CHECK(cudaEventElapsedTime(&ms, ev[0], ev[1]));
+        g_lbs_last_ms[dev] = ms;
+    }
     if (total_host) *total_host = tot;
     if (hflags[0]) throw gu_error(GU_ERR_INVALID_ARGUMENT, "work counts must be >= 0");
     if (tot > INT32_MAX) throw gu_error(GU_ERR_OVERFLOW, "total work exceeds INT32_MAX (int32 scanned offsets)");

@@ -113,6 +113,7 @@ def lib():
         "gu_power_start": ([ctypes.c_int, ctypes.c_int, ctypes.POINTER(_vp)], ctypes.c_int),
         "gu_power_stop": ([_vp, ctypes.POINTER(ctypes.c_double), _i64p], ctypes.c_int),
         "gu_lbs": ([_vp, ctypes.c_int32, _vp, _vp, ctypes.c_int64, _vp, _i64p, _vp], ctypes.c_int),
+        "gu_lbs_last_ms": ([ctypes.POINTER(ctypes.c_double)], ctypes.c_int),
         "gu_race_and_resolve": ([_vp, ctypes.c_int32, _vp, _vp], ctypes.c_int),
         "gu_server_create": ([ctypes.c_size_t, ctypes.c_int, ctypes.c_int, ctypes.POINTER(_vp)], ctypes.c_int),
         "gu_server_destroy": ([_vp], ctypes.c_int),
@@ -409,6 +410,13 @@ def lbs(counts_dev, scanned_dev, result_dev, total_dev=None, stream=None):
                        total_dev.data_ptr() if total_dev is not None else None, ctypes.byref(tot),
                        _stream_handle(stream)))
     return tot.value
+
+
+def lbs_last_ms():
+    """Device time of the last lbs call on the current device (ms)."""
+    ms = ctypes.c_double()
+    check(lib().gu_lbs_last_ms(ctypes.byref(ms)))
+    return ms.value
 
 
 def race_and_resolve(pred_dev, winners_dev, stream=None):

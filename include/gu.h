@@ -325,6 +325,11 @@ gu_status gu_bfs_many(const gu_search_item *items, int32_t count, void *stream);
 gu_status gu_lbs(const int32_t *counts_dev, int32_t N, int32_t *scanned_dev, int32_t *result_dev,
                  int64_t result_capacity, int32_t *total_dev, int64_t *total_host, void *stream);
 
+/* Device time of the last gu_lbs call on the current device, in ms (CUDA events
+ * around its kernels on the call's stream; 0 before the first call).  A
+ * profiling hook with no reference counterpart. */
+gu_status gu_lbs_last_ms(double *ms);
+
 /* Warp leader election over nwarps groups of 32 predicates: winners_dev[32w+l] =
  * the highest lane of group w whose predicate is non-zero, or l itself if none
  * is.  Exposes race_and_resolve_warp (race_and_resolve.cuh:13-25), the device
