@@ -268,6 +268,35 @@ def edges_and_bytes(torch, dist, deg, n):
     return E_tot, V_tot, alg_bytes
 
 
+def cpu_model():
+    """The host CPU as /proc/cpuinfo names it (x86: model name; Arm: implementer and part codes)."""
+    import platform
+    try:
+        with open("/proc/cpuinfo") as f:
+            info = f.read().splitlines()
+    except OSError:
+        return platform.machine()
+    fields = {}
+    for line in info:
+        if ":" in line:
+            k, v = line.split(":", 1)
+            fields.setdefault(k.strip(), v.strip())
+    if "model name" in fields:
+        return fields["model name"]
+    parts = [f"{k} {fields[k]}" for k in ("CPU implementer", "CPU part") if k in fields]
+    return platform.machine() + (" (" + ", ".join(parts) + ")" if parts else "")
+
+
+def cpu_one_thread(hg, srcs, nsrc=4):
+    """The oracle port on one host thread over the first `nsrc` sources: GTEPS."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    part = np.asarray(srcs[:nsrc])
+    t0 = time.perf_counter()
+    _, scanned = oracle.bfs_multi(hg.R, hg.C, hg.n, part, nthreads=1)
+    return scanned / 2.0 / (time.perf_counter() - t0) / 1e9, len(part)
+
+
 def cpu_sample(hg, srcs, seconds):
     """Oracle port on all host threads over growing source samples until `seconds`."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -316,12 +345,15 @@ def run_reference(args):
     T = sum(times)
     value = sum(edges) / T / 1e9
     sample = f"{per_step} sources per step ({cores} host threads), of the {args.sources} workload sources"
+    v1, n1 = cpu_one_thread(hg, srcs)
     line = {"impl": "reference", "metric": "multi-source BFS GTEPS", "value": value, "unit": "GTEPS",
             "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * T / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
             "data": "synthetic",
             "config": config_of(args, hg),
-            "cpu_baseline": {"value": value, "unit": "GTEPS", "cores": cores, "kind": "port", "sample": sample},
+            "cpu_baseline": {"value": value, "unit": "GTEPS", "cores": cores, "kind": "port", "sample": sample,
+                             "value_1thread": v1, "sample_1thread": f"first {n1} workload sources on one thread",
+                             "cpu_model": cpu_model()},
             "e2e": {"value": value, "unit": "GTEPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -419,9 +451,12 @@ def run_ours(args):
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         e_cpu, t_cpu, nsrc, cores = cpu_sample(hg, srcs, args.cpu_seconds)
+        v1, n1 = cpu_one_thread(hg, srcs)
         cpu = {"value": e_cpu / t_cpu / 1e9, "unit": "GTEPS", "cores": cores, "kind": "port",
                "sample": f"first {nsrc} of the {len(srcs)} workload sources, oracle port of "
-                         f"multi_search_test.cu:17-38 on {cores} host threads, {t_cpu:.1f} s"}
+                         f"multi_search_test.cu:17-38 on {cores} host threads, {t_cpu:.1f} s",
+               "value_1thread": v1, "sample_1thread": f"first {n1} workload sources on one thread",
+               "cpu_model": cpu_model()}
 
     sub = {}
     if rank == 0 and ws == 1 and not (args.kernel_only or args.no_sublines):
