@@ -472,6 +472,7 @@ static void bfs_device(DeviceGraph &g, int variant, const int32_t *sources_dev, 
             opt.beta = g.tune.beta;
             opt.batch_words = g.tune.words;
             opt.max_blocks = g.tune.ctas_per_sm > 0 ? g.sm_count * g.tune.ctas_per_sm : 0;
+            opt.rare_frac = g.tune.rare_frac;
             opt.tuned = true;
         }
     } else if (variant == GU_BFS_AUTO) {
@@ -526,13 +527,14 @@ gu_status gu_graph_autotune(gu_graph g, const int32_t *sources_dev, int32_t k, g
         int32_t *const rows = scratch.rows;
         const cudaStream_t st = scratch.st;
         std::vector<gu_tuning> cand;
-        auto add = [&](int engine, float alpha, float beta, int words, int ctas = 0) {
+        auto add = [&](int engine, float alpha, float beta, int words, int ctas = 0, float rare = MS_RARE_FRAC) {
             gu_tuning t;
             t.engine = engine;
             t.alpha = alpha;
             t.beta = beta;
             t.words = words;
             t.ctas_per_sm = ctas;
+            t.rare_frac = rare;
             t.seconds = 0;
             cand.push_back(t);
         };
@@ -543,6 +545,8 @@ gu_status gu_graph_autotune(gu_graph g, const int32_t *sources_dev, int32_t k, g
         for (int w = wd; w >= 1 && w >= wd / 2; w /= 2) {
             for (const auto &ab : grid) add(GU_ENGINE_BATCHED, ab[0], ab[1], w);
             add(GU_ENGINE_BATCHED, 2.f, 24.f, w, 1);  // half the grid: one CTA per SM
+            add(GU_ENGINE_BATCHED, 2.f, 24.f, w, 0, 0.06f);  // more sources left to the bottom-up parts
+            add(GU_ENGINE_BATCHED, 2.f, 24.f, w, 0, 1.f / 3.f);
         }
         const DeviceGraph::Tuning saved = dg.tune;
         gu_tuning pick{};
@@ -556,6 +560,7 @@ gu_status gu_graph_autotune(gu_graph g, const int32_t *sources_dev, int32_t k, g
                 dg.tune.beta = t.beta;
                 dg.tune.words = t.words;
                 dg.tune.ctas_per_sm = t.ctas_per_sm;
+                dg.tune.rare_frac = t.rare_frac;
                 bool fell_back = false;
                 double best_t = 1e30;
                 for (int rep = 0; rep < 3; ++rep) {
@@ -593,6 +598,7 @@ gu_status gu_graph_autotune(gu_graph g, const int32_t *sources_dev, int32_t k, g
         dg.tune.beta = pick.beta;
         dg.tune.words = pick.words;
         dg.tune.ctas_per_sm = pick.ctas_per_sm;
+        dg.tune.rare_frac = pick.rare_frac;
         if (best) *best = pick;
         if (ntrials) *ntrials = std::min(nt, max_trials);
     });
@@ -617,12 +623,15 @@ gu_status gu_graph_set_tuning(gu_graph g, const gu_tuning *t)
             throw gu_error(GU_ERR_INVALID_ARGUMENT, "batched engine needs alpha, beta > 0 and words 0, 1, 2 or 4");
         if (t->ctas_per_sm < 0 || t->ctas_per_sm > 2)
             throw gu_error(GU_ERR_INVALID_ARGUMENT, "ctas_per_sm must be 0, 1 or 2");
+        if (!(t->rare_frac >= 0.f && t->rare_frac <= 1.f))
+            throw gu_error(GU_ERR_INVALID_ARGUMENT, "rare_frac must be in [0, 1]");
         dg.tune.set = true;
         dg.tune.engine = t->engine;
         dg.tune.alpha = t->alpha;
         dg.tune.beta = t->beta;
         dg.tune.words = t->words;
         dg.tune.ctas_per_sm = t->ctas_per_sm;
+        dg.tune.rare_frac = t->rare_frac;
     });
 }
 

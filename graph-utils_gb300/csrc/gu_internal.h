@@ -128,6 +128,12 @@ struct ChunkMap {
 // 256-byte-aligned int32 arrays in HBM.  RT/CT is the transposed (in-edge)
 // CSR, identical to R/C for undirected graphs.  F (COO source of every CSR
 // entry) is built on first use by the edge-parallel variant.
+// The batched engine's default rare-source fraction (MsOptions::rare_frac).  On
+// R-MAT graphs against 1/3: scale 20 x 512 sources 1.637 -> 1.610 ms, scale 18 x
+// 1024 sources 1.465 -> 1.311 ms (0.06: 1.227), scale 22 x 256 sources 2.82 ->
+// 2.84 ms; gu_graph_autotune also tries 0.06 and 1/3.
+constexpr float MS_RARE_FRAC = 0.15f;
+
 struct DeviceGraph {
     int device = 0;
     int32_t n = 0;
@@ -144,6 +150,7 @@ struct DeviceGraph {
         float alpha = 2.f, beta = 24.f;
         int words = 0;
         int ctas_per_sm = 0;  // batched engine's grid: CTAs per SM (0: as many as fit)
+        float rare_frac = MS_RARE_FRAC;
     } tune;
     void *ctl_host = nullptr;  // pinned copy of the batched engine's control block, written after each launch
     int32_t *ell = nullptr;  // low-degree graphs: neighbours padded to ell_width per vertex (-1), built on first use
@@ -186,8 +193,8 @@ struct MsOptions {
     float gamma = 4.f;    // ... or when frontier out-edges < n / gamma
     // bottom-up levels expand top-down the sources that fewer than this fraction
     // of the CTAs discovered in the previous level (0: none)
-    float rare_frac = 1.f / 3.f;
-    bool tuned = false;  // alpha, beta, words come from the graph's tuning: the GU_MS_* variables do not apply
+    float rare_frac = MS_RARE_FRAC;
+    bool tuned = false;  // alpha, beta, rare_frac, words come from the graph's tuning: the GU_MS_* variables do not apply
     Workspace *ws = nullptr;  // scratch to use (default: the graph's)
     int max_blocks = 0;       // cap on the persistent grid (0: the whole GPU)
     bool timed = true;        // record the graph's launch events

@@ -1974,7 +1974,7 @@ void launch_msbfs(DeviceGraph &g, const int32_t *sources, int32_t k, int32_t *di
     a.alpha = opt.tuned ? opt.alpha : env_float("GU_MS_ALPHA", opt.alpha);
     a.beta = opt.tuned ? opt.beta : env_float("GU_MS_BETA", opt.beta);
     a.gamma = env_float("GU_MS_GAMMA", opt.gamma);
-    a.rare_frac = env_float("GU_MS_RARE", opt.rare_frac);
+    a.rare_frac = opt.tuned ? opt.rare_frac : env_float("GU_MS_RARE", opt.rare_frac);
     int degbits = 1;
     while (degbits < 31 && (1ll << degbits) <= (long long)g.max_degree) ++degbits;
     a.degbits = degbits;

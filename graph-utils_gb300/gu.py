@@ -32,15 +32,17 @@ _vp = ctypes.c_void_p
 class GuTuning(ctypes.Structure):
     """gu_tuning: AUTO's engine choice and its measured kernel time."""
     _fields_ = [("engine", ctypes.c_int32), ("alpha", ctypes.c_float), ("beta", ctypes.c_float),
-                ("words", ctypes.c_int32), ("ctas_per_sm", ctypes.c_int32), ("seconds", ctypes.c_double)]
+                ("words", ctypes.c_int32), ("ctas_per_sm", ctypes.c_int32), ("rare_frac", ctypes.c_float),
+                ("seconds", ctypes.c_double)]
 
 
 ENGINES = {0: "batched", 1: "per-source", 2: "one-cta"}
+RARE_FRAC = 0.15  # the batched engine's default rare-source fraction (gu_tuning.rare_frac)
 
 
 def _tuning_dict(t):
     return {"engine": ENGINES[t.engine], "alpha": float(t.alpha), "beta": float(t.beta), "words": int(t.words),
-            "ctas_per_sm": int(t.ctas_per_sm), "seconds": float(t.seconds)}
+            "ctas_per_sm": int(t.ctas_per_sm), "rare_frac": float(t.rare_frac), "seconds": float(t.seconds)}
 
 
 class GuError(RuntimeError):
@@ -299,7 +301,7 @@ class Graph:
             return
         eng = {v: k for k, v in ENGINES.items()}[tuning["engine"]]
         t = GuTuning(eng, float(tuning.get("alpha", 2.0)), float(tuning.get("beta", 24.0)), int(tuning.get("words", 0)),
-                     int(tuning.get("ctas_per_sm", 0)), 0.0)
+                     int(tuning.get("ctas_per_sm", 0)), float(tuning.get("rare_frac", RARE_FRAC)), 0.0)
         check(lib().gu_graph_set_tuning(self._h, ctypes.byref(t)))
 
     def last_launch(self):

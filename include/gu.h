@@ -232,6 +232,8 @@ typedef struct gu_tuning {
     float alpha, beta;  /* batched engine's direction thresholds */
     int32_t words;      /* batched engine: 64-source words per batch (1, 2 or 4) */
     int32_t ctas_per_sm; /* batched engine: CTAs per SM of its persistent grid (0: as many as fit, or 1, 2) */
+    float rare_frac;    /* batched engine: bottom-up levels expand top-down the sources fewer than this
+                           fraction of the CTAs found in the previous level (0 .. 1; 0: none) */
     double seconds;     /* measured kernel time on the sample (autotune output) */
 } gu_tuning;
 

@@ -307,6 +307,13 @@ def test_autotune_keeps_distances(shape):
     np.testing.assert_array_equal(run_bfs(g, srcs, "auto")[0], ref)
     with pytest.raises(gu.GuError):
         g.set_tuning({"engine": "batched", "alpha": 2.0, "beta": 24.0, "words": 0, "ctas_per_sm": 3})
+    # and the fraction of sources left to top-down in bottom-up levels
+    assert {round(t["rare_frac"], 3) for t in trials if t["engine"] == "batched"} >= {0.06, 0.15, 0.333}
+    for rare in (0.0, 0.06, 1.0):
+        g.set_tuning({"engine": "batched", "alpha": 2.0, "beta": 24.0, "words": 0, "rare_frac": rare})
+        np.testing.assert_array_equal(run_bfs(g, srcs, "auto")[0], ref, err_msg=f"rare_frac {rare}")
+    with pytest.raises(gu.GuError):
+        g.set_tuning({"engine": "batched", "alpha": 2.0, "beta": 24.0, "words": 0, "rare_frac": 1.5})
     g.set_tuning(None)
     np.testing.assert_array_equal(run_bfs(g, srcs, "auto")[0], ref)
 
