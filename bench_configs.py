@@ -547,12 +547,16 @@ def serve_subline(torch, rate=800.0, seconds=1.0, burst=2000):
     random DAGs (n about 2^16) resident on the device, with the C5 request mix (BC of 64-256
     sources): p50 / p99 latency of a Poisson stream at `rate`, and at saturation (`burst`
     requests submitted at once) the served throughput against the same requests issued one
-    synchronous call each."""
+    synchronous call each; both forms run the saturation requests once untimed first."""
     rng = np.random.default_rng(11)
     rmats, dags, comp = _serving_set(torch, 6, (12, 16), 2, (16, 16.5), rng)
     plan = _serving_plan(rng, rmats, dags, rate, seconds, 256)
-    lat = _serve_stream(plan, comp)
     sat_plan = [(0.0,) + p[1:] for p in _serving_plan(rng, rmats, dags, float(burst), 1.0, 256)[:burst]]
+    # warm-up, untimed: the first pass of a process through the server and the one-call
+    # form ran at about 70 % of later passes (5220 / 1363 against 7550 / 1740 requests/s)
+    _serve_stream(sat_plan, comp)
+    _one_call_per_request(torch, sat_plan, comp)
+    lat = _serve_stream(plan, comp)
     sat = _serve_stream(sat_plan, comp)
     plain = _one_call_per_request(torch, sat_plan, comp)
     for _, _, g in rmats + dags:
