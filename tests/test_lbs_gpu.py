@@ -37,7 +37,10 @@ def test_lbs_golden(name):
     np.testing.assert_array_equal(result, g["result"])
 
 
-@pytest.mark.parametrize("seed,N,hi", [(1, 1_000_003, 8), (2, 50_000, 2000), (3, 4097, 1), (4, 123_457, 0)])
+# 6,000,017 counts are 733 scan tiles: more CTAs than the GPU holds at once, so the
+# dependent launches start only after the scan's last CTAs have begun
+@pytest.mark.parametrize("seed,N,hi", [(1, 1_000_003, 8), (2, 50_000, 2000), (3, 4097, 1), (4, 123_457, 0),
+                                       (5, 6_000_017, 3)])
 def test_lbs_random_vs_oracle(seed, N, hi):
     rng = np.random.default_rng(seed)
     counts = rng.integers(0, hi + 1, N).astype(np.int32)
@@ -47,6 +50,28 @@ def test_lbs_random_vs_oracle(seed, N, hi):
     assert total == rt
     np.testing.assert_array_equal(scanned, rs)
     np.testing.assert_array_equal(result, rr)
+
+
+@pytest.mark.parametrize("c_off,s_off,r_off", [(1, 0, 0), (0, 3, 1), (3, 1, 2), (2, 2, 3)])
+def test_lbs_unaligned_views(c_off, s_off, r_off):
+    """Counts, scanned and result as views at element offsets from their buffers'
+    16-byte-aligned starts: the owners' 16-byte stores realign to the result
+    buffer, and nothing outside the views is written."""
+    rng = np.random.default_rng(10 + c_off + 4 * r_off)
+    N = 70_001
+    counts = rng.integers(0, 6, N).astype(np.int32)
+    total = int(counts.sum())
+    cbuf = torch.zeros(N + 8, dtype=torch.int32, device="cuda")
+    cbuf[c_off:c_off + N] = torch.as_tensor(counts, device="cuda")
+    sbuf = torch.full((N + 8,), -5, dtype=torch.int32, device="cuda")
+    rbuf = torch.full((total + 8,), -5, dtype=torch.int32, device="cuda")
+    t = gu.lbs(cbuf[c_off:c_off + N], sbuf[s_off:s_off + N], rbuf[r_off:r_off + total])
+    rs, rr, rt = oracle.lbs(counts)
+    assert t == rt == total
+    np.testing.assert_array_equal(sbuf[s_off:s_off + N].cpu().numpy(), rs)
+    np.testing.assert_array_equal(rbuf[r_off:r_off + total].cpu().numpy(), rr)
+    assert bool((sbuf[:s_off] == -5).all()) and bool((sbuf[s_off + N:] == -5).all())
+    assert bool((rbuf[:r_off] == -5).all()) and bool((rbuf[r_off + total:] == -5).all())
 
 
 def test_lbs_grid_degree_array():
