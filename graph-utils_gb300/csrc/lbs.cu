@@ -386,7 +386,8 @@ void launch_lbs(const int32_t *counts, int32_t N, int32_t *scanned, int32_t *res
         GU_CUDA_CHECK(cudaLaunchKernelEx(&cfg, lbs_scan_apply, counts, N, ntiles, (const long long *)sums, scanned,
                                          (const int *)flags, tot_d, flags + 1, total_dev, (long long)result_capacity,
                                          result ? 1 : 0, kpart, nsearch_max + 2));
-        static int sms = 0;  // persistent search CTAs: eight per SM, each pipelining its tiles
+        static int sms_of[128];  // persistent search CTAs: eight per SM, each pipelining its tiles
+        int &sms = sms_of[dev >= 0 && dev < 128 ? dev : 0];
         if (!sms) GU_CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
         const int gsearch = (int)std::min<long long>(std::max<long long>(nsearch_max, 1), (long long)sms * 8);
         cfg.gridDim = dim3((unsigned)gsearch);
