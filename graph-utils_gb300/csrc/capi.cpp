@@ -694,6 +694,10 @@ gu_status gu_bfs_host(gu_graph g, int variant, const int32_t *sources_host, int3
         // chunk's rows are copied on the graph's copy stream once its search has
         // finished.  The host link, not the search, then bounds the call.
         if (!dg.copy_st) GU_CUDA_CHECK(cudaStreamCreateWithFlags(&dg.copy_st, cudaStreamNonBlocking));
+        struct CopyFence {  // no copy into the caller's rows outlives the call, errors included
+            cudaStream_t s;
+            ~CopyFence() { cudaStreamSynchronize(s); }
+        } fence{dg.copy_st};
         const size_t row = sizeof(int32_t) * (size_t)dg.n;
         int32_t b = 0;
         while (b < k) {
