@@ -172,3 +172,34 @@ def test_wait_limit_and_alloc_hook_arguments_on_the_host():
         assert L.gu_choose_device(-1, ctypes.byref(chosen)) == 2  # GU_ERR_CUDA, no exit()
         assert chosen.value == -7
         assert L.gu_last_error()
+
+
+def test_ctypes_structs_match_the_c_header(tmp_path):
+    """gu.py's ctypes mirrors of the C structs (gu_tuning, gu_search_item) have the
+    header's size and field offsets, as gcc lays them out from include/gu.h."""
+    import ctypes
+    import shutil
+    import subprocess
+    if shutil.which("gcc") is None:
+        pytest.skip("gcc absent")
+    structs = {"gu_tuning": gu.GuTuning, "gu_search_item": gu.SearchItem}
+    lines = ["#include <stddef.h>", "#include <stdio.h>", '#include "gu.h"', "int main(void) {"]
+    for cname, py in structs.items():
+        lines.append(f'  printf("{cname} size %zu\\n", sizeof({cname}));')
+        for fname, _ in py._fields_:
+            lines.append(f'  printf("{cname} {fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    r = subprocess.run(["gcc", "-std=c11", "-I" + os.path.join(ROOT, "include"), "-I/usr/local/cuda/include",
+                        str(src), "-o", str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    got = {}
+    for line in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.splitlines():
+        cname, field, value = line.split()
+        got[(cname, field)] = int(value)
+    for cname, py in structs.items():
+        assert got[(cname, "size")] == ctypes.sizeof(py), cname
+        for fname, _ in py._fields_:
+            assert got[(cname, fname)] == getattr(py, fname).offset, (cname, fname)
