@@ -62,3 +62,39 @@ def test_both_arms_print_the_same_config():
 
 def test_cpu_model_names_the_host():
     assert isinstance(bench.cpu_model(), str) and bench.cpu_model()
+
+
+def test_serving_plan_mix_and_ranges():
+    """The serving workload's requests: Poisson arrivals, 60 % BFS rows of 1-256
+    sources, 20 % BC of 64..bc_max sources, 20 % DAG reachability of 1-256
+    sources, distinct in-range sources, the same plan for the same seed."""
+    np = pytest.importorskip("numpy")
+    import bench_configs
+    import gu
+
+    class G:
+        def __init__(self, n):
+            self.n = n
+    rmats = [("r0", G(5000), None), ("r1", G(9000), None)]
+    dags = [("d0", G(7000), None)]
+    plan = bench_configs._serving_plan(np.random.default_rng(4), rmats, dags, 4000.0, 1.0, 512)
+    again = bench_configs._serving_plan(np.random.default_rng(4), rmats, dags, 4000.0, 1.0, 512)
+    assert len(plan) == len(again) and all(a[0] == b[0] and a[1] == b[1] and np.array_equal(a[4], b[4])
+                                           for a, b in zip(plan, again))
+    assert 3600 < len(plan) < 4400
+    times = [p[0] for p in plan]
+    assert all(b >= a for a, b in zip(times, times[1:]))
+    kinds = [p[1] for p in plan]
+    share = {q: kinds.count(q) / len(plan) for q in (gu.QUERY_BFS, gu.QUERY_BC, gu.QUERY_REACH)}
+    assert abs(share[gu.QUERY_BFS] - 0.6) < 0.04 and abs(share[gu.QUERY_BC] - 0.2) < 0.03
+    assert abs(share[gu.QUERY_REACH] - 0.2) < 0.03
+    for t, q, hg, g, srcs in plan:
+        lo, hi = (64, 512) if q == gu.QUERY_BC else (1, 256)
+        assert lo <= len(srcs) <= hi
+        assert srcs.dtype == np.int32 and len(np.unique(srcs)) == len(srcs)
+        assert srcs.min() >= 0 and srcs.max() < hg.n
+        assert (hg in [r[1] for r in dags]) == (q == gu.QUERY_REACH)
+    # result sizes: BFS rows, one BC vector, one count per source
+    assert bench_configs._out_bytes(gu.QUERY_BFS, G(100), np.arange(3)) == 3 * 100 * 4
+    assert bench_configs._out_bytes(gu.QUERY_BC, G(100), np.arange(3)) == 100 * 8
+    assert bench_configs._out_bytes(gu.QUERY_REACH, G(100), np.arange(3)) == 3 * 8
