@@ -78,6 +78,7 @@ def test_lbs_grid_degree_array():
     hg = gu.HostGraph.grid(2048, 2048, 0.05, seed=7)
     counts = np.diff(hg.R).astype(np.int32)
     scanned, result, total, _ = run_lbs(counts)
+    assert 0.0 < gu.lbs_last_ms() < 100.0  # the call's device time (events around its kernels)
     rs, rr, rt = oracle.lbs(counts)
     assert total == rt == hg.m
     np.testing.assert_array_equal(scanned, rs)
